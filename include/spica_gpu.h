@@ -1,0 +1,148 @@
+/* spica_gpu.h -- C ABI of the GB300 path-tracing library (libspica_gpu.so).
+ *
+ * This is the drop-in boundary for the reference renderer's hot path.  Plain C:
+ * pointers, sizes and status codes only.  Every call returns 0 on success or a
+ * negative status; spgpu_last_error() gives the message of the last failure on the
+ * calling thread (the reference aborts through Assertion/FatalError instead,
+ * core/common.h:69-115; a C++ plugin wrapper turns a negative status into FatalError).
+ *
+ * One context = one device + one scene + its BVH.  A context is used by one host
+ * thread at a time.  "device pointer" arguments are CUDA device memory (for example
+ * a torch tensor's data_ptr); "host" entry points take host memory and copy both
+ * ways themselves.  `stream` is a cudaStream_t passed as void* (NULL = the context's
+ * own stream).
+ */
+#ifndef SPICA_GPU_H
+#define SPICA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct spgpu_ctx spgpu_ctx;
+
+/* status codes */
+#define SPGPU_OK 0
+#define SPGPU_EINVAL (-1)     /* bad argument */
+#define SPGPU_EBUILD (-2)     /* BVH build failed (see message) */
+#define SPGPU_ECUDA (-3)      /* CUDA runtime error */
+#define SPGPU_ENOMEM (-4)     /* device allocation failed */
+#define SPGPU_ESTATE (-5)     /* call order: no scene / no BVH yet */
+#define SPGPU_EKERNEL (-6)    /* a kernel reported an error (stack overflow, bounded wait expired) */
+
+/* material records: 8 floats, [0] = type; the same records the reference's
+ * Diffuse, RoughConductor ("ggx", no roughness remap) and Dielectric plugins take
+ * (bsdfs/diffuse.cc:23, bsdfs/roughconductor.cc:38, bsdfs/dielectric.cc:30) */
+#define SPGPU_MAT_LAMBERT 0    /* [1..3] reflectance */
+#define SPGPU_MAT_CONDUCTOR 1  /* [1] alpha, [2..4] eta, [5..7] k */
+#define SPGPU_MAT_DIELECTRIC 2 /* [1] interior IOR */
+
+typedef struct {
+    int device;          /* CUDA device ordinal */
+    int reserved[7];
+} spgpu_config;
+
+typedef struct {
+    int64_t triangles;
+    int64_t wide_nodes;
+    int32_t depth;       /* wide-node levels */
+    int32_t lights;      /* area-light triangles + environment map */
+    double build_ms;     /* last spgpu_build_bvh, device time */
+    float bounds[6];     /* scene box lo.xyz, hi.xyz */
+} spgpu_bvh_info;
+
+/* Closest-hit result, 16 bytes: t along the unit direction, primitive index
+ * (-1 = miss), barycentrics u, v of the reference's Moller-Trumbore test
+ * (core/triangle.cc:98). */
+typedef struct {
+    float t;
+    int32_t prim;
+    float u, v;
+} spgpu_hit;
+
+/* Traversal counters of the last spgpu_trace_stats call: mean nodes and triangles
+ * visited per ray (used for the roofline's algorithmic bytes). */
+typedef struct {
+    int64_t rays;
+    double nodes_per_ray;
+    double tris_per_ray;
+} spgpu_trace_counters;
+
+/* Render request.  camera = eye[3], look[3], up[3], vertical fov in degrees: the
+ * reference's PerspectiveCamera with Transform::lookAt (cameras/perspective.cc:36,
+ * core/transform.cc:167).  Samples sample_offset .. sample_offset+spp-1 of every
+ * pixel are traced; the film is accumulated, not cleared. */
+typedef struct {
+    float camera[10];
+    int32_t width, height;
+    int32_t spp;
+    int32_t sample_offset;
+    int32_t max_depth;   /* the reference's "maxDepth" render parameter */
+    uint32_t seed;
+    int32_t reserved[4];
+} spgpu_render_desc;
+
+typedef struct {
+    int64_t paths;             /* camera paths traced */
+    int64_t rays_closest;      /* camera + continuation rays */
+    int64_t rays_shadow;       /* light-sample and MIS-connection rays (any hit) */
+    double ms;                 /* device time of the call */
+} spgpu_render_stats;
+
+/* ---- context ----------------------------------------------------------------- */
+/* replaces: PluginManager::createObject / createAccelerator (core/cobject.cc:60,68) */
+int spgpu_create(const spgpu_config *cfg, spgpu_ctx **out);
+void spgpu_destroy(spgpu_ctx *ctx);
+const char *spgpu_last_error(void);
+const char *spgpu_version(void);
+
+/* ---- scene (host pointers) ------------------------------------------------------
+ * replaces: the primitive vector handed to the accelerator plugin's createInstance
+ * (core/cobject.h:66-75) and Scene(accel, lights) (core/scene.h:25-30).
+ * verts: ntri*9 floats (p0, p1, p2); tri_mat: material index per triangle;
+ * materials: nmat*8 floats; tri_emit: ntri*3 floats (zero = not an emitter, else a
+ * one-sided AreaLight, lights/area.cc:29), may be NULL; env: env_w*env_h*3 floats, a
+ * lat-long map whose row 0 is the +z pole (lights/envmap.cc:17), may be NULL. */
+int spgpu_upload_scene(spgpu_ctx *ctx, int32_t ntri, const float *verts, const int32_t *tri_mat, int32_t nmat,
+                       const float *materials, const float *tri_emit, int32_t env_w, int32_t env_h,
+                       const float *env);
+
+/* replaces: Accelerator::construct() (core/accelerator.h:35; BVHAccel::construct,
+ * accelerators/bvh.cc:139) -- builds the compressed 8-wide BVH on the device. */
+int spgpu_build_bvh(spgpu_ctx *ctx);
+int spgpu_bvh_stats(spgpu_ctx *ctx, spgpu_bvh_info *out);
+
+/* ---- ray batches ----------------------------------------------------------------
+ * replaces: Primitive::intersect(Ray&, SurfaceInteraction*) and intersect(Ray&)
+ * of the accelerator (core/primitive.h:22-23; BVHAccel::intersect,
+ * accelerators/bvh.cc:315-329) for n rays at once.
+ * org_tmin, dir_tmax: n float4 (16-byte aligned) -- origin + tmin, unit direction +
+ * tmax (the reference's ray.maxDist).  Closest: out = n spgpu_hit.  Any: out = n
+ * uint32 (1 = occluded). */
+int spgpu_trace(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out,
+                void *stream);                                                       /* device pointers */
+int spgpu_trace_host(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
+                     void *out);                                                     /* host pointers   */
+/* same as spgpu_trace on device pointers, counting node and triangle visits */
+int spgpu_trace_stats(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
+                      void *out, spgpu_trace_counters *counters);
+
+/* ---- rendering -------------------------------------------------------------------
+ * replaces: Integrator::render(camera, scene, params) of the path integrator plugin
+ * (core/integrator.h:34; SamplerIntegrator::render, core/integrator.cc:46, with
+ * PathIntegrator::Li, integrators/path/path.cc:42).
+ * film: width*height float4 (sum r, g, b, sample count) in the reference film's
+ * pixel order (x mirrored, core/integrator.cc:88); accumulated in place. */
+int spgpu_render(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, spgpu_render_stats *stats,
+                 void *stream);                                                      /* device film */
+int spgpu_render_host(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film,
+                      spgpu_render_stats *stats);                                    /* host film   */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPICA_GPU_H */

@@ -1,0 +1,506 @@
+// bvh.cu -- device build of the compressed 8-wide BVH.
+//
+// Replaces the reference's serial binary SAH build (accelerators/bvh.cc:150-237,
+// BVHAccel::constructRec) with a data-parallel one on the GPU:
+//   1. per-triangle bounds and centroid bounds              (k_prim_bounds)
+//   2. 63-bit Morton codes of the centroids, radix sort     (k_morton + cub)
+//   3. binary radix tree over the sorted codes              (k_karras)
+//      -- Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees,
+//         and k-d Trees" (HPG 2012)
+//   4. bottom-up bounds refit with arrival counters         (k_refit)
+//   5. top-down collapse into 8-wide nodes, level by level  (k_collapse)
+//      each wide node takes its binary node's two children and repeatedly opens
+//      the internal child of largest surface area until it has 8 children;
+//      children of at most 3 triangles that are left over become leaves.
+//      Children are placed in slots by a greedy octant assignment so that the
+//      traversal's slot order s ^ (7 - octant) runs roughly front to back, their
+//      boxes are quantised conservatively to 8 bits on the node's grid, and leaf
+//      triangles are copied into leaf order as (v0, e1, e2) records.
+// The triangle set, and so the closest hit of every ray, is the reference's; only
+// the tree differs.  Its build is deterministic (no atomics decide structure).
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "bvh.cuh"
+
+namespace spgpu {
+
+namespace {
+
+constexpr int kLeafMax = 3;   // triangles a wide-node leaf may hold
+
+__device__ __forceinline__ void atomicMinFloat(float *a, float v) {
+    if (v >= 0.0f) atomicMin(reinterpret_cast<int *>(a), __float_as_int(v));
+    else atomicMax(reinterpret_cast<unsigned int *>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomicMaxFloat(float *a, float v) {
+    if (v >= 0.0f) atomicMax(reinterpret_cast<int *>(a), __float_as_int(v));
+    else atomicMin(reinterpret_cast<unsigned int *>(a), __float_as_uint(v));
+}
+
+// scene bounds [0..5] and centroid bounds [6..11]
+__global__ void k_prim_bounds(const float *__restrict__ verts, int n, float *__restrict__ bounds) {
+    float lo[6], hi[6];
+    for (int k = 0; k < 6; k++) {
+        lo[k] = 3.0e38f;
+        hi[k] = -3.0e38f;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float *v = verts + 9 * static_cast<int64_t>(i);
+        for (int a = 0; a < 3; a++) {
+            const float mn = fminf(v[a], fminf(v[3 + a], v[6 + a]));
+            const float mx = fmaxf(v[a], fmaxf(v[3 + a], v[6 + a]));
+            lo[a] = fminf(lo[a], mn);
+            hi[a] = fmaxf(hi[a], mx);
+            const float c = 0.5f * (mn + mx);
+            lo[3 + a] = fminf(lo[3 + a], c);
+            hi[3 + a] = fmaxf(hi[3 + a], c);
+        }
+    }
+    for (int k = 0; k < 6; k++) {
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; a++) {
+            atomicMinFloat(&bounds[a], lo[a]);
+            atomicMaxFloat(&bounds[3 + a], hi[a]);
+            atomicMinFloat(&bounds[6 + a], lo[3 + a]);
+            atomicMaxFloat(&bounds[9 + a], hi[3 + a]);
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t spread21(uint32_t x) {
+    uint64_t v = x & 0x1FFFFFu;
+    v = (v | (v << 32)) & 0x1F00000000FFFFull;
+    v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+__global__ void k_morton(const float *__restrict__ verts, int n, const float *__restrict__ bounds,
+                         uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *v = verts + 9 * static_cast<int64_t>(i);
+    uint32_t q[3];
+    for (int a = 0; a < 3; a++) {
+        const float c = 0.5f * (fminf(v[a], fminf(v[3 + a], v[6 + a])) + fmaxf(v[a], fmaxf(v[3 + a], v[6 + a])));
+        const float lo = bounds[6 + a], ext = bounds[9 + a] - bounds[6 + a];
+        const float u = ext > 0.0f ? (c - lo) / ext : 0.5f;
+        q[a] = static_cast<uint32_t>(fminf(fmaxf(u * 2097152.0f, 0.0f), 2097151.0f));
+    }
+    keys[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    vals[i] = static_cast<uint32_t>(i);
+}
+
+// common prefix length of sorted keys i, j (index tie-break for equal keys)
+__device__ __forceinline__ int delta(const uint64_t *__restrict__ k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = k[i], b = k[j];
+    if (a == b) return 64 + __clz(static_cast<uint32_t>(i ^ j));
+    return __clzll(a ^ b);
+}
+
+// internal nodes 0..n-2, leaf j is node n-1+j
+__global__ void k_karras(const uint64_t *__restrict__ keys, int n, int2 *__restrict__ child, int *__restrict__ parent,
+                         int2 *__restrict__ range) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int dir = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, n, i, i - dir);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * dir) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * dir) > dmin) l += t;
+    const int j = i + l * dir;
+    const int dnode = delta(keys, n, i, j);
+    int s = 0;
+    int div = 2;
+    int t;
+    do {
+        t = (l + div - 1) / div;
+        if (delta(keys, n, i, i + (s + t) * dir) > dnode) s += t;
+        div <<= 1;
+    } while (t > 1);
+    const int gamma = i + s * dir + min(dir, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
+    const int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
+    child[i] = make_int2(left, right);
+    range[i] = make_int2(lo, hi);
+    parent[left] = i;
+    parent[right] = i;
+}
+
+__global__ void k_refit(const float *__restrict__ verts, const uint32_t *__restrict__ order, int n,
+                        const int2 *__restrict__ child, const int *__restrict__ parent, float4 *bmin, float4 *bmax,
+                        int *flags) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const float *v = verts + 9 * static_cast<int64_t>(order[j]);
+    int node = n - 1 + j;
+    bmin[node] = make_float4(fminf(v[0], fminf(v[3], v[6])), fminf(v[1], fminf(v[4], v[7])),
+                             fminf(v[2], fminf(v[5], v[8])), 0.0f);
+    bmax[node] = make_float4(fmaxf(v[0], fmaxf(v[3], v[6])), fmaxf(v[1], fmaxf(v[4], v[7])),
+                             fmaxf(v[2], fmaxf(v[5], v[8])), 0.0f);
+    __threadfence();
+    if (n == 1) return;
+    int p = parent[node];
+    while (true) {
+        if (atomicAdd(&flags[p], 1) == 0) return;   // the sibling finishes this node
+        __threadfence();
+        const int2 c = child[p];
+        const float4 a0 = __ldcg(&bmin[c.x]), a1 = __ldcg(&bmax[c.x]);
+        const float4 b0 = __ldcg(&bmin[c.y]), b1 = __ldcg(&bmax[c.y]);
+        __stcg(&bmin[p], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f));
+        __stcg(&bmax[p], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f));
+        __threadfence();
+        if (p == 0) return;
+        p = parent[p];
+    }
+}
+
+__device__ __forceinline__ float areaOf(float4 lo, float4 hi) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+struct CollapseArgs {
+    const float *verts;
+    const uint32_t *order;
+    const int *tri_mat;
+    const int *tri_light;
+    int n;
+    const int2 *child;
+    const int2 *range;
+    const float4 *bmin;
+    const float4 *bmax;
+    WideNode *nodes;
+    TriRecord *tris;
+    int2 *slot_shade;
+    int *counters;   // [0] wide nodes allocated, [1] triangles placed, [2] next-level items
+};
+
+__device__ __forceinline__ void nodeRange(const CollapseArgs &A, int b, int *first, int *count) {
+    if (b >= A.n - 1) {
+        *first = b - (A.n - 1);
+        *count = 1;
+    } else {
+        const int2 r = A.range[b];
+        *first = r.x;
+        *count = r.y - r.x + 1;
+    }
+}
+
+// one thread per wide node of the current level; items are (binary node, wide node)
+__global__ void k_collapse(CollapseArgs A, const int2 *__restrict__ items, int nitems, int2 *__restrict__ next) {
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nitems) return;
+    const int b = items[it].x, w = items[it].y;
+    const bool rootLeaf = b >= A.n - 1;   // single-triangle scene
+    int C[8];
+    int nc = 0;
+    if (rootLeaf) {
+        C[nc++] = b;
+    } else {
+        C[nc++] = A.child[b].x;
+        C[nc++] = A.child[b].y;
+        while (nc < 8) {
+            int best = -1;
+            float bestA = -1.0f;
+            for (int k = 0; k < nc; k++) {
+                if (C[k] < A.n - 1) {
+                    const float a = areaOf(A.bmin[C[k]], A.bmax[C[k]]);
+                    if (a > bestA) {
+                        bestA = a;
+                        best = k;
+                    }
+                }
+            }
+            if (best < 0) break;
+            const int2 cc = A.child[C[best]];
+            C[best] = cc.x;
+            C[nc++] = cc.y;
+        }
+    }
+    // node box
+    float3 lo = mk(3.0e38f, 3.0e38f, 3.0e38f), hi = mk(-3.0e38f, -3.0e38f, -3.0e38f);
+    for (int k = 0; k < nc; k++) {
+        lo = fminf3(lo, xyz(A.bmin[C[k]]));
+        hi = fmaxf3(hi, xyz(A.bmax[C[k]]));
+    }
+    const float3 ctr = (lo + hi) * 0.5f;
+    // greedy slot assignment: child whose centroid offset lies in octant o prefers slot o
+    int slotOf[8];
+    bool usedSlot[8] = {false, false, false, false, false, false, false, false};
+    bool done[8] = {false, false, false, false, false, false, false, false};
+    float cost[8][8];
+    for (int k = 0; k < nc; k++) {
+        const float3 c = (xyz(A.bmin[C[k]]) + xyz(A.bmax[C[k]])) * 0.5f - ctr;
+        for (int s = 0; s < 8; s++) {
+            const float3 sg = mk((s & 1) ? -1.0f : 1.0f, (s & 2) ? -1.0f : 1.0f, (s & 4) ? -1.0f : 1.0f);
+            cost[k][s] = -dot(c, sg);
+        }
+    }
+    for (int r = 0; r < nc; r++) {
+        float bc = 3.0e38f;
+        int bk = -1, bs = -1;
+        for (int k = 0; k < nc; k++) {
+            if (done[k]) continue;
+            for (int s = 0; s < 8; s++) {
+                if (usedSlot[s]) continue;
+                if (cost[k][s] < bc) {
+                    bc = cost[k][s];
+                    bk = k;
+                    bs = s;
+                }
+            }
+        }
+        done[bk] = true;
+        usedSlot[bs] = true;
+        slotOf[bk] = bs;
+    }
+    // classify children: internal (wide node) or leaf (<= 3 triangles)
+    int slotChild[8];
+    for (int s = 0; s < 8; s++) slotChild[s] = -1;
+    for (int k = 0; k < nc; k++) slotChild[slotOf[k]] = C[k];
+    uint32_t imask = 0;
+    int nInt = 0, nTri = 0;
+    for (int s = 0; s < 8; s++) {
+        const int c = slotChild[s];
+        if (c < 0) continue;
+        int first, count;
+        nodeRange(A, c, &first, &count);
+        if (count > kLeafMax) {
+            imask |= 1u << s;
+            nInt++;
+        } else {
+            nTri += count;
+        }
+    }
+    const int childBase = nInt ? atomicAdd(&A.counters[0], nInt) : 0;
+    const int triBase = nTri ? atomicAdd(&A.counters[1], nTri) : 0;
+    const int itemBase = nInt ? atomicAdd(&A.counters[2], nInt) : 0;
+
+    WideNode node;
+    node.px = lo.x;
+    node.py = lo.y;
+    node.pz = lo.z;
+    int e[3];
+    const float ext[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+    for (int a = 0; a < 3; a++) {
+        int ex = -126;
+        if (ext[a] > 0.0f) {
+            frexpf(ext[a] / 255.0f, &ex);   // ext/255 = m 2^ex, m in [0.5, 1)
+            ex = max(ex, -126);
+            for (int g = 0; g < 4 && ldexpf(255.0f, ex) < ext[a]; g++) ex++;
+        }
+        e[a] = ex;
+    }
+    node.ex = static_cast<uint8_t>(e[0] + 127);
+    node.ey = static_cast<uint8_t>(e[1] + 127);
+    node.ez = static_cast<uint8_t>(e[2] + 127);
+    node.imask = static_cast<uint8_t>(imask);
+    node.child_base = static_cast<uint32_t>(childBase);
+    node.tri_base = static_cast<uint32_t>(triBase);
+    const double p[3] = {lo.x, lo.y, lo.z};
+    int rank = 0, triOff = 0;
+    for (int s = 0; s < 8; s++) {
+        const int c = slotChild[s];
+        if (c < 0) {
+            node.meta[s] = 0;
+            node.qlo_x[s] = node.qlo_y[s] = node.qlo_z[s] = 0;
+            node.qhi_x[s] = node.qhi_y[s] = node.qhi_z[s] = 0;
+            continue;
+        }
+        const float4 cl = A.bmin[c], ch = A.bmax[c];
+        const double clo[3] = {cl.x, cl.y, cl.z}, chi[3] = {ch.x, ch.y, ch.z};
+        uint8_t ql[3], qh[3];
+        for (int a = 0; a < 3; a++) {
+            const double sc = ldexp(1.0, e[a]);
+            double l = floor((clo[a] - p[a]) / sc), h = ceil((chi[a] - p[a]) / sc);
+            l = fmin(fmax(l, 0.0), 255.0);
+            h = fmin(fmax(h, 0.0), 255.0);
+            ql[a] = static_cast<uint8_t>(l);
+            qh[a] = static_cast<uint8_t>(h);
+        }
+        node.qlo_x[s] = ql[0];
+        node.qlo_y[s] = ql[1];
+        node.qlo_z[s] = ql[2];
+        node.qhi_x[s] = qh[0];
+        node.qhi_y[s] = qh[1];
+        node.qhi_z[s] = qh[2];
+        if (imask & (1u << s)) {
+            node.meta[s] = static_cast<uint8_t>(0x20 | (24 + s));
+            next[itemBase + rank] = make_int2(c, childBase + rank);
+            rank++;
+        } else {
+            int first, count;
+            nodeRange(A, c, &first, &count);
+            node.meta[s] = static_cast<uint8_t>((((1u << count) - 1u) << 5) | static_cast<uint32_t>(triOff));
+            for (int q = 0; q < count; q++) {
+                const uint32_t prim = A.order[first + q];
+                const float *v = A.verts + 9 * static_cast<int64_t>(prim);
+                TriRecord r;
+                r.v0 = make_float4(v[0], v[1], v[2], __int_as_float(static_cast<int>(prim)));
+                r.e1 = make_float4(v[3] - v[0], v[4] - v[1], v[5] - v[2], 0.0f);
+                r.e2 = make_float4(v[6] - v[0], v[7] - v[1], v[8] - v[2], 0.0f);
+                A.tris[triBase + triOff + q] = r;
+                A.slot_shade[triBase + triOff + q] =
+                    make_int2(A.tri_mat ? A.tri_mat[prim] : 0, A.tri_light ? A.tri_light[prim] : -1);
+            }
+            triOff += count;
+        }
+    }
+    A.nodes[w] = node;
+}
+
+template <class T>
+T *dalloc(size_t n) {
+    T *p = nullptr;
+    if (cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) return nullptr;
+    return p;
+}
+
+}  // namespace
+
+void freeWideBVH(DeviceBVH *b) {
+    cudaFree(b->nodes);
+    cudaFree(b->tris);
+    cudaFree(b->slot_shade);
+    *b = DeviceBVH{};
+}
+
+int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d_tri_light, DeviceBVH *out,
+                 cudaStream_t stream, char *err, size_t errlen) {
+    freeWideBVH(out);
+    if (n <= 0) {
+        snprintf(err, errlen, "buildWideBVH: empty scene");
+        return -2;
+    }
+    const int nNodes = 2 * n - 1;
+    float *d_bounds = dalloc<float>(12);
+    uint64_t *keys[2] = {dalloc<uint64_t>(n), dalloc<uint64_t>(n)};
+    uint32_t *vals[2] = {dalloc<uint32_t>(n), dalloc<uint32_t>(n)};
+    int2 *child = dalloc<int2>(n);
+    int2 *range = dalloc<int2>(n);
+    int *parent = dalloc<int>(nNodes);
+    int *flags = dalloc<int>(n);
+    float4 *bmin = dalloc<float4>(nNodes);
+    float4 *bmax = dalloc<float4>(nNodes);
+    int2 *items[2] = {dalloc<int2>(n), dalloc<int2>(n)};
+    int *counters = dalloc<int>(4);
+    out->nodes = dalloc<WideNode>(n);
+    out->tris = dalloc<TriRecord>(n);
+    out->slot_shade = dalloc<int2>(n);
+    int rc = 0;
+    void *tmp = nullptr;
+    size_t tmpBytes = 0;
+    auto fail = [&](const char *what, cudaError_t e) {
+        snprintf(err, errlen, "buildWideBVH: %s: %s", what, cudaGetErrorString(e));
+        rc = -3;
+    };
+    if (!d_bounds || !keys[0] || !keys[1] || !vals[0] || !vals[1] || !child || !range || !parent || !flags ||
+        !bmin || !bmax || !items[0] || !items[1] || !counters || !out->nodes || !out->tris || !out->slot_shade) {
+        snprintf(err, errlen, "buildWideBVH: device allocation failed for %d triangles", n);
+        rc = -4;
+    }
+    if (rc == 0) {
+        const float init[12] = {3e38f, 3e38f, 3e38f, -3e38f, -3e38f, -3e38f,
+                                3e38f, 3e38f, 3e38f, -3e38f, -3e38f, -3e38f};
+        cudaMemcpyAsync(d_bounds, init, sizeof(init), cudaMemcpyHostToDevice, stream);
+        cudaMemsetAsync(flags, 0, sizeof(int) * n, stream);
+        cudaMemsetAsync(counters, 0, sizeof(int) * 4, stream);
+        const int T = 256;
+        k_prim_bounds<<<std::min((n + T - 1) / T, 1216), T, 0, stream>>>(d_verts, n, d_bounds);
+        k_morton<<<(n + T - 1) / T, T, 0, stream>>>(d_verts, n, d_bounds, keys[0], vals[0]);
+        cub::DoubleBuffer<uint64_t> kb(keys[0], keys[1]);
+        cub::DoubleBuffer<uint32_t> vb(vals[0], vals[1]);
+        cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, kb, vb, n, 0, 63, stream);
+        if (cudaMalloc(&tmp, tmpBytes) != cudaSuccess) {
+            snprintf(err, errlen, "buildWideBVH: sort scratch allocation failed");
+            rc = -4;
+        } else {
+            cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, kb, vb, n, 0, 63, stream);
+            const uint64_t *sk = kb.Current();
+            const uint32_t *order = vb.Current();
+            if (n > 1) k_karras<<<(n - 1 + T - 1) / T, T, 0, stream>>>(sk, n, child, parent, range);
+            k_refit<<<(n + T - 1) / T, T, 0, stream>>>(d_verts, order, n, child, parent, bmin, bmax, flags);
+            CollapseArgs A{d_verts, order, d_tri_mat, d_tri_light, n, child, range, bmin, bmax,
+                           out->nodes, out->tris, out->slot_shade, counters};
+            // root: wide node 0 from binary root (internal 0, or the single leaf)
+            const int one = 1;
+            const int2 root = make_int2(n > 1 ? 0 : 0 + (n - 1), 0);
+            cudaMemcpyAsync(items[0], &root, sizeof(int2), cudaMemcpyHostToDevice, stream);
+            cudaMemcpyAsync(counters, &one, sizeof(int), cudaMemcpyHostToDevice, stream);
+            int nitems = 1, depth = 0, cur = 0;
+            while (nitems > 0) {
+                cudaMemsetAsync(counters + 2, 0, sizeof(int), stream);
+                k_collapse<<<(nitems + 127) / 128, 128, 0, stream>>>(A, items[cur], nitems, items[cur ^ 1]);
+                cudaMemcpyAsync(&nitems, counters + 2, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                cudaError_t e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess) {
+                    fail("collapse", e);
+                    break;
+                }
+                cur ^= 1;
+                depth++;
+                if (depth > 4096) {
+                    snprintf(err, errlen, "buildWideBVH: collapse did not terminate");
+                    rc = -5;
+                    break;
+                }
+            }
+            int hostCounters[4] = {0, 0, 0, 0};
+            cudaMemcpyAsync(hostCounters, counters, sizeof(hostCounters), cudaMemcpyDeviceToHost, stream);
+            cudaError_t e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess && rc == 0) fail("final sync", e);
+            if (rc == 0) {
+                float hb[12];
+                cudaMemcpy(hb, d_bounds, sizeof(hb), cudaMemcpyDeviceToHost);
+                out->lo = mk(hb[0], hb[1], hb[2]);
+                out->hi = mk(hb[3], hb[4], hb[5]);
+                out->n_nodes = hostCounters[0];
+                out->ntri = n;
+                out->depth = depth;
+                if (hostCounters[1] != n) {
+                    snprintf(err, errlen, "buildWideBVH: placed %d of %d triangles", hostCounters[1], n);
+                    rc = -6;
+                } else if (depth > kStackDepth) {
+                    snprintf(err, errlen, "buildWideBVH: tree depth %d exceeds the traversal stack (%d)", depth,
+                             kStackDepth);
+                    rc = -7;
+                }
+            }
+        }
+    }
+    cudaFree(tmp);
+    cudaFree(d_bounds);
+    cudaFree(keys[0]);
+    cudaFree(keys[1]);
+    cudaFree(vals[0]);
+    cudaFree(vals[1]);
+    cudaFree(child);
+    cudaFree(range);
+    cudaFree(parent);
+    cudaFree(flags);
+    cudaFree(bmin);
+    cudaFree(bmax);
+    cudaFree(items[0]);
+    cudaFree(items[1]);
+    cudaFree(counters);
+    if (rc != 0) freeWideBVH(out);
+    return rc;
+}
+
+}  // namespace spgpu

@@ -1,0 +1,131 @@
+// ctx.cuh -- the library context behind spgpu_ctx: scene, lights, environment map,
+// BVH and the renderer's queues, all resident in device memory.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "bvh.cuh"
+#include "common.cuh"
+
+namespace spgpu {
+
+// Area light record (one per emitting triangle, in triangle order, like the
+// reference's per-triangle AreaLight list): 5 x float4.
+struct alignas(16) LightRecord {
+    float4 p0;     // xyz vertex 0, w = area
+    float4 e1;     // xyz p1 - p0
+    float4 e2;     // xyz p2 - p0
+    float4 n;      // xyz unit face normal (one-sided emission side)
+    float4 L;      // xyz emitted radiance
+};
+
+// Environment map: level-0 texels for lookups plus the sampling distribution of
+// Envmap::Envmap (lights/envmap.cc:17-47) -- conditional rows and the marginal.
+struct DeviceEnv {
+    int w = 0, h = 0;
+    float4 *tex = nullptr;        // [h*w] radiance
+    float *condCdf = nullptr;     // [h*(w+1)]
+    float *condFunc = nullptr;    // [h*w]
+    float *margCdf = nullptr;     // [h+1]
+    float *margFunc = nullptr;    // [h]  (= row integrals)
+    float margIntegral = 0.0f;
+    float3 center{0, 0, 0};
+    float radius = 0.0f;
+};
+
+// Everything the wavefront kernels read about the scene, passed by value.
+struct SceneView {
+    const WideNode *nodes;
+    const TriRecord *tris;
+    const int2 *slotShade;        // (material, light) per leaf slot
+    uint32_t nNodes, nTris;
+    const MaterialRecord *mats;
+    const LightRecord *lights;
+    int nArea;                    // area lights
+    int nLights;                  // nArea + (env ? 1 : 0)
+    int hasEnv;
+    DeviceEnv env;
+};
+
+// Per-pass queues of the wavefront renderer (sized for one path per pixel).
+struct RenderQueues {
+    int64_t capacity = 0;         // paths per pass
+    int maxDepth = 0;
+    float4 *pathBeta = nullptr;   // [cap] beta.rgb, w = specular flag
+    float4 *rayO[2] = {nullptr, nullptr};   // [cap] origin, w = path id bits
+    float4 *rayD[2] = {nullptr, nullptr};   // [cap] direction, w = tmax
+    HitRecord *hits = nullptr;    // [cap]
+    int *classQ = nullptr;        // [3*cap] ray indices per material class
+    float4 *shO = nullptr;        // [2*cap] origin, w = film pixel bits
+    float4 *shD = nullptr;        // [2*cap] direction, w = tmax
+    float4 *shL = nullptr;        // [2*cap] contribution
+    int *counters = nullptr;      // [(maxDepth+2) * 8]
+    unsigned long long *stats = nullptr;   // [4] paths, closest rays, shadow rays, spare
+    int *err = nullptr;           // [1] kernel error flags
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graphKey[4] = {0, 0, 0, 0};
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // scene
+    int ntri = 0;
+    float *verts = nullptr;
+    int *triMat = nullptr;
+    int *triLight = nullptr;
+    int nmat = 0;
+    MaterialRecord *mats = nullptr;
+    int nArea = 0;
+    LightRecord *lights = nullptr;
+    bool hasEnv = false;
+    DeviceEnv env;
+    bool sceneReady = false;
+    // accelerator
+    DeviceBVH bvh;
+    bool bvhReady = false;
+    double buildMs = 0.0;
+    // ray-batch scratch
+    int *traceErr = nullptr;
+    unsigned long long *traceStats = nullptr;
+    // renderer
+    RenderQueues rq;
+
+    SceneView view() const {
+        SceneView v;
+        v.nodes = bvh.nodes;
+        v.tris = bvh.tris;
+        v.slotShade = bvh.slot_shade;
+        v.nNodes = static_cast<uint32_t>(bvh.n_nodes);
+        v.nTris = static_cast<uint32_t>(bvh.ntri);
+        v.mats = mats;
+        v.lights = lights;
+        v.nArea = nArea;
+        v.nLights = nArea + (hasEnv ? 1 : 0);
+        v.hasEnv = hasEnv ? 1 : 0;
+        v.env = env;
+        return v;
+    }
+};
+
+void setError(const std::string &msg);
+int cudaFail(const char *what, cudaError_t e);
+void freeRenderQueues(RenderQueues *q);
+
+// camera matrices of the reference's PerspectiveCamera, computed in double on the
+// host and rounded once: raster -> camera (4x4, projective) and camera -> world.
+struct CameraView {
+    float r2c[16];
+    float c2w[12];
+};
+CameraView makeCamera(const float *camera, int width, int height);
+
+// wavefront.cu: trace desc->spp samples per pixel into film (device, float4 per pixel)
+int renderFrame(Ctx *ctx, const float *camera, int width, int height, int spp, int sampleOffset, int maxDepth,
+                uint32_t seed, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream);
+
+}  // namespace spgpu

@@ -1,0 +1,252 @@
+"""Host-side mirror of the reference's accelerator and integrator plugins over the
+C ABI of libspica_gpu.so (include/spica_gpu.h), through ctypes.
+
+Names follow the reference's interfaces:
+  GpuBVHAccel       -- Accelerator (core/accelerator.h:23): construct(), worldBound(),
+                       intersect(...) for closest hit and any hit
+                       (BVHAccel::intersect, accelerators/bvh.cc:315-329)
+  GpuPathIntegrator -- SamplerIntegrator/PathIntegrator (core/integrator.h:44,
+                       integrators/path/path.h:21): render(camera, scene, params)
+                       reading "maxDepth" and "sampleCount" like the reference
+                       (core/integrator.cc:63, integrators/path/path.cc:68)
+Errors: every negative status of the C ABI raises SpgpuError with the library's
+message (the reference aborts via Assertion/FatalError, core/common.h:69-115).
+The CUDA library is required: there is no CPU fallback; loading fails loudly when
+the extension has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+
+class SpgpuError(RuntimeError):
+    pass
+
+
+class BVHInfo(C.Structure):
+    _fields_ = [("triangles", C.c_int64), ("wide_nodes", C.c_int64), ("depth", C.c_int32),
+                ("lights", C.c_int32), ("build_ms", C.c_double), ("bounds", C.c_float * 6)]
+
+
+class TraceCounters(C.Structure):
+    _fields_ = [("rays", C.c_int64), ("nodes_per_ray", C.c_double), ("tris_per_ray", C.c_double)]
+
+
+class RenderDesc(C.Structure):
+    _fields_ = [("camera", C.c_float * 10), ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
+                ("sample_offset", C.c_int32), ("max_depth", C.c_int32), ("seed", C.c_uint32),
+                ("reserved", C.c_int32 * 4)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("paths", C.c_int64), ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64), ("ms", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int), ("reserved", C.c_int * 7)]
+
+
+# every extern "C" symbol include/spica_gpu.h declares
+EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version", "spgpu_upload_scene",
+           "spgpu_build_bvh", "spgpu_bvh_stats", "spgpu_trace", "spgpu_trace_host", "spgpu_trace_stats",
+           "spgpu_render", "spgpu_render_host"]
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None):
+    """Load libspica_gpu.so (built by spica_gb300.build).  Raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise SpgpuError(f"CUDA library not built: {p} (run python -m spica_gb300.build)")
+    lib = C.CDLL(p)
+    vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int32
+    lib.spgpu_create.argtypes = [C.POINTER(Config), C.POINTER(vp)]
+    lib.spgpu_destroy.argtypes = [vp]
+    lib.spgpu_destroy.restype = None
+    lib.spgpu_last_error.restype = C.c_char_p
+    lib.spgpu_version.restype = C.c_char_p
+    lib.spgpu_upload_scene.argtypes = [vp, i32, vp, vp, i32, vp, vp, i32, i32, vp]
+    lib.spgpu_build_bvh.argtypes = [vp]
+    lib.spgpu_bvh_stats.argtypes = [vp, C.POINTER(BVHInfo)]
+    lib.spgpu_trace.argtypes = [vp, C.c_int, vp, vp, i64, vp, vp]
+    lib.spgpu_trace_host.argtypes = [vp, C.c_int, vp, vp, i64, vp]
+    lib.spgpu_trace_stats.argtypes = [vp, C.c_int, vp, vp, i64, vp, C.POINTER(TraceCounters)]
+    lib.spgpu_render.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats), vp]
+    lib.spgpu_render_host.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats)]
+    for name in EXPORTS:
+        if name not in ("spgpu_destroy", "spgpu_last_error", "spgpu_version"):
+            getattr(lib, name).restype = C.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        msg = _lib.spgpu_last_error().decode() if _lib is not None else ""
+        raise SpgpuError(f"{what} failed ({rc}): {msg}")
+
+
+def _ptr(a) -> int:
+    """Device or host address of a torch tensor or numpy array."""
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+class Context:
+    """One device, one scene and its BVH (spgpu_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        cfg = Config(device=device)
+        h = C.c_void_p()
+        _check(self.lib.spgpu_create(C.byref(cfg), C.byref(h)), "spgpu_create")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.spgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def upload_scene(self, sc):
+        verts = np.ascontiguousarray(sc.verts, np.float32)
+        tri_mat = np.ascontiguousarray(sc.tri_mat, np.int32)
+        mats = np.ascontiguousarray(sc.materials, np.float32)
+        emit = None if sc.tri_emit is None else np.ascontiguousarray(sc.tri_emit, np.float32)
+        env = None if sc.env is None else np.ascontiguousarray(sc.env, np.float32)
+        eh, ew = (env.shape[0], env.shape[1]) if env is not None else (0, 0)
+        _check(self.lib.spgpu_upload_scene(self.h, verts.shape[0], verts.ctypes.data, tri_mat.ctypes.data,
+                                           mats.shape[0], mats.ctypes.data,
+                                           emit.ctypes.data if emit is not None else None, ew, eh,
+                                           env.ctypes.data if env is not None else None), "spgpu_upload_scene")
+
+    def build_bvh(self):
+        _check(self.lib.spgpu_build_bvh(self.h), "spgpu_build_bvh")
+
+    def bvh_info(self) -> BVHInfo:
+        info = BVHInfo()
+        _check(self.lib.spgpu_bvh_stats(self.h, C.byref(info)), "spgpu_bvh_stats")
+        return info
+
+
+class GpuBVHAccel:
+    """Accelerator over the device-built compressed 8-wide BVH."""
+
+    def __init__(self, scene, device: int = 0, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context(device)
+        self.scene = scene
+        self.ctx.upload_scene(scene)
+        self.constructed = False
+
+    def construct(self):
+        self.ctx.build_bvh()
+        self.constructed = True
+        return self
+
+    def worldBound(self):
+        b = self.ctx.bvh_info().bounds
+        return np.array(b[0:3]), np.array(b[3:6])
+
+    def info(self) -> BVHInfo:
+        return self.ctx.bvh_info()
+
+    # --- device tensors (torch): org_tmin, dir_tmax (n, 4) float32 on the GPU
+    def intersect_device(self, org_tmin, dir_tmax, out, any_hit: bool = False, stream: int = 0):
+        n = org_tmin.shape[0]
+        _check(self.ctx.lib.spgpu_trace(self.ctx.h, int(any_hit), _ptr(org_tmin), _ptr(dir_tmax), n, _ptr(out),
+                                        C.c_void_p(stream) if stream else None), "spgpu_trace")
+
+    def intersect_stats(self, org_tmin, dir_tmax, out, any_hit: bool = False) -> TraceCounters:
+        c = TraceCounters()
+        _check(self.ctx.lib.spgpu_trace_stats(self.ctx.h, int(any_hit), _ptr(org_tmin), _ptr(dir_tmax),
+                                              org_tmin.shape[0], _ptr(out), C.byref(c)), "spgpu_trace_stats")
+        return c
+
+    # --- host arrays (numpy)
+    def intersect(self, org, dir, tmax=None, tmin=None):
+        """Closest hit for n rays: returns (prim (n,) int32, -1 = miss; t; u; v)."""
+        ot, dt = _pack_rays(org, dir, tmax, tmin)
+        out = np.zeros((ot.shape[0], 4), np.float32)
+        _check(self.ctx.lib.spgpu_trace_host(self.ctx.h, 0, ot.ctypes.data, dt.ctypes.data, ot.shape[0],
+                                             out.ctypes.data), "spgpu_trace_host")
+        prim = out[:, 1].view(np.int32).copy()
+        return prim, out[:, 0].copy(), out[:, 2].copy(), out[:, 3].copy()
+
+    def intersect_any(self, org, dir, tmax=None, tmin=None):
+        """Any hit in (eps, tmax] for n rays: returns (n,) bool."""
+        ot, dt = _pack_rays(org, dir, tmax, tmin)
+        out = np.zeros(ot.shape[0], np.uint32)
+        _check(self.ctx.lib.spgpu_trace_host(self.ctx.h, 1, ot.ctypes.data, dt.ctypes.data, ot.shape[0],
+                                             out.ctypes.data), "spgpu_trace_host")
+        return out.astype(bool)
+
+
+def _pack_rays(org, dir, tmax=None, tmin=None):
+    org = np.asarray(org, np.float32).reshape(-1, 3)
+    dir = np.asarray(dir, np.float32).reshape(-1, 3)
+    n = org.shape[0]
+    ot = np.empty((n, 4), np.float32)
+    dt = np.empty((n, 4), np.float32)
+    ot[:, :3] = org
+    ot[:, 3] = 0.0 if tmin is None else tmin
+    dt[:, :3] = dir
+    dt[:, 3] = 1.0e32 if tmax is None else tmax
+    return ot, dt
+
+
+class GpuPathIntegrator:
+    """Path integrator on the GPU wavefront: render(camera, scene, params)."""
+
+    def __init__(self, seed: int = 0):
+        self.seed = seed
+        self.last_stats = None
+
+    def render(self, camera, accel: GpuBVHAccel, params: dict, film=None, sample_offset: int = 0):
+        """camera: (eye3, look3, up3, fov_deg); params: {"width", "height", "maxDepth",
+        "sampleCount"}.  Returns the film (H, W, 4) float32 host array: sum of radiance
+        and sample count per pixel, in the reference film's pixel order."""
+        W, H = int(params["width"]), int(params["height"])
+        d = self.desc(camera, W, H, int(params["sampleCount"]), int(params.get("maxDepth", 16)), sample_offset)
+        if film is None:
+            film = np.zeros((H, W, 4), np.float32)
+        st = RenderStats()
+        _check(accel.ctx.lib.spgpu_render_host(accel.ctx.h, C.byref(d), film.ctypes.data, C.byref(st)),
+               "spgpu_render_host")
+        self.last_stats = st
+        return film
+
+    def render_device(self, camera, accel: GpuBVHAccel, params: dict, film, sample_offset: int = 0,
+                      stream: int = 0) -> RenderStats:
+        """Same on a device film (torch tensor (H, W, 4) float32 on the GPU)."""
+        W, H = int(params["width"]), int(params["height"])
+        d = self.desc(camera, W, H, int(params["sampleCount"]), int(params.get("maxDepth", 16)), sample_offset)
+        st = RenderStats()
+        _check(accel.ctx.lib.spgpu_render(accel.ctx.h, C.byref(d), _ptr(film), C.byref(st),
+                                          C.c_void_p(stream) if stream else None), "spgpu_render")
+        self.last_stats = st
+        return st
+
+    def desc(self, camera, W, H, spp, max_depth, sample_offset=0) -> RenderDesc:
+        d = RenderDesc()
+        for i, v in enumerate(np.asarray(camera, np.float64).reshape(-1)[:10]):
+            d.camera[i] = float(v)
+        d.width, d.height, d.spp = W, H, spp
+        d.sample_offset, d.max_depth, d.seed = sample_offset, max_depth, self.seed & 0xFFFFFFFF
+        return d

@@ -1,0 +1,42 @@
+"""The C-ABI library builds, loads, and exports every symbol include/*.h declares.
+No compute calls: this runs without a GPU."""
+import ctypes
+import glob
+import os
+import re
+
+from conftest import ROOT
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[\w\s\*]+?\b(spgpu_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    from spica_gb300 import build, gpu
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    declared = _declared()
+    assert declared, "no declarations parsed"
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(gpu.EXPORTS) <= declared
+
+
+def test_loader_fails_loudly_without_library(tmp_path):
+    import pytest
+    from spica_gb300 import gpu
+    with pytest.raises(gpu.SpgpuError):
+        gpu.load_library(str(tmp_path / "missing.so"))
+
+
+def test_version_string():
+    from spica_gb300 import gpu
+    lib = gpu.load_library()
+    assert b"sm_103a" in lib.spgpu_version()
