@@ -1,0 +1,336 @@
+"""Benchmark of the GPU path-tracing hot path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload: the mid-scale plain render -- 500 seeded instances of tessellated spheres
+and boxes (~2.03M triangles) on a ground plane; 40% Lambert, 40% GGX conductor, 20%
+dielectric; 4 quad area lights plus a 1024x512 sky with a 0.5 deg sun; 1920x1080,
+max depth 16.  A step is one sample for every pixel (2,073,600 path samples) through
+the wavefront integrator.  Inputs (scene, BVH, queues) are resident in HBM before the
+timed region; each step's working set (~0.6 GB of queues plus ~0.12 GB of scene) is
+larger than the 129 MB L2.
+
+The JSON line carries, besides the headline path samples/s:
+  e2e        the same metric through the host entry point spgpu_render_host: every
+             step copies the film (float4 per pixel) host->device, renders, and copies
+             it back, from pinned host memory
+  roofline   the closest-hit traversal kernel ("extend"), measured live: algorithmic
+             bytes = rays x (32 B ray + 16 B hit + nodes/ray x 80 B + triangles/ray x
+             48 B) per launch over its CUDA-event duration, against the measured HBM
+             copy bandwidth
+  cpu_baseline  the CPU oracle (the compiled reference where it exists, else the C++
+             restatement) on a bounded sample of the same workload, all host threads
+  microbench the ray-BVH intersection microbench (1,048,576-triangle displaced sphere,
+             8M coherent + 8M incoherent rays), Mrays/s closest and any hit
+--impl reference runs the reference's CPU implementation alone on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "path samples/s"
+UNIT = "path samples/s"
+CONFIG = {"workload": "mid-scale plain render: 500 instances, ~2.03M triangles, 4 area lights + 1024x512 sky, "
+                      "1920x1080, max depth 16, 1 sample per pixel per step",
+          "scene_seed": 0, "width": 1920, "height": 1080, "max_depth": 16,
+          "l2": "per-step working set larger than L2 (no flush)", "parallelism": "replicas"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-i", str(index), "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle():
+    from oracle import spo
+    kind = "reference" if spo.available("ref") else "port"
+    if kind == "port" and not spo.available("port"):
+        spo.build("port")
+    return spo.Oracle(kind), kind
+
+
+def cpu_sample(scene, seconds: float = 15.0, threads: int = 0):
+    """Path samples/s of the CPU oracle on a bounded sample of the workload: film rows
+    spread over the image (1 sample per pixel), sized to about `seconds` of work after
+    a calibration band.  Returns (value, kind, cores, description, build_s)."""
+    o, kind = cpu_oracle()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    sc = o.scene(scene)
+    build_s = time.perf_counter() - t0
+    W, H = scene.width, scene.height
+    cal_rows = 2
+    t0 = time.perf_counter()
+    o_rows = [H // 2]
+    sc.render(scene.camera, W, H, 1, scene.max_depth, seed=5, window=(0, H // 2, W, cal_rows), nthreads=threads)
+    rate = cal_rows * W / max(time.perf_counter() - t0, 1e-6)
+    rows = int(max(4, min(H, seconds * rate / W)))
+    bands = max(1, min(16, rows // 2))
+    per = max(1, rows // bands)
+    starts = np.linspace(0, H - per, bands).astype(int)
+    total, t0 = 0, time.perf_counter()
+    for y in starts:
+        sc.render(scene.camera, W, H, 1, scene.max_depth, seed=9, window=(0, int(y), W, per), nthreads=threads)
+        total += W * per
+    dt = time.perf_counter() - t0
+    del o_rows
+    desc = f"{bands} bands x {per} rows x {W} px at 1 sample/pixel ({total} path samples, {dt:.1f} s)"
+    return total / dt, kind, threads, desc, build_s
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from spica_gb300 import scenes
+    scene = scenes.mid_scale()
+    o, kind = cpu_oracle()
+    threads = os.cpu_count() or 1
+    sc = o.scene(scene)
+    W, H = scene.width, scene.height
+    rows = 8   # each step: 8 film rows (15,360 path samples), bands spread over the image
+    ys = np.linspace(0, H - rows, max(args.steps, 1) + args.warmup).astype(int)
+    for k in range(args.warmup):
+        sc.render(scene.camera, W, H, 1, scene.max_depth, seed=100 + k, window=(0, int(ys[k]), W, rows),
+                  nthreads=threads)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        y = int(ys[args.warmup + k])
+        sc.render(scene.camera, W, H, 1, scene.max_depth, seed=200 + k, window=(0, y, W, rows), nthreads=threads)
+    dt = time.perf_counter() - t0
+    value = args.steps * rows * W / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(CONFIG, step=f"{rows} film rows x {W} px, 1 sample per pixel"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{args.steps} steps of {rows} rows x {W} px"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def microbench(torch, GpuBVHAccel, scenes, reps=3):
+    sph = scenes.displaced_sphere(levels=9, seed=0)
+    acc = GpuBVHAccel(sph).construct()
+    org, d, tmax = scenes.microbench_rays(sph, 8 << 20, 8 << 20, 4096, 2048, seed=0)
+    n = org.shape[0]
+    ot = torch.zeros((n, 4), device="cuda")
+    dt = torch.zeros((n, 4), device="cuda")
+    ot[:, :3] = torch.from_numpy(org).cuda()
+    dt[:, :3] = torch.from_numpy(d).cuda()
+    dt[:, 3] = 1e32
+    hits = torch.zeros((n, 4), device="cuda")
+    anyo = torch.zeros(n, dtype=torch.int32, device="cuda")
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(reps):
+            s.record()
+            fn()
+            e.record()
+            torch.cuda.synchronize()
+            best = min(best, s.elapsed_time(e))
+        return best
+
+    ms_c = timed(lambda: acc.intersect_device(ot, dt, hits, stream=stream))
+    cc = acc.intersect_stats(ot, dt, hits)
+    dt[:, 3] = torch.from_numpy(tmax).cuda()
+    ms_a = timed(lambda: acc.intersect_device(ot, dt, anyo, any_hit=True, stream=stream))
+    ca = acc.intersect_stats(ot, dt, anyo, any_hit=True)
+    info = acc.info()
+    return {"triangles": int(sph.ntri), "rays": int(n), "closest_mrays_s": n / ms_c / 1e3,
+            "any_mrays_s": n / ms_a / 1e3, "closest_nodes_per_ray": cc.nodes_per_ray,
+            "closest_tris_per_ray": cc.tris_per_ray, "any_nodes_per_ray": ca.nodes_per_ray,
+            "any_tris_per_ray": ca.tris_per_ray, "bvh_build_ms": info.build_ms, "wide_nodes": int(info.wide_nodes)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-micro", action="store_true", help="skip the intersection microbench")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from spica_gb300 import GpuBVHAccel, GpuPathIntegrator, scenes
+    from spica_gb300.gpu import KERNEL_CLASSES
+
+    scene = scenes.mid_scale()
+    W, H, md = scene.width, scene.height, scene.max_depth
+    npix = W * H
+    acc = GpuBVHAccel(scene, device=local).construct()
+    info = acc.info()
+    integ = GpuPathIntegrator(seed=1234 + rank)
+    params = {"width": W, "height": H, "maxDepth": md}
+    film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    # warm-up (graph capture happens in the first call)
+    integ.render_device(scene.camera, acc, dict(params, sampleCount=max(args.warmup, 1)), film, stream=stream)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    st = integ.render_device(scene.camera, acc, dict(params, sampleCount=args.steps), film,
+                             sample_offset=max(args.warmup, 1), stream=stream)
+    ev1.record()
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * args.steps * npix / (ms / 1e3)
+    rays = st.rays_closest + st.rays_shadow
+
+    # end to end through the host entry point, pinned host film copied both ways per step
+    host_film = torch.zeros((H, W, 4), dtype=torch.float32).pin_memory()
+    hf = host_film.numpy()
+    integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=1 << 16)
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=(1 << 16) + 1 + k)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = ws * args.steps * npix / e2e_s
+    film_bytes = npix * 16
+
+    if rank != 0:
+        return 0
+
+    # per-kernel profile: event-timed launches of 2 passes, then visit counters
+    prof_film = torch.zeros_like(film)
+    pr = integ.profile_device(scene.camera, acc, dict(params, sampleCount=2), prof_film, sample_offset=1 << 20,
+                              stream=stream)
+    total_k = sum(pr.kernel_ms[i] for i in range(7))
+    kernels = {KERNEL_CLASSES[i]: {"ms": pr.kernel_ms[i], "launches": int(pr.launches[i]),
+                                   "share": pr.kernel_ms[i] / total_k if total_k else 0.0} for i in range(7)}
+    ext_ms_per_launch = pr.kernel_ms[1] / max(pr.launches[1], 1)
+    rays_per_launch = pr.rays_closest / max(pr.launches[1], 1)
+    bytes_per_ray = 32 + 16 + 80 * pr.closest_nodes_per_ray + 48 * pr.closest_tris_per_ray
+    hbm, peak_src = peaks()
+    achieved = rays_per_launch * bytes_per_ray / (ext_ms_per_launch / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "extend (closest-hit traversal)", "achieved": achieved, "peak": hbm,
+                "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
+                "traffic": None, "bytes_per_ray": bytes_per_ray, "rays_per_launch": rays_per_launch,
+                "ms_per_launch": ext_ms_per_launch, "nodes_per_ray": pr.closest_nodes_per_ray,
+                "tris_per_ray": pr.closest_tris_per_ray}
+    traffic_file = os.path.join(ROOT, "profiles", "extend_traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            roofline["traffic"] = json.load(open(traffic_file))["bytes_per_launch_full"]
+        except Exception:
+            pass
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": dict(CONFIG, triangles=int(scene.ntri), wide_nodes=int(info.wide_nodes),
+                           bvh_build_ms=info.build_ms),
+            "mrays_s": ws * args.steps * rays / max(st.paths, 1) * npix / (ms / 1e3) / 1e6 if st.paths else None,
+            "rays_per_path": rays / max(st.paths, 1),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": film_bytes + 80,
+                    "d2h_bytes_per_step": film_bytes},
+            "gpu_launches": int(args.steps * (2 + 5 * (md + 1))), "clocks": clk, "roofline": roofline,
+            "kernels": kernels}
+    if not args.no_micro:
+        line["microbench"] = microbench(torch, GpuBVHAccel, scenes)
+    if not args.no_cpu and ws == 1:
+        v, kind, cores, desc, build_s = cpu_sample(scene)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc,
+                                "bvh_build_s": build_s}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

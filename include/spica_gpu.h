@@ -9,8 +9,8 @@
  * One context = one device + one scene + its BVH.  A context is used by one host
  * thread at a time.  "device pointer" arguments are CUDA device memory (for example
  * a torch tensor's data_ptr); "host" entry points take host memory and copy both
- * ways themselves.  `stream` is a cudaStream_t passed as void* (NULL = the context's
- * own stream).
+ * ways themselves.  `stream` is a cudaStream_t passed as void*; NULL is CUDA's
+ * legacy default stream (the one torch uses unless told otherwise).
  */
 #ifndef SPICA_GPU_H
 #define SPICA_GPU_H
@@ -140,6 +140,22 @@ int spgpu_render(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, spg
                  void *stream);                                                      /* device film */
 int spgpu_render_host(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film,
                       spgpu_render_stats *stats);                                    /* host film   */
+
+/* Profiling (no counterpart in the reference, which has only a progress printf,
+ * core/integrator.cc:92-96): the same samples as spgpu_render, launched kernel by
+ * kernel without the graph and timed with CUDA events on `stream`, then repeated
+ * with BVH visit counters.  Kernel classes: 0 raygen, 1 extend (closest hit),
+ * 2 shade Lambert, 3 shade GGX conductor, 4 shade dielectric, 5 shadow (any hit),
+ * 6 finish.  The film receives both runs' samples. */
+typedef struct {
+    double kernel_ms[8];
+    int64_t launches[8];
+    int64_t paths, rays_closest, rays_shadow;
+    double closest_nodes_per_ray, closest_tris_per_ray;
+    double shadow_nodes_per_ray, shadow_tris_per_ray;
+} spgpu_kernel_profile;
+int spgpu_render_profile(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, spgpu_kernel_profile *out,
+                         void *stream);
 
 #ifdef __cplusplus
 }

@@ -587,8 +587,7 @@ int spgpu_trace(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *d
     if (!h) return SPGPU_EINVAL;
     Ctx &C = h->c;
     cudaSetDevice(C.device);
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : C.stream;
-    return launchTrace(C, any_hit, org_tmin, dir_tmax, n, out, s, false);
+    return launchTrace(C, any_hit, org_tmin, dir_tmax, n, out, static_cast<cudaStream_t>(stream), false);
 }
 
 int spgpu_trace_stats(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out,
@@ -662,7 +661,7 @@ int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_re
         return SPGPU_EINVAL;
     }
     cudaSetDevice(C.device);
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : C.stream;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     unsigned long long st[4] = {0, 0, 0, 0};
     float ms = 0.0f;
     const int rc = renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
@@ -673,6 +672,40 @@ int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_re
         stats->rays_shadow = static_cast<int64_t>(st[2]);
         stats->ms = ms;
     }
+    return rc;
+}
+
+int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_kernel_profile *out,
+                         void *stream) {
+    if (!h || !d || !film || !out) {
+        setError("spgpu_render_profile: invalid arguments");
+        return SPGPU_EINVAL;
+    }
+    Ctx &C = h->c;
+    if (!C.bvhReady) {
+        setError("spgpu_render_profile: no BVH");
+        return SPGPU_ESTATE;
+    }
+    if (d->width <= 0 || d->height <= 0 || d->spp < 0 || d->max_depth < 0 || d->max_depth > 64 ||
+        (reinterpret_cast<uintptr_t>(film) & 15)) {
+        setError("spgpu_render_profile: invalid resolution, spp, max_depth or film alignment");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(C.device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::memset(out, 0, sizeof(*out));
+    long long launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long st[4] = {0, 0, 0, 0}, vis[4] = {0, 0, 0, 0};
+    const int rc = renderProfile(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                                 reinterpret_cast<float4 *>(film), out->kernel_ms, launches, st, vis, s);
+    for (int k = 0; k < 8; k++) out->launches[k] = launches[k];
+    out->paths = static_cast<int64_t>(st[0]);
+    out->rays_closest = static_cast<int64_t>(st[1]);
+    out->rays_shadow = static_cast<int64_t>(st[2]);
+    out->closest_nodes_per_ray = st[1] ? static_cast<double>(vis[0]) / st[1] : 0.0;
+    out->closest_tris_per_ray = st[1] ? static_cast<double>(vis[1]) / st[1] : 0.0;
+    out->shadow_nodes_per_ray = st[2] ? static_cast<double>(vis[2]) / st[2] : 0.0;
+    out->shadow_tris_per_ray = st[2] ? static_cast<double>(vis[3]) / st[2] : 0.0;
     return rc;
 }
 

@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "../../include/spica_gpu.h"
 #include "ctx.cuh"
@@ -55,6 +56,7 @@ struct PassArgs {
     int *counters;     // per bounce: [0] rays in, [1..3] class counts, [4] shadow rays
     int *ctl;          // [0] sample index of the pass
     unsigned long long *stats;
+    unsigned long long *visit;   // [0..1] extend nodes / triangles, [2..3] shadow nodes / triangles
     int *err;
 };
 
@@ -187,15 +189,16 @@ __global__ void k_raygen(PassArgs p) {
     if (blockIdx.x == 0 && threadIdx.x == 0) p.counters[0] = p.npix;
 }
 
+template <bool STATS>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(PassArgs p, int b) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
+    uint32_t nodeCount = 0, triCount = 0;
     const int *cnt = p.counters + b * kCountersPerBounce;
     int *classCnt = p.counters + b * kCountersPerBounce + 1;
     const int n = cnt[0];
     const float4 *rO = (b & 1) ? p.rayO1 : p.rayO0;
     const float4 *rD = (b & 1) ? p.rayD1 : p.rayD0;
     bool overflow = false;
-    uint32_t dummy = 0;
     const int stride = gridDim.x * blockDim.x;
     const int nIter = (n + stride - 1) / stride;   // uniform trip count keeps warps whole for the ballots
     for (int it = 0; it < nIter; it++) {
@@ -206,8 +209,9 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(PassArgs p, int b) {
             const float4 o4 = rO[i], d4 = rD[i];
             float tmax = d4.w, u = 0.0f, v = 0.0f;
             int slot = -1;
-            const bool hit = traceWide<false, false>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(o4), xyz(d4), 0.0f, tmax, slot, u, v,
-                                                     stack + threadIdx.x, kTraceBlock, &dummy, &dummy, &overflow);
+            const bool hit = traceWide<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(o4), xyz(d4),
+                                                     0.0f, tmax, slot, u, v, stack + threadIdx.x, kTraceBlock,
+                                                     &nodeCount, &triCount, &overflow);
             if (hit) {
                 HitRecord h;
                 h.t = tmax;
@@ -229,6 +233,10 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(PassArgs p, int b) {
         }
     }
     if (overflow) atomicOr(p.err, 1);
+    if (STATS) {
+        atomicAdd(&p.visit[0], static_cast<unsigned long long>(nodeCount));
+        atomicAdd(&p.visit[1], static_cast<unsigned long long>(triCount));
+    }
 }
 
 template <int CLS>
@@ -418,20 +426,26 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
     }
 }
 
+template <bool STATS>
 __global__ void __launch_bounds__(kTraceBlock) k_shadow(PassArgs p, int b) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     const int n = p.counters[b * kCountersPerBounce + 4];
     bool overflow = false;
-    uint32_t dummy = 0;
+    uint32_t nodeCount = 0, triCount = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 o4 = p.shO[i], d4 = p.shD[i];
         float tmax = d4.w, u, v;
         int slot;
-        const bool occ = traceWide<true, false>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(o4), xyz(d4), 0.0f, tmax, slot, u, v,
-                                                stack + threadIdx.x, kTraceBlock, &dummy, &dummy, &overflow);
+        const bool occ = traceWide<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(o4), xyz(d4),
+                                                0.0f, tmax, slot, u, v, stack + threadIdx.x, kTraceBlock, &nodeCount,
+                                                &triCount, &overflow);
         if (!occ) filmAdd(p.film, __float_as_int(o4.w), xyz(p.shL[i]));
     }
     if (overflow) atomicOr(p.err, 1);
+    if (STATS) {
+        atomicAdd(&p.visit[2], static_cast<unsigned long long>(nodeCount));
+        atomicAdd(&p.visit[3], static_cast<unsigned long long>(triCount));
+    }
 }
 
 __global__ void k_finish(PassArgs p) {
@@ -471,7 +485,7 @@ int ensureQueues(RenderQueues &q, int64_t npix, int maxDepth) {
     q.shD = dalloc<float4>(2 * cap);
     q.shL = dalloc<float4>(2 * cap);
     q.counters = dalloc<int>(static_cast<size_t>(maxDepth + 2) * kCountersPerBounce + 8);
-    q.stats = dalloc<unsigned long long>(4);
+    q.stats = dalloc<unsigned long long>(8);
     q.err = dalloc<int>(1);
     if (!q.pathBeta || !q.rayO[0] || !q.rayO[1] || !q.rayD[0] || !q.rayD[1] || !q.hits || !q.classQ || !q.shO ||
         !q.shD || !q.shL || !q.counters || !q.stats || !q.err) {
@@ -480,6 +494,65 @@ int ensureQueues(RenderQueues &q, int64_t npix, int maxDepth) {
         return SPGPU_ENOMEM;
     }
     return 0;
+}
+
+struct Grids {
+    int trace, shade, raygen;
+};
+
+Grids passGrids(int device, int64_t npix) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int occT = 0, occS = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occT, k_extend<false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occS, k_shade<0>, kShadeBlock, 0);
+    Grids g;
+    g.trace = sms * std::max(occT, 1);
+    g.shade = sms * std::max(occS, 1);
+    g.raygen = static_cast<int>(std::min<int64_t>((npix + 255) / 256, static_cast<int64_t>(sms) * 8));
+    return g;
+}
+
+// One pass of kernels on stream cs.  With ev (2 events per kernel, in launch order)
+// every kernel is bracketed for timing, and STATS variants count BVH visits.
+enum KernelClass { kRaygen = 0, kExtend, kShadeL, kShadeC, kShadeD, kShadow, kFinish, kNumClasses };
+
+template <bool STATS>
+void launchPass(const PassArgs &a, const Grids &g, cudaStream_t cs, size_t ctrBytes, cudaEvent_t *ev,
+                int *evClass, int *nev) {
+    auto mark = [&](int cls) {
+        if (ev) {
+            evClass[*nev / 2] = cls;
+            cudaEventRecord(ev[(*nev)++], cs);
+        }
+    };
+    auto done = [&]() {
+        if (ev) cudaEventRecord(ev[(*nev)++], cs);
+    };
+    cudaMemsetAsync(a.counters, 0, ctrBytes, cs);
+    mark(kRaygen);
+    k_raygen<<<g.raygen, 256, 0, cs>>>(a);
+    done();
+    for (int b = 0; b <= a.maxDepth; b++) {
+        mark(kExtend);
+        k_extend<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
+        done();
+        mark(kShadeL);
+        k_shade<kMatLambert><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
+        done();
+        mark(kShadeC);
+        k_shade<kMatConductor><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
+        done();
+        mark(kShadeD);
+        k_shade<kMatDielectric><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
+        done();
+        mark(kShadow);
+        k_shadow<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
+        done();
+    }
+    mark(kFinish);
+    k_finish<<<1, 32, 0, cs>>>(a);
+    done();
 }
 
 uint64_t hashBytes(const void *d, size_t n, uint64_t h = 1469598103934665603ull) {
@@ -508,14 +581,14 @@ void freeRenderQueues(RenderQueues *q) {
     *q = RenderQueues{};
 }
 
-int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
-                float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
-    Ctx &C = *ctx;
+namespace {
+int setupPass(Ctx &C, const float *camera, int W, int H, int maxDepth, uint32_t seed, float4 *film, PassArgs *out) {
     RenderQueues &q = C.rq;
     const int64_t npix = static_cast<int64_t>(W) * H;
     int rc = ensureQueues(q, npix, maxDepth);
     if (rc) return rc;
-    PassArgs a;
+    PassArgs &a = *out;
+    std::memset(&a, 0, sizeof(a));
     a.sv = C.view();
     a.cam = makeCamera(camera, W, H);
     a.W = W;
@@ -538,7 +611,20 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
     a.counters = q.counters;
     a.ctl = q.counters + (q.maxDepth + 2) * kCountersPerBounce;
     a.stats = q.stats;
+    a.visit = q.stats + 4;
     a.err = q.err;
+    return 0;
+}
+}  // namespace
+
+int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
+                float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
+    Ctx &C = *ctx;
+    RenderQueues &q = C.rq;
+    const int64_t npix = static_cast<int64_t>(W) * H;
+    PassArgs a;
+    int rc = setupPass(C, camera, W, H, maxDepth, seed, film, &a);
+    if (rc) return rc;
 
     // (re)capture the pass graph when anything baked into it changes
     uint64_t key[4];
@@ -551,28 +637,13 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
             cudaGraphExecDestroy(q.graph);
             q.graph = nullptr;
         }
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
-        int occT = 0, occS = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occT, k_extend, kTraceBlock, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occS, k_shade<0>, kShadeBlock, 0);
-        const int gT = sms * std::max(occT, 1), gS = sms * std::max(occS, 1);
-        const int gR = static_cast<int>(std::min<int64_t>((npix + 255) / 256, sms * 8));
+        const Grids gr = passGrids(C.device, npix);
         const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;
         cudaStream_t cs = C.stream;
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cudaFail("cudaStreamBeginCapture", e);
-        cudaMemsetAsync(q.counters, 0, ctrBytes, cs);
-        k_raygen<<<gR, 256, 0, cs>>>(a);
-        for (int b = 0; b <= maxDepth; b++) {
-            k_extend<<<gT, kTraceBlock, 0, cs>>>(a, b);
-            k_shade<kMatLambert><<<gS, kShadeBlock, 0, cs>>>(a, b);
-            k_shade<kMatConductor><<<gS, kShadeBlock, 0, cs>>>(a, b);
-            k_shade<kMatDielectric><<<gS, kShadeBlock, 0, cs>>>(a, b);
-            k_shadow<<<gT, kTraceBlock, 0, cs>>>(a, b);
-        }
-        k_finish<<<1, 32, 0, cs>>>(a);
+        launchPass<false>(a, gr, cs, ctrBytes, nullptr, nullptr, nullptr);
         e = cudaStreamEndCapture(cs, &g);
         if (e != cudaSuccess) return cudaFail("cudaStreamEndCapture", e);
         e = cudaGraphInstantiate(&q.graph, g, 0);
@@ -583,7 +654,7 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    cudaError_t e = cudaMemsetAsync(q.stats, 0, 4 * sizeof(unsigned long long), stream);
+    cudaError_t e = cudaMemsetAsync(q.stats, 0, 8 * sizeof(unsigned long long), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(q.err, 0, sizeof(int), stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(a.ctl, &sampleOffset, sizeof(int), cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaEventRecord(e0, stream);
@@ -603,6 +674,65 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
     *msOut = ms;
     if (err) {
         setError("spgpu_render: traversal stack overflow");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
+}
+
+int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
+                  float4 *film, double *kernelMs, long long *launches, unsigned long long *statsOut,
+                  unsigned long long *visitOut, cudaStream_t stream) {
+    Ctx &C = *ctx;
+    RenderQueues &q = C.rq;
+    PassArgs a;
+    int rc = setupPass(C, camera, W, H, maxDepth, seed, film, &a);
+    if (rc) return rc;
+    const Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
+    const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;
+    const int perPass = 2 * (2 + 5 * (maxDepth + 1));
+    std::vector<cudaEvent_t> ev(static_cast<size_t>(perPass) * std::max(spp, 1));
+    std::vector<int> cls(ev.size() / 2 + 1);
+    for (auto &e : ev) cudaEventCreate(&e);
+    for (int k = 0; k < kNumClasses; k++) {
+        kernelMs[k] = 0.0;
+        launches[k] = 0;
+    }
+    cudaError_t e = cudaMemsetAsync(q.stats, 0, 8 * sizeof(unsigned long long), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(q.err, 0, sizeof(int), stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(a.ctl, &sampleOffset, sizeof(int), cudaMemcpyHostToDevice, stream);
+    // timing: plain kernels, each bracketed by events
+    int nev = 0;
+    for (int s = 0; s < spp && e == cudaSuccess; s++) {
+        launchPass<false>(a, gr, stream, ctrBytes, ev.data(), cls.data(), &nev);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    for (int i = 0; i + 1 < nev && e == cudaSuccess; i += 2) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+        kernelMs[cls[i / 2]] += ms;
+        launches[cls[i / 2]] += 1;
+    }
+    unsigned long long st[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(st, q.stats, sizeof(st), cudaMemcpyDeviceToHost);
+    // counting: the same samples again with the visit counters on
+    if (e == cudaSuccess) e = cudaMemsetAsync(q.stats, 0, 8 * sizeof(unsigned long long), stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(a.ctl, &sampleOffset, sizeof(int), cudaMemcpyHostToDevice, stream);
+    for (int s = 0; s < spp && e == cudaSuccess; s++) {
+        launchPass<true>(a, gr, stream, ctrBytes, nullptr, nullptr, nullptr);
+        e = cudaGetLastError();
+    }
+    unsigned long long st2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int err = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st2, q.stats, sizeof(st2), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, q.err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return cudaFail("spgpu_render_profile", e);
+    for (int k = 0; k < 4; k++) statsOut[k] = st[k];
+    for (int k = 0; k < 4; k++) visitOut[k] = st2[4 + k];
+    if (err) {
+        setError("spgpu_render_profile: traversal stack overflow");
         return SPGPU_EKERNEL;
     }
     return 0;

@@ -50,6 +50,16 @@ class RenderStats(C.Structure):
     _fields_ = [("paths", C.c_int64), ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64), ("ms", C.c_double)]
 
 
+class KernelProfile(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double * 8), ("launches", C.c_int64 * 8), ("paths", C.c_int64),
+                ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64), ("closest_nodes_per_ray", C.c_double),
+                ("closest_tris_per_ray", C.c_double), ("shadow_nodes_per_ray", C.c_double),
+                ("shadow_tris_per_ray", C.c_double)]
+
+
+KERNEL_CLASSES = ["raygen", "extend", "shade_lambert", "shade_conductor", "shade_dielectric", "shadow", "finish"]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("reserved", C.c_int * 7)]
 
@@ -57,7 +67,7 @@ class Config(C.Structure):
 # every extern "C" symbol include/spica_gpu.h declares
 EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version", "spgpu_upload_scene",
            "spgpu_build_bvh", "spgpu_bvh_stats", "spgpu_trace", "spgpu_trace_host", "spgpu_trace_stats",
-           "spgpu_render", "spgpu_render_host"]
+           "spgpu_render", "spgpu_render_host", "spgpu_render_profile"]
 
 _lib = None
 
@@ -85,6 +95,7 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_trace_stats.argtypes = [vp, C.c_int, vp, vp, i64, vp, C.POINTER(TraceCounters)]
     lib.spgpu_render.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats), vp]
     lib.spgpu_render_host.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats)]
+    lib.spgpu_render_profile.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(KernelProfile), vp]
     for name in EXPORTS:
         if name not in ("spgpu_destroy", "spgpu_last_error", "spgpu_version"):
             getattr(lib, name).restype = C.c_int
@@ -242,6 +253,16 @@ class GpuPathIntegrator:
                                           C.c_void_p(stream) if stream else None), "spgpu_render")
         self.last_stats = st
         return st
+
+    def profile_device(self, camera, accel: GpuBVHAccel, params: dict, film, sample_offset: int = 0,
+                       stream: int = 0) -> KernelProfile:
+        """Per-kernel event timings and BVH visit counts of params["sampleCount"] passes."""
+        W, H = int(params["width"]), int(params["height"])
+        d = self.desc(camera, W, H, int(params["sampleCount"]), int(params.get("maxDepth", 16)), sample_offset)
+        pr = KernelProfile()
+        _check(accel.ctx.lib.spgpu_render_profile(accel.ctx.h, C.byref(d), _ptr(film), C.byref(pr),
+                                                  C.c_void_p(stream) if stream else None), "spgpu_render_profile")
+        return pr
 
     def desc(self, camera, W, H, spp, max_depth, sample_offset=0) -> RenderDesc:
         d = RenderDesc()

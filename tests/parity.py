@@ -8,8 +8,10 @@ Hit primitives must be identical except for *stated FP32 ties*, decided in doubl
     below 8 * 2^-24 times the condition number of the Moller-Trumbore terms);
   * for any-hit, the nearest surface lies within 1e-5 relative of tmax.
 Hit distances of identical primitives must agree within 1e-5 relative.
-Images: per pixel and channel, z = (mean_gpu - mean_ref) / sqrt(var_gpu + var_ref)
-(variances of the means); at most 1 % of |z| may exceed 3 (a Gaussian gives 0.27 %).
+Images: per pixel and channel, z = (mean_gpu - mean_ref) / sqrt(var_gpu + var_ref + f^2)
+(variances of the means; f = 1e-5 x |mean| absorbs FP32-vs-FP64 rounding where a pixel
+sees a constant radiance, e.g. a uniform region of the environment map, and both
+variances are zero); at most 1 % of |z| may exceed 3 (a Gaussian gives 0.27 %).
 """
 from __future__ import annotations
 
@@ -103,10 +105,14 @@ def classify_any(verts, org, dir, tmax, hit_gpu, hit_ref, prim_near, t_near, pri
             "fail": int((~tie).sum()), "fail_idx": mis[~tie][:20].tolist()}
 
 
+ROUNDING_FLOOR = 1e-5
+
+
 def zscores(mean_a, var_a, mean_b, var_b):
+    floor = (ROUNDING_FLOOR * np.maximum(np.abs(mean_a), np.abs(mean_b))) ** 2
+    v = var_a + var_b + floor
     with np.errstate(divide="ignore", invalid="ignore"):
-        z = (mean_a - mean_b) / np.sqrt(var_a + var_b)
-    z[~np.isfinite(z)] = 0.0
-    both_zero = (var_a + var_b) == 0
-    z[both_zero & (mean_a != mean_b)] = np.inf
+        z = (mean_a - mean_b) / np.sqrt(v)
+    z[(v == 0) & (mean_a == mean_b)] = 0.0
+    z[(v == 0) & (mean_a != mean_b)] = np.inf
     return z

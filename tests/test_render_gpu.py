@@ -54,7 +54,11 @@ def test_matches_reference_render(gpulib, name):
     mr, vr = ref_moments(g)
     z = zscores(mg, vg, mr, vr)
     frac = float((np.abs(z) > 3).mean())
-    assert frac < 0.01, (frac, float(np.abs(z).max()))
+    dump = os.environ.get("SPICA_TEST_DUMP")
+    if dump:
+        np.savez_compressed(os.path.join(dump, f"{name}_gpu.npz"), mg=mg, vg=vg, mr=mr, vr=vr, z=z)
+    worst = np.unravel_index(np.argmax(np.abs(z)), z.shape)
+    assert frac < 0.01, (frac, float(np.abs(z).max()), float(z.mean()), worst, float(mg[worst]), float(mr[worst]))
     # image mean within 3 standard errors
     se = np.sqrt(vg.sum() + vr.sum()) / z.size
     assert abs(mg.mean() - mr.mean()) < 3 * se + 1e-6, (mg.mean(), mr.mean(), se)
