@@ -116,31 +116,30 @@ def cpu_oracle():
 
 
 def cpu_sample(scene, seconds: float = 15.0, threads: int = 0):
-    """Path samples/s of the CPU oracle on a bounded sample of the workload: film rows
-    spread over the image (1 sample per pixel), sized to about `seconds` of work after
-    a calibration band.  Returns (value, kind, cores, description, build_s)."""
+    """Path samples/s of the CPU oracle on a bounded sample of the workload: passes of
+    1 sample per pixel over 8 film rows spread down the image (one band of 8 rows per
+    step of the row index), repeated until `seconds` of work are done.
+    Returns (value, kind, cores, description, build_s)."""
     o, kind = cpu_oracle()
     threads = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
     sc = o.scene(scene)
     build_s = time.perf_counter() - t0
     W, H = scene.width, scene.height
-    cal_rows = 2
-    t0 = time.perf_counter()
-    o_rows = [H // 2]
-    sc.render(scene.camera, W, H, 1, scene.max_depth, seed=5, window=(0, H // 2, W, cal_rows), nthreads=threads)
-    rate = cal_rows * W / max(time.perf_counter() - t0, 1e-6)
-    rows = int(max(4, min(H, seconds * rate / W)))
-    bands = max(1, min(16, rows // 2))
-    per = max(1, rows // bands)
-    starts = np.linspace(0, H - per, bands).astype(int)
-    total, t0 = 0, time.perf_counter()
-    for y in starts:
-        sc.render(scene.camera, W, H, 1, scene.max_depth, seed=9, window=(0, int(y), W, per), nthreads=threads)
-        total += W * per
-    dt = time.perf_counter() - t0
-    del o_rows
-    desc = f"{bands} bands x {per} rows x {W} px at 1 sample/pixel ({total} path samples, {dt:.1f} s)"
+    rows, bands = 8, 16
+    starts = np.linspace(0, H - rows, bands).astype(int)
+    total, k, t0 = 0, 0, time.perf_counter()
+    while True:
+        y = int(starts[k % bands])
+        sc.render(scene.camera, W, H, 1, scene.max_depth, seed=9 + k // bands, window=(0, y, W, rows),
+                  nthreads=threads)
+        total += W * rows
+        k += 1
+        dt = time.perf_counter() - t0
+        if dt >= seconds and k >= bands:
+            break
+    desc = (f"{k} bands of {rows} rows x {W} px (16 band positions spread over the image), 1 sample/pixel: "
+            f"{total} path samples in {dt:.1f} s")
     return total / dt, kind, threads, desc, build_s
 
 
@@ -176,10 +175,10 @@ def run_reference(args):
     return 0
 
 
-def microbench(torch, GpuBVHAccel, scenes, reps=3):
+def microbench(torch, GpuBVHAccel, scenes, reps=3, rays=16 << 20):
     sph = scenes.displaced_sphere(levels=9, seed=0)
     acc = GpuBVHAccel(sph).construct()
-    org, d, tmax = scenes.microbench_rays(sph, 8 << 20, 8 << 20, 4096, 2048, seed=0)
+    org, d, tmax = scenes.microbench_rays(sph, rays // 2, rays - rays // 2, 4096, 2048, seed=0)
     n = org.shape[0]
     ot = torch.zeros((n, 4), device="cuda")
     dt = torch.zeros((n, 4), device="cuda")
@@ -218,11 +217,17 @@ def microbench(torch, GpuBVHAccel, scenes, reps=3):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-micro", action="store_true", help="skip the intersection microbench")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-API measurement")
+    ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel profile (roofline)")
+    ap.add_argument("--width", type=int, default=1920, help="film width (profiling cases only)")
+    ap.add_argument("--height", type=int, default=1080, help="film height (profiling cases only)")
+    ap.add_argument("--micro-only", type=int, default=0, metavar="RAYS",
+                    help="only the intersection microbench, on RAYS rays (profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -236,7 +241,10 @@ def main():
     from spica_gb300 import GpuBVHAccel, GpuPathIntegrator, scenes
     from spica_gb300.gpu import KERNEL_CLASSES
 
-    scene = scenes.mid_scale()
+    if args.micro_only:
+        print(json.dumps({"microbench": microbench(torch, GpuBVHAccel, scenes, rays=args.micro_only)}), flush=True)
+        return 0
+    scene = scenes.mid_scale(width=args.width, height=args.height)
     W, H, md = scene.width, scene.height, scene.max_depth
     npix = W * H
     acc = GpuBVHAccel(scene, device=local).construct()
@@ -272,21 +280,28 @@ def main():
     rays = st.rays_closest + st.rays_shadow
 
     # end to end through the host entry point, pinned host film copied both ways per step
-    host_film = torch.zeros((H, W, 4), dtype=torch.float32).pin_memory()
-    hf = host_film.numpy()
-    integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=1 << 16)
-    barrier()
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=(1 << 16) + 1 + k)
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = ws * args.steps * npix / e2e_s
     film_bytes = npix * 16
+    e2e_value = None
+    if not args.no_e2e:
+        host_film = torch.zeros((H, W, 4), dtype=torch.float32).pin_memory()
+        hf = host_film.numpy()
+        integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=1 << 16)
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=(1 << 16) + 1 + k)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        e2e_value = ws * args.steps * npix / e2e_s
 
     if rank != 0:
         return 0
 
+    if args.no_profile:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                          "config": dict(CONFIG, width=W, height=H), "profiling_case": True}), flush=True)
+        return 0
     # per-kernel profile: event-timed launches of 2 passes, then visit counters
     prof_film = torch.zeros_like(film)
     pr = integ.profile_device(scene.camera, acc, dict(params, sampleCount=2), prof_film, sample_offset=1 << 20,
@@ -318,8 +333,9 @@ def main():
                            bvh_build_ms=info.build_ms),
             "mrays_s": ws * args.steps * rays / max(st.paths, 1) * npix / (ms / 1e3) / 1e6 if st.paths else None,
             "rays_per_path": rays / max(st.paths, 1),
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": film_bytes + 80,
-                    "d2h_bytes_per_step": film_bytes},
+            "e2e": None if e2e_value is None else {"value": e2e_value, "unit": UNIT,
+                                                   "h2d_bytes_per_step": film_bytes + 80,
+                                                   "d2h_bytes_per_step": film_bytes},
             "gpu_launches": int(args.steps * (2 + 5 * (md + 1))), "clocks": clk, "roofline": roofline,
             "kernels": kernels}
     if not args.no_micro:

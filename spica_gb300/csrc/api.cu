@@ -199,6 +199,14 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(const float4 *__restrict_
         if (ANY) {
             outAny[i] = hit ? 1u : 0u;
         } else {
+            if (hit) {
+                // near-grazing hits (|cos| < 0.1 between ray and triangle normal): the
+                // FP32 distance is re-evaluated in FP64 to keep 1e-5 relative accuracy
+                const TriRecord tr = tris[slot];
+                const float3 n = cross(xyz(tr.v1) - xyz(tr.v0), xyz(tr.v2) - xyz(tr.v0));
+                const float dn = fabsf(dot(xyz(d), n));
+                if (dn < 0.1f * length(n)) refineHitFP64(tr, xyz(o), xyz(d), &tmax, &u, &v);
+            }
             spgpu_hit h;
             h.t = hit ? tmax : 0.0f;
             h.prim = hit ? __float_as_int(__ldg(&tris[slot].v0.w)) : -1;

@@ -15,7 +15,7 @@
 //      Children are placed in slots by a greedy octant assignment so that the
 //      traversal's slot order s ^ (7 - octant) runs roughly front to back, their
 //      boxes are quantised conservatively to 8 bits on the node's grid, and leaf
-//      triangles are copied into leaf order as (v0, e1, e2) records.
+//      triangles are copied into leaf order as (v0, v1, v2) records.
 // The triangle set, and so the closest hit of every ray, is the reference's; only
 // the tree differs.  Its build is deterministic (no atomics decide structure).
 #include <cub/device/device_radix_sort.cuh>
@@ -353,8 +353,8 @@ __global__ void k_collapse(CollapseArgs A, const int2 *__restrict__ items, int n
                 const float *v = A.verts + 9 * static_cast<int64_t>(prim);
                 TriRecord r;
                 r.v0 = make_float4(v[0], v[1], v[2], __int_as_float(static_cast<int>(prim)));
-                r.e1 = make_float4(v[3] - v[0], v[4] - v[1], v[5] - v[2], 0.0f);
-                r.e2 = make_float4(v[6] - v[0], v[7] - v[1], v[8] - v[2], 0.0f);
+                r.v1 = make_float4(v[3], v[4], v[5], 0.0f);
+                r.v2 = make_float4(v[6], v[7], v[8], 0.0f);
                 A.tris[triBase + triOff + q] = r;
                 A.slot_shade[triBase + triOff + q] =
                     make_int2(A.tri_mat ? A.tri_mat[prim] : 0, A.tri_light ? A.tri_light[prim] : -1);

@@ -146,9 +146,9 @@ __device__ __forceinline__ bool traceWide(const WideNode *__restrict__ nodes, co
             }
             if (STATS) (*triCount)++;
             const float4 v0 = __ldg(&tris[ti].v0);
-            const float4 e1 = __ldg(&tris[ti].e1);
-            const float4 e2 = __ldg(&tris[ti].e2);
-            const float3 E1 = xyz(e1), E2 = xyz(e2);
+            const float4 v1 = __ldg(&tris[ti].v1);
+            const float4 v2 = __ldg(&tris[ti].v2);
+            const float3 E1 = xyz(v1) - xyz(v0), E2 = xyz(v2) - xyz(v0);
             const float3 pv = cross(d, E2);
             const float det = dot(E1, pv);
             if (det > -kEpsT && det < kEpsT) continue;

@@ -64,13 +64,40 @@ struct alignas(16) WideNode {
 };
 static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
 
-// Triangle record in leaf order: 3 x float4 = 48 bytes.
-//   v0.xyz + primitive id (int bits in .w), e1 = v1 - v0, e2 = v2 - v0
+// Triangle record in leaf order: 3 x float4 = 48 bytes, the input vertices unchanged
+// (edges are formed in registers, so an exact FP64 re-evaluation stays possible):
+//   v0.xyz + primitive id (int bits in .w), v1.xyz, v2.xyz
 struct alignas(16) TriRecord {
     float4 v0;
-    float4 e1;
-    float4 e2;
+    float4 v1;
+    float4 v2;
 };
+
+// Moller-Trumbore of the reference (core/triangle.cc:98) re-evaluated in double for
+// one ray / triangle pair, with the direction renormalised in double as the
+// reference's Ray constructor does (core/ray.cc:15).  Used for near-grazing hits,
+// where the FP32 distance loses relative accuracy in proportion to 1/cos(theta).
+__device__ __forceinline__ void refineHitFP64(const TriRecord &tr, float3 o, float3 d, float *t, float *u,
+                                              float *v) {
+    const double ox = o.x, oy = o.y, oz = o.z;
+    const double dn = sqrt(static_cast<double>(d.x) * d.x + static_cast<double>(d.y) * d.y +
+                           static_cast<double>(d.z) * d.z);
+    const double dx = d.x / dn, dy = d.y / dn, dz = d.z / dn;
+    const double ax = tr.v0.x, ay = tr.v0.y, az = tr.v0.z;
+    const double e1x = static_cast<double>(tr.v1.x) - ax, e1y = static_cast<double>(tr.v1.y) - ay,
+                 e1z = static_cast<double>(tr.v1.z) - az;
+    const double e2x = static_cast<double>(tr.v2.x) - ax, e2y = static_cast<double>(tr.v2.y) - ay,
+                 e2z = static_cast<double>(tr.v2.z) - az;
+    const double px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+    const double det = e1x * px + e1y * py + e1z * pz;
+    if (det == 0.0) return;
+    const double inv = 1.0 / det;
+    const double tx = ox - ax, ty = oy - ay, tz = oz - az;
+    const double qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+    *u = static_cast<float>((tx * px + ty * py + tz * pz) * inv);
+    *v = static_cast<float>((dx * qx + dy * qy + dz * qz) * inv);
+    *t = static_cast<float>((e2x * qx + e2y * qy + e2z * qz) * inv);
+}
 
 // Closest-hit record (16 B): t, primitive id (-1 = miss), barycentric u, v.
 struct alignas(16) HitRecord {

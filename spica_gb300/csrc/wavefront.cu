@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
             spec = bt.w != 0.0f;
             const int fi = filmIndex(p, pid);
             const TriRecord tr = S.tris[h.prim];
-            const float3 n = normalize(cross(xyz(tr.e1), xyz(tr.e2)));
+            const float3 n = normalize(cross(xyz(tr.v1) - xyz(tr.v0), xyz(tr.v2) - xyz(tr.v0)));
             const int2 sh = __ldg(&S.slotShade[h.prim]);
             const MaterialRecord m = S.mats[sh.x];
             const float3 d = xyz(d4);
