@@ -179,43 +179,47 @@ void freeScene(Ctx &C) {
 
 // --------------------------------------------------------------------------- tracing
 template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(kTraceBlock) k_trace(const float4 *__restrict__ org, const float4 *__restrict__ dir,
-                                                       int64_t n, const WideNode *__restrict__ nodes,
+__global__ void __launch_bounds__(kTraceBlock, 8) k_trace(const float4 *__restrict__ org, const float4 *__restrict__ dir,
+                                                       int n, const WideNode *__restrict__ nodes,
                                                        const TriRecord *__restrict__ tris, uint32_t nNodes,
                                                        uint32_t nTris, spgpu_hit *__restrict__ outHit,
-                                                       uint32_t *__restrict__ outAny, int *err,
+                                                       uint32_t *__restrict__ outAny, int *ctl,
                                                        unsigned long long *stats) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     uint32_t nodeCount = 0, triCount = 0;
     bool overflow = false;
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const float4 o = org[i], d = dir[i];
-        float tmax = d.w;
-        int slot = -1;
-        float u = 0.0f, v = 0.0f;
-        const bool hit = traceWide<ANY, STATS>(nodes, tris, nNodes, nTris, xyz(o), xyz(d), o.w, tmax, slot, u, v,
-                                               stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow);
+    auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
+        const float4 a = org[i], b = dir[i];
+        *o = xyz(a);
+        *d = xyz(b);
+        *t0 = a.w;
+        *t1 = b.w;
+    };
+    auto done = [&](int i, const TraceLane &L) {
+        if (i < 0) return;
         if (ANY) {
-            outAny[i] = hit ? 1u : 0u;
-        } else {
-            if (hit) {
-                // near-grazing hits (|cos| < 0.1 between ray and triangle normal): the
-                // FP32 distance is re-evaluated in FP64 to keep 1e-5 relative accuracy
-                const TriRecord tr = tris[slot];
-                const float3 n = cross(xyz(tr.v1) - xyz(tr.v0), xyz(tr.v2) - xyz(tr.v0));
-                const float dn = fabsf(dot(xyz(d), n));
-                if (dn < 0.1f * length(n)) refineHitFP64(tr, xyz(o), xyz(d), &tmax, &u, &v);
-            }
-            spgpu_hit h;
-            h.t = hit ? tmax : 0.0f;
-            h.prim = hit ? __float_as_int(__ldg(&tris[slot].v0.w)) : -1;
-            h.u = u;
-            h.v = v;
-            reinterpret_cast<float4 *>(outHit)[i] = *reinterpret_cast<float4 *>(&h);
+            outAny[i] = L.found ? 1u : 0u;
+            return;
         }
-    }
-    if (overflow) atomicOr(err, 1);
+        float t = L.tmax, u = L.hu, v = L.hv;
+        int prim = -1;
+        if (L.found) {
+            // The FP32 distance has relative error ~ eps * kappa with
+            // kappa = (|o - v0| / t + 1) * |e1| |e2| / |det| (grazing incidence or a hit
+            // very close to the origin); such hits are re-evaluated in FP64 to keep 1e-5
+            // relative accuracy.
+            const TriRecord tr = tris[L.hitSlot];
+            const float3 e1 = xyz(tr.v1) - xyz(tr.v0), e2 = xyz(tr.v2) - xyz(tr.v0);
+            const float det = fabsf(dot(e1, cross(L.d, e2)));
+            const float kappa = (length(L.o - xyz(tr.v0)) / t + 1.0f) * length(e1) * length(e2);
+            if (!(kappa < 16.0f * det)) refineHitFP64(tr, L.o, L.d, &t, &u, &v);
+            prim = __float_as_int(tr.v0.w);
+        }
+        reinterpret_cast<float4 *>(outHit)[i] = make_float4(L.found ? t : 0.0f, __int_as_float(prim), u, v);
+    };
+    tracePersistent<ANY, STATS>(nodes, tris, nNodes, nTris, n, ctl + 1, stack + threadIdx.x, kTraceBlock, &nodeCount,
+                                &triCount, &overflow, fetch, done);
+    if (overflow) atomicOr(ctl, 1);
     if (STATS) {
         atomicAdd(&stats[0], static_cast<unsigned long long>(nodeCount));
         atomicAdd(&stats[1], static_cast<unsigned long long>(triCount));
@@ -226,6 +230,13 @@ int numSMs(int device) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     return sms > 0 ? sms : 1;
+}
+
+// persistent grid: every block resident at once (SMs x blocks per SM)
+int residentTraceBlocks(int device) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<false, false>, kTraceBlock, 0);
+    return numSMs(device) * (occ > 0 ? occ : 1);
 }
 
 int launchTrace(Ctx &C, int any, const float *org, const float *dir, int64_t n, void *out, cudaStream_t s,
@@ -243,23 +254,27 @@ int launchTrace(Ctx &C, int any, const float *org, const float *dir, int64_t n, 
         return SPGPU_EINVAL;
     }
     if (n == 0) return 0;
-    cudaError_t e = cudaMemsetAsync(C.traceErr, 0, sizeof(int), s);
+    if (n > (int64_t(1) << 30)) {
+        setError("spgpu_trace: at most 2^30 rays per call");
+        return SPGPU_EINVAL;
+    }
+    cudaError_t e = cudaMemsetAsync(C.traceErr, 0, 2 * sizeof(int), s);
     if (e != cudaSuccess) return cudaFail("cudaMemsetAsync", e);
     const int64_t blocksNeeded = (n + kTraceBlock - 1) / kTraceBlock;
-    const int grid = static_cast<int>(std::min<int64_t>(blocksNeeded, static_cast<int64_t>(numSMs(C.device)) * 8));
+    const int grid = static_cast<int>(std::min<int64_t>(blocksNeeded, static_cast<int64_t>(residentTraceBlocks(C.device))));
     const uint32_t NN = static_cast<uint32_t>(C.bvh.n_nodes), NT = static_cast<uint32_t>(C.bvh.ntri);
     const float4 *o4 = reinterpret_cast<const float4 *>(org);
     const float4 *d4 = reinterpret_cast<const float4 *>(dir);
     if (any) {
-        if (stats) k_trace<true, true><<<grid, kTraceBlock, 0, s>>>(o4, d4, n, C.bvh.nodes, C.bvh.tris, NN, NT, nullptr,
+        if (stats) k_trace<true, true><<<grid, kTraceBlock, 0, s>>>(o4, d4, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN, NT, nullptr,
                                                                     static_cast<uint32_t *>(out), C.traceErr, C.traceStats);
-        else k_trace<true, false><<<grid, kTraceBlock, 0, s>>>(o4, d4, n, C.bvh.nodes, C.bvh.tris, NN, NT, nullptr,
+        else k_trace<true, false><<<grid, kTraceBlock, 0, s>>>(o4, d4, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN, NT, nullptr,
                                                                static_cast<uint32_t *>(out), C.traceErr, C.traceStats);
     } else {
-        if (stats) k_trace<false, true><<<grid, kTraceBlock, 0, s>>>(o4, d4, n, C.bvh.nodes, C.bvh.tris, NN, NT,
+        if (stats) k_trace<false, true><<<grid, kTraceBlock, 0, s>>>(o4, d4, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN, NT,
                                                                      static_cast<spgpu_hit *>(out), nullptr, C.traceErr,
                                                                      C.traceStats);
-        else k_trace<false, false><<<grid, kTraceBlock, 0, s>>>(o4, d4, n, C.bvh.nodes, C.bvh.tris, NN, NT,
+        else k_trace<false, false><<<grid, kTraceBlock, 0, s>>>(o4, d4, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN, NT,
                                                                 static_cast<spgpu_hit *>(out), nullptr, C.traceErr,
                                                                 C.traceStats);
     }
@@ -421,7 +436,7 @@ int spgpu_create(const spgpu_config *cfg, spgpu_ctx **out) {
     C.device = cfg ? cfg->device : 0;
     cudaError_t e = cudaSetDevice(C.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&C.traceErr, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&C.traceErr, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&C.traceStats, 4 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         const int rc = cudaFail("spgpu_create", e);

@@ -42,140 +42,251 @@ struct TraceStats {   // per-ray visit counters, for the roofline's algorithmic 
 // Any hit returns on the first triangle with t in (eps, tmax].
 // Returns false and sets *overflow if the tree is deeper than the stack.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float byteToFloat(uint32_t w, int k) { return static_cast<float>((w >> (8 * k)) & 0xFFu); }
+// byte k of w as an exact float: PRMT assembles 0x4B0000bb (= 2^23 + b), then one FADD
+__device__ __forceinline__ float byteToFloat(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | static_cast<uint32_t>(k))) - 8388608.0f;
+}
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+// Per 4 child slots at once (one byte each): the bit index of the slot's hit bits in
+// the 32-bit hit mask and the bits themselves.  Internal children (meta 0b001_11sss)
+// land on bit 24 + (s ^ octInv), leaves on their triangle offset with 1..3 bits.
+__device__ __forceinline__ void metaDecode4(uint32_t meta4, uint32_t octInv4, uint32_t *bitIndex4,
+                                           uint32_t *childBits4) {
+    const uint32_t isInner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+    const uint32_t innerMask4 = __byte_perm(isInner4 << 3, 0u, 0xBA98u);   // 0xFF where internal
+    *bitIndex4 = (meta4 ^ (octInv4 & innerMask4)) & 0x1F1F1F1Fu;
+    *childBits4 = (meta4 >> 5) & 0x07070707u;
+}
 
 // Every node and triangle index is checked against the tree's sizes and the loop is
 // bounded (kMaxVisits), so a malformed tree ends the ray with *overflow set instead of
 // reading out of bounds or spinning.
 constexpr uint32_t kMaxVisits = 1u << 22;
 
+// Traversal state of one ray, kept in registers between steps so that a warp can
+// retire finished rays and start new ones in the middle of a traversal.
+struct TraceLane {
+    float3 o, d, idir;
+    float tmin, tmax, tEps;
+    uint32_t octant, octInv;
+    uint2 G;          // node group: child base, pending-child bits (visit order) | internal mask
+    int sp;
+    uint32_t visits;
+    int hitSlot;
+    float hu, hv;
+    bool found;
+};
+
+__device__ __forceinline__ void laneInit(TraceLane &L, float3 o, float3 d, float tmin, float tmax) {
+    L.o = o;
+    L.d = d;
+    L.idir = mk(d.x == 0.0f ? kInfT : 1.0f / d.x, d.y == 0.0f ? kInfT : 1.0f / d.y, d.z == 0.0f ? kInfT : 1.0f / d.z);
+    L.octant = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    L.octInv = 7u - L.octant;
+    L.tmin = tmin;
+    L.tmax = tmax;
+    L.tEps = fmaxf(tmin, kEpsT);
+    L.G = make_uint2(0u, (1u << (24 + L.octInv)) | 1u);   // the root as slot 0 of a virtual parent
+    L.sp = 0;
+    L.visits = 0;
+    L.hitSlot = -1;
+    L.hu = L.hv = 0.0f;
+    L.found = false;
+}
+
+// One step of the traversal: open the next pending child of the current node group
+// (popping a group from the stack first when the current one is exhausted) and test
+// the triangles of the leaves it hits.  Returns true when the ray is finished.
+template <bool ANY, bool STATS>
+__device__ __forceinline__ bool laneStep(TraceLane &L, const WideNode *__restrict__ nodes,
+                                         const TriRecord *__restrict__ tris, uint32_t nNodes, uint32_t nTris,
+                                         uint2 *__restrict__ stack, int stride, uint2 *spill, uint32_t *nodeCount,
+                                         uint32_t *triCount, bool *overflow) {
+    if (++L.visits > kMaxVisits) {
+        *overflow = true;
+        return true;
+    }
+    if (!(L.G.y & 0xFF000000u)) {
+        if (L.sp == 0) return true;
+        L.sp--;
+        L.G = L.sp < kStackShared ? stack[L.sp * stride] : spill[L.sp - kStackShared];
+    }
+    const uint32_t key = __ffs(L.G.y >> 24) - 1;
+    L.G.y &= ~(1u << (24 + key));
+    const uint32_t slot = key ^ L.octInv;
+    const uint32_t child = L.G.x + __popc((L.G.y & 0xFFu) & ((1u << slot) - 1u));
+    if (child >= nNodes) {
+        *overflow = true;
+        return true;
+    }
+    if (L.G.y & 0xFF000000u) {
+        if (L.sp >= kStackDepth) {
+            *overflow = true;
+            return true;
+        }
+        if (L.sp < kStackShared) stack[L.sp * stride] = L.G;
+        else spill[L.sp - kStackShared] = L.G;
+        L.sp++;
+    }
+    if (STATS) (*nodeCount)++;
+    const float4 *nodes4 = reinterpret_cast<const float4 *>(nodes);
+    const float4 n0 = __ldg(nodes4 + 5 * child + 0);
+    const float4 n1 = __ldg(nodes4 + 5 * child + 1);
+    const float4 n2 = __ldg(nodes4 + 5 * child + 2);
+    const float4 n3 = __ldg(nodes4 + 5 * child + 3);
+    const float4 n4 = __ldg(nodes4 + 5 * child + 4);
+    const uint32_t ew = __float_as_uint(n0.w);
+    const float sx = __uint_as_float((ew & 0xFFu) << 23);
+    const float sy = __uint_as_float(((ew >> 8) & 0xFFu) << 23);
+    const float sz = __uint_as_float(((ew >> 16) & 0xFFu) << 23);
+    const float ax = sx * L.idir.x, ay = sy * L.idir.y, az = sz * L.idir.z;
+    const float bx = (n0.x - L.o.x) * L.idir.x, by = (n0.y - L.o.y) * L.idir.y, bz = (n0.z - L.o.z) * L.idir.z;
+    // near / far quantised planes per axis, swapped for negative directions
+    const uint2 qlx = make_uint2(__float_as_uint(n2.x), __float_as_uint(n2.y));
+    const uint2 qly = make_uint2(__float_as_uint(n2.z), __float_as_uint(n2.w));
+    const uint2 qlz = make_uint2(__float_as_uint(n3.x), __float_as_uint(n3.y));
+    const uint2 qhx = make_uint2(__float_as_uint(n3.z), __float_as_uint(n3.w));
+    const uint2 qhy = make_uint2(__float_as_uint(n4.x), __float_as_uint(n4.y));
+    const uint2 qhz = make_uint2(__float_as_uint(n4.z), __float_as_uint(n4.w));
+    const uint2 nx = (L.octant & 1u) ? qhx : qlx, fx = (L.octant & 1u) ? qlx : qhx;
+    const uint2 ny = (L.octant & 2u) ? qhy : qly, fy = (L.octant & 2u) ? qly : qhy;
+    const uint2 nz = (L.octant & 4u) ? qhz : qlz, fz = (L.octant & 4u) ? qlz : qhz;
+    const uint32_t octInv4 = L.octInv * 0x01010101u;
+    uint32_t bidx[2], cbits[2];
+    metaDecode4(__float_as_uint(n1.z), octInv4, &bidx[0], &cbits[0]);
+    metaDecode4(__float_as_uint(n1.w), octInv4, &bidx[1], &cbits[1]);
+    uint32_t hitmask = 0u;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int h = k >> 2, b = k & 3;
+        const float tnx = fmaf(byteToFloat(h ? nx.y : nx.x, b), ax, bx);
+        const float tny = fmaf(byteToFloat(h ? ny.y : ny.x, b), ay, by);
+        const float tnz = fmaf(byteToFloat(h ? nz.y : nz.x, b), az, bz);
+        const float tfx = fmaf(byteToFloat(h ? fx.y : fx.x, b), ax, bx);
+        const float tfy = fmaf(byteToFloat(h ? fy.y : fy.x, b), ay, by);
+        const float tfz = fmaf(byteToFloat(h ? fz.y : fz.x, b), az, bz);
+        const float t0 = fmaxf(fmax3f(tnx, tny, tnz), L.tmin);
+        const float t1 = fminf(fmin3f(tfx, tfy, tfz), L.tmax);
+        const uint32_t bits = (cbits[h] >> (8 * b)) & 0xFFu;
+        const uint32_t shift = (bidx[h] >> (8 * b)) & 0xFFu;
+        if (t0 <= t1 * 1.0000010f) hitmask |= bits << shift;
+    }
+    L.G = make_uint2(__float_as_uint(n1.x), (hitmask & 0xFF000000u) | (ew >> 24));
+    uint32_t tbits = hitmask & 0x00FFFFFFu;
+    const uint32_t tbase = __float_as_uint(n1.y);
+    while (tbits) {
+        const int b = __ffs(tbits) - 1;
+        tbits &= tbits - 1u;
+        const uint32_t ti = tbase + static_cast<uint32_t>(b);
+        if (ti >= nTris) {
+            *overflow = true;
+            return true;
+        }
+        if (STATS) (*triCount)++;
+        const float4 v0 = __ldg(&tris[ti].v0);
+        const float4 v1 = __ldg(&tris[ti].v1);
+        const float4 v2 = __ldg(&tris[ti].v2);
+        const float3 E1 = xyz(v1) - xyz(v0), E2 = xyz(v2) - xyz(v0);
+        const float3 pv = cross(L.d, E2);
+        const float det = dot(E1, pv);
+        if (det > -kEpsT && det < kEpsT) continue;
+        const float inv = 1.0f / det;
+        const float3 tv = L.o - xyz(v0);
+        const float u = dot(tv, pv) * inv;
+        if (u < 0.0f || u > 1.0f) continue;
+        const float3 qv = cross(tv, E1);
+        const float v = dot(L.d, qv) * inv;
+        if (v < 0.0f || u + v > 1.0f) continue;
+        const float t = dot(E2, qv) * inv;
+        if (t <= L.tEps || t > L.tmax) continue;
+        L.found = true;
+        if (ANY) return true;
+        L.tmax = t;
+        L.hitSlot = static_cast<int>(ti);
+        L.hu = u;
+        L.hv = v;
+    }
+    return !(L.G.y & 0xFF000000u) && L.sp == 0;
+}
+
 template <bool ANY, bool STATS>
 __device__ __forceinline__ bool traceWide(const WideNode *__restrict__ nodes, const TriRecord *__restrict__ tris,
                                           uint32_t nNodes, uint32_t nTris, float3 o, float3 d, float tmin,
                                           float &tmax, int &hitSlot, float &hu, float &hv, uint2 *__restrict__ stack,
                                           int stride, uint32_t *nodeCount, uint32_t *triCount, bool *overflow) {
-    const float3 idir = mk(d.x == 0.0f ? kInfT : 1.0f / d.x, d.y == 0.0f ? kInfT : 1.0f / d.y,
-                           d.z == 0.0f ? kInfT : 1.0f / d.z);
-    const uint32_t octant = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-    const uint32_t octInv = 7u - octant;
-    const float tEps = fmaxf(tmin, kEpsT);
-    bool found = false;
-
     uint2 spill[kStackDepth - kStackShared];
-    uint2 G = make_uint2(0u, (1u << (24 + octInv)) | 1u);   // the root as slot 0 of a virtual parent
-    uint2 T = make_uint2(0u, 0u);
-    int sp = 0;
-    uint32_t visits = 0;
-    const float4 *nodes4 = reinterpret_cast<const float4 *>(nodes);
+    TraceLane L;
+    laneInit(L, o, d, tmin, tmax);
+    while (!laneStep<ANY, STATS>(L, nodes, tris, nNodes, nTris, stack, stride, spill, nodeCount, triCount,
+                                 overflow)) {
+    }
+    tmax = L.tmax;
+    hitSlot = L.hitSlot;
+    hu = L.hu;
+    hv = L.hv;
+    return L.found;
+}
 
+// Persistent driver: a warp keeps up to 32 rays in flight and refills the lanes whose
+// rays have finished, kRefill or more at a time, from a global ray counter (one
+// atomicAdd per refill), so lanes do not idle while the slowest ray of a batch finishes
+// (after Aila and Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG
+// 2009).  fetch(i, &o, &d, &tmin, &tmax) loads ray i; done(i, L) consumes its result.
+// All 32 lanes of each warp execute every iteration of the loop (warp-uniform control),
+// so done() may use warp-collective operations.
+constexpr int kRefill = 8;
+
+template <bool ANY, bool STATS, class Fetch, class Done>
+__device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nodes,
+                                                const TriRecord *__restrict__ tris, uint32_t nNodes,
+                                                uint32_t nTris, int n, int *rayCounter, uint2 *__restrict__ stack,
+                                                int stride, uint32_t *nodeCount, uint32_t *triCount,
+                                                bool *overflow, Fetch fetch, Done done) {
+    uint2 spill[kStackDepth - kStackShared];
+    TraceLane L;
+    int ray = -1;          // >= 0 in flight, -1 idle, -2 no work left
+    bool finished = false;   // ray finished in the last step, result not yet consumed
+    const int lane = threadIdx.x & 31;
     while (true) {
-        if (++visits > kMaxVisits) {
-            *overflow = true;
-            return found;
+        done(finished ? ray : -1, L);
+        if (finished) {
+            ray = -1;
+            finished = false;
         }
-        if (G.y & 0xFF000000u) {
-            const uint32_t key = __ffs(G.y >> 24) - 1;
-            G.y &= ~(1u << (24 + key));
-            const uint32_t slot = key ^ octInv;
-            const uint32_t child = G.x + __popc((G.y & 0xFFu) & ((1u << slot) - 1u));
-            if (child >= nNodes) {
-                *overflow = true;
-                return found;
-            }
-            if (G.y & 0xFF000000u) {
-                if (sp >= kStackDepth) {
-                    *overflow = true;
-                    return found;
-                }
-                if (sp < kStackShared) stack[sp * stride] = G;
-                else spill[sp - kStackShared] = G;
-                sp++;
-            }
-            if (STATS) (*nodeCount)++;
-            const float4 n0 = __ldg(nodes4 + 5 * child + 0);
-            const float4 n1 = __ldg(nodes4 + 5 * child + 1);
-            const float4 n2 = __ldg(nodes4 + 5 * child + 2);
-            const float4 n3 = __ldg(nodes4 + 5 * child + 3);
-            const float4 n4 = __ldg(nodes4 + 5 * child + 4);
-            const uint32_t ew = __float_as_uint(n0.w);
-            const float sx = __uint_as_float((ew & 0xFFu) << 23);
-            const float sy = __uint_as_float(((ew >> 8) & 0xFFu) << 23);
-            const float sz = __uint_as_float(((ew >> 16) & 0xFFu) << 23);
-            const float ax = sx * idir.x, ay = sy * idir.y, az = sz * idir.z;
-            const float bx = (n0.x - o.x) * idir.x, by = (n0.y - o.y) * idir.y, bz = (n0.z - o.z) * idir.z;
-            // near / far quantised planes per axis, swapped for negative directions
-            const uint2 qlx = make_uint2(__float_as_uint(n2.x), __float_as_uint(n2.y));
-            const uint2 qly = make_uint2(__float_as_uint(n2.z), __float_as_uint(n2.w));
-            const uint2 qlz = make_uint2(__float_as_uint(n3.x), __float_as_uint(n3.y));
-            const uint2 qhx = make_uint2(__float_as_uint(n3.z), __float_as_uint(n3.w));
-            const uint2 qhy = make_uint2(__float_as_uint(n4.x), __float_as_uint(n4.y));
-            const uint2 qhz = make_uint2(__float_as_uint(n4.z), __float_as_uint(n4.w));
-            const uint2 nx = (octant & 1u) ? qhx : qlx, fx = (octant & 1u) ? qlx : qhx;
-            const uint2 ny = (octant & 2u) ? qhy : qly, fy = (octant & 2u) ? qly : qhy;
-            const uint2 nz = (octant & 4u) ? qhz : qlz, fz = (octant & 4u) ? qlz : qhz;
-            const uint32_t meta0 = __float_as_uint(n1.z), meta1 = __float_as_uint(n1.w);
-            uint32_t hitmask = 0u;
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-                const int h = k >> 2, b = k & 3;
-                const uint32_t m = ((h ? meta1 : meta0) >> (8 * b)) & 0xFFu;
-                const float tnx = fmaf(byteToFloat(h ? nx.y : nx.x, b), ax, bx);
-                const float tny = fmaf(byteToFloat(h ? ny.y : ny.x, b), ay, by);
-                const float tnz = fmaf(byteToFloat(h ? nz.y : nz.x, b), az, bz);
-                const float tfx = fmaf(byteToFloat(h ? fx.y : fx.x, b), ax, bx);
-                const float tfy = fmaf(byteToFloat(h ? fy.y : fy.x, b), ay, by);
-                const float tfz = fmaf(byteToFloat(h ? fz.y : fz.x, b), az, bz);
-                const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-                const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-                if (m != 0u && t0 <= t1 * 1.0000010f) {
-                    if ((m & 0x18u) == 0x18u) hitmask |= 1u << (24 + (k ^ octInv));
-                    else hitmask |= (m >> 5) << (m & 0x1Fu);
+        const unsigned idle = __ballot_sync(0xffffffffu, ray == -1);
+        const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0);
+        if (idle && (__popc(idle) >= kRefill || busy == 0)) {
+            int base = 0;
+            if (lane == __ffs(idle) - 1) base = atomicAdd(rayCounter, __popc(idle));
+            base = __shfl_sync(0xffffffffu, base, __ffs(idle) - 1);
+            if (ray == -1) {
+                const int r = base + __popc(idle & ((1u << lane) - 1u));
+                if (r < n) {
+                    float3 o, d;
+                    float t0, t1;
+                    fetch(r, &o, &d, &t0, &t1);
+                    laneInit(L, o, d, t0, t1);
+                    ray = r;
+                } else {
+                    ray = -2;
                 }
             }
-            G = make_uint2(__float_as_uint(n1.x), (hitmask & 0xFF000000u) | (ew >> 24));
-            T = make_uint2(__float_as_uint(n1.y), hitmask & 0x00FFFFFFu);
         }
-
-        while (T.y) {
-            const int b = __ffs(T.y) - 1;
-            T.y &= T.y - 1u;
-            const int ti = static_cast<int>(T.x) + b;
-            if (static_cast<uint32_t>(ti) >= nTris) {
-                *overflow = true;
-                return found;
-            }
-            if (STATS) (*triCount)++;
-            const float4 v0 = __ldg(&tris[ti].v0);
-            const float4 v1 = __ldg(&tris[ti].v1);
-            const float4 v2 = __ldg(&tris[ti].v2);
-            const float3 E1 = xyz(v1) - xyz(v0), E2 = xyz(v2) - xyz(v0);
-            const float3 pv = cross(d, E2);
-            const float det = dot(E1, pv);
-            if (det > -kEpsT && det < kEpsT) continue;
-            const float inv = 1.0f / det;
-            const float3 tv = o - xyz(v0);
-            const float u = dot(tv, pv) * inv;
-            if (u < 0.0f || u > 1.0f) continue;
-            const float3 qv = cross(tv, E1);
-            const float v = dot(d, qv) * inv;
-            if (v < 0.0f || u + v > 1.0f) continue;
-            const float t = dot(E2, qv) * inv;
-            if (t <= tEps || t > tmax) continue;
-            found = true;
-            if (ANY) return true;
-            tmax = t;
-            hitSlot = ti;
-            hu = u;
-            hv = v;
-        }
-
-        if (!(G.y & 0xFF000000u)) {
-            if (sp == 0) break;
-            sp--;
-            G = sp < kStackShared ? stack[sp * stride] : spill[sp - kStackShared];
+        if (__all_sync(0xffffffffu, ray == -2)) break;
+        if (ray >= 0) {
+            finished = laneStep<ANY, STATS>(L, nodes, tris, nNodes, nTris, stack, stride, spill, nodeCount,
+                                            triCount, overflow);
         }
     }
-    return found;
 }
 
 // host entry points (bvh.cu)

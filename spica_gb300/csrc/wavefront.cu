@@ -53,7 +53,8 @@ struct PassArgs {
     HitRecord *hits;
     int *classQ;
     float4 *shO, *shD, *shL;
-    int *counters;     // per bounce: [0] rays in, [1..3] class counts, [4] shadow rays
+    int *counters;     // per bounce: [0] rays in, [1..3] class counts, [4] shadow rays,
+                       // [5] / [6] extend / shadow ray-fetch counters
     int *ctl;          // [0] sample index of the pass
     unsigned long long *stats;
     unsigned long long *visit;   // [0..1] extend nodes / triangles, [2..3] shadow nodes / triangles
@@ -190,40 +191,39 @@ __global__ void k_raygen(PassArgs p) {
 }
 
 template <bool STATS>
-__global__ void __launch_bounds__(kTraceBlock) k_extend(PassArgs p, int b) {
+__global__ void __launch_bounds__(kTraceBlock, 8) k_extend(PassArgs p, int b) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     uint32_t nodeCount = 0, triCount = 0;
-    const int *cnt = p.counters + b * kCountersPerBounce;
-    int *classCnt = p.counters + b * kCountersPerBounce + 1;
+    int *cnt = p.counters + b * kCountersPerBounce;
+    int *classCnt = cnt + 1;
     const int n = cnt[0];
     const float4 *rO = (b & 1) ? p.rayO1 : p.rayO0;
     const float4 *rD = (b & 1) ? p.rayD1 : p.rayD0;
     bool overflow = false;
-    const int stride = gridDim.x * blockDim.x;
-    const int nIter = (n + stride - 1) / stride;   // uniform trip count keeps warps whole for the ballots
-    for (int it = 0; it < nIter; it++) {
-        const int i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const bool live = i < n;
+    auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
+        const float4 d4 = rD[i];
+        *o = xyz(rO[i]);
+        *d = xyz(d4);
+        *t0 = 0.0f;
+        *t1 = d4.w;
+    };
+    auto done = [&](int i, const TraceLane &L) {
+        if (!__any_sync(0xffffffffu, i >= 0)) return;
         int cls = -1;
-        if (live) {
-            const float4 o4 = rO[i], d4 = rD[i];
-            float tmax = d4.w, u = 0.0f, v = 0.0f;
-            int slot = -1;
-            const bool hit = traceWide<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(o4), xyz(d4),
-                                                     0.0f, tmax, slot, u, v, stack + threadIdx.x, kTraceBlock,
-                                                     &nodeCount, &triCount, &overflow);
-            if (hit) {
+        if (i >= 0) {
+            if (L.found) {
                 HitRecord h;
-                h.t = tmax;
-                h.prim = slot;
-                h.u = u;
-                h.v = v;
+                h.t = L.tmax;
+                h.prim = L.hitSlot;
+                h.u = L.hu;
+                h.v = L.hv;
                 p.hits[i] = h;
-                cls = __ldg(&p.sv.mats[__ldg(&p.sv.slotShade[slot]).x].type);
+                cls = __ldg(&p.sv.mats[__ldg(&p.sv.slotShade[L.hitSlot]).x].type);
             } else if (p.sv.hasEnv) {
-                const int pid = __float_as_int(o4.w);
+                // escaped: the environment at the first hit or after a specular bounce
+                const int pid = __float_as_int(rO[i].w);
                 const float4 bt = p.beta[pid];
-                if (b == 0 || bt.w != 0.0f) filmAdd(p.film, filmIndex(p, pid), xyz(bt) * envLe(p.sv.env, xyz(d4)));
+                if (b == 0 || bt.w != 0.0f) filmAdd(p.film, filmIndex(p, pid), xyz(bt) * envLe(p.sv.env, L.d));
             }
         }
 #pragma unroll
@@ -231,7 +231,9 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(PassArgs p, int b) {
             const int k = warpAppend(cls == c, &classCnt[c]);
             if (k >= 0) p.classQ[c * p.cap + k] = i;
         }
-    }
+    };
+    tracePersistent<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, cnt + 5, stack + threadIdx.x,
+                                  kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
     if (overflow) atomicOr(p.err, 1);
     if (STATS) {
         atomicAdd(&p.visit[0], static_cast<unsigned long long>(nodeCount));
@@ -427,20 +429,24 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
 }
 
 template <bool STATS>
-__global__ void __launch_bounds__(kTraceBlock) k_shadow(PassArgs p, int b) {
+__global__ void __launch_bounds__(kTraceBlock, 8) k_shadow(PassArgs p, int b) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
-    const int n = p.counters[b * kCountersPerBounce + 4];
+    int *cnt = p.counters + b * kCountersPerBounce;
+    const int n = cnt[4];
     bool overflow = false;
     uint32_t nodeCount = 0, triCount = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o4 = p.shO[i], d4 = p.shD[i];
-        float tmax = d4.w, u, v;
-        int slot;
-        const bool occ = traceWide<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(o4), xyz(d4),
-                                                0.0f, tmax, slot, u, v, stack + threadIdx.x, kTraceBlock, &nodeCount,
-                                                &triCount, &overflow);
-        if (!occ) filmAdd(p.film, __float_as_int(o4.w), xyz(p.shL[i]));
-    }
+    auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
+        const float4 d4 = p.shD[i];
+        *o = xyz(p.shO[i]);
+        *d = xyz(d4);
+        *t0 = 0.0f;
+        *t1 = d4.w;
+    };
+    auto done = [&](int i, const TraceLane &L) {
+        if (i >= 0 && !L.found) filmAdd(p.film, __float_as_int(p.shO[i].w), xyz(p.shL[i]));
+    };
+    tracePersistent<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, cnt + 6, stack + threadIdx.x,
+                                 kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
     if (overflow) atomicOr(p.err, 1);
     if (STATS) {
         atomicAdd(&p.visit[2], static_cast<unsigned long long>(nodeCount));

@@ -40,3 +40,23 @@ def test_version_string():
     from spica_gb300 import gpu
     lib = gpu.load_library()
     assert b"sm_103a" in lib.spgpu_version()
+
+
+def test_reference_side_plugins_compile_and_export():
+    """The drop-in plugins build against the reference's own headers (only where the
+    reference tree exists) and export the plugin manager's entry points."""
+    import subprocess
+
+    import pytest
+    from oracle import spo
+    if not os.path.isdir(spo.REF_TREE):
+        pytest.skip("reference tree not present on this host")
+    from spica_gb300 import build
+    build.build()
+    d = os.path.join(ROOT, "spica_gb300", "plugins")
+    r = subprocess.run(["make", "-C", d, f"REF={spo.REF_TREE}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for name in ("gpubvh", "gpupath"):
+        so = os.path.join(d, "_build", name + ".so")
+        syms = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
+        assert " createInstance" in syms and " getDescription" in syms, name
