@@ -214,6 +214,32 @@ def microbench(torch, GpuBVHAccel, scenes, reps=3, rays=16 << 20):
             "any_tris_per_ray": ca.tris_per_ray, "bvh_build_ms": info.build_ms, "wide_nodes": int(info.wide_nodes)}
 
 
+def batch_bench(torch, GpuBatch, scenes, reps=3):
+    """64 seeded box-room variants (resolution 64..512 squared, 16..256 spp) in one
+    persistent graph-captured launch; launch shape from the autotuner."""
+    vs = scenes.batch_variants(64, seed=0)
+    t0 = time.perf_counter()
+    b = GpuBatch(vs, seed=7, autotune=True)
+    prep_s = time.perf_counter() - t0
+    films = torch.zeros((b.pixels, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    b.run(films, stream=stream)
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        ms, st = b.run(films, stream=stream)
+        if best is None or st.ms < best[1].ms:
+            best = (ms, st)
+    ms, st = best
+    samples = sum(v.width * v.height * v.spp for v in vs)
+    return {"renders": len(vs), "path_samples": int(samples), "ms": st.ms,
+            "samples_per_s": samples / (st.ms / 1e3), "mrays_s": (st.rays_closest + st.rays_shadow) / (st.ms * 1e3),
+            "latency_ms_p50": float(np.percentile(ms, 50)), "latency_ms_p99": float(np.percentile(ms, 99)),
+            "tuning": {"block": b.tuning.block, "tile_pixels": b.tuning.tile_pixels, "chunk_spp": b.tuning.chunk_spp,
+                       "candidates": b.tuning.candidates, "calib_ms": b.tuning.calib_ms},
+            "prepare_s": prep_s}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -222,6 +248,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-micro", action="store_true", help="skip the intersection microbench")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-renders measurement")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-API measurement")
     ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel profile (roofline)")
     ap.add_argument("--width", type=int, default=1920, help="film width (profiling cases only)")
@@ -238,7 +265,7 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    from spica_gb300 import GpuBVHAccel, GpuPathIntegrator, scenes
+    from spica_gb300 import GpuBatch, GpuBVHAccel, GpuPathIntegrator, scenes
     from spica_gb300.gpu import KERNEL_CLASSES
 
     if args.micro_only:
@@ -340,6 +367,8 @@ def main():
             "kernels": kernels}
     if not args.no_micro:
         line["microbench"] = microbench(torch, GpuBVHAccel, scenes)
+    if not args.no_batch:
+        line["batch"] = batch_bench(torch, GpuBatch, scenes)
     if not args.no_cpu and ws == 1:
         v, kind, cores, desc, build_s = cpu_sample(scene)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc,

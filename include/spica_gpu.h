@@ -141,6 +141,40 @@ int spgpu_render(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, spg
 int spgpu_render_host(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film,
                       spgpu_render_stats *stats);                                    /* host film   */
 
+/* ---- batched renders ---------------------------------------------------------------
+ * replaces: a sequence of Integrator::render calls on many small scenes
+ * (core/integrator.cc:46), one per scene.  A batch is prepared once (scenes uploaded,
+ * one BVH each, work list planned, launch shape chosen by the autotuner when
+ * `autotune` != 0) and then traced by spgpu_batch_run in a single persistent kernel
+ * launch replayed from a CUDA graph.  Preparing a batch replaces the context's scene
+ * (the last item's scene remains uploaded).  Scenes of a batch have no environment
+ * map.  films: device memory of spgpu_batch_film_pixels() float4 pixels, the items'
+ * films back to back in item order, each in the reference film's pixel order;
+ * accumulated in place.  render_ms[i]: time from the launch's start until the last
+ * sample of item i was added. */
+typedef struct {
+    int32_t ntri;
+    const float *verts;
+    const int32_t *tri_mat;
+    int32_t nmat;
+    const float *materials;
+    const float *tri_emit;
+    spgpu_render_desc desc;
+} spgpu_batch_item;
+
+typedef struct {
+    int32_t block;          /* threads per block */
+    int32_t tile_pixels;    /* pixels per work item */
+    int32_t chunk_spp;      /* samples per pixel per work item */
+    int32_t candidates;     /* configurations the autotuner timed */
+    double calib_ms;        /* device time spent timing them */
+} spgpu_batch_tuning;
+
+int spgpu_batch_prepare(spgpu_ctx *ctx, int32_t count, const spgpu_batch_item *items, int32_t autotune,
+                        spgpu_batch_tuning *tuning);
+int64_t spgpu_batch_film_pixels(spgpu_ctx *ctx);
+int spgpu_batch_run(spgpu_ctx *ctx, float *films, double *render_ms, spgpu_render_stats *stats, void *stream);
+
 /* Profiling (no counterpart in the reference, which has only a progress printf,
  * core/integrator.cc:92-96): the same samples as spgpu_render, launched kernel by
  * kernel without the graph and timed with CUDA events on `stream`, then repeated

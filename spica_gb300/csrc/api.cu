@@ -11,10 +11,6 @@
 #include "../../include/spica_gpu.h"
 #include "ctx.cuh"
 
-struct spgpu_ctx {
-    spgpu::Ctx c;
-};
-
 namespace spgpu {
 
 namespace {
@@ -454,6 +450,8 @@ void spgpu_destroy(spgpu_ctx *h) {
     if (C.stream) cudaStreamSynchronize(C.stream);
     freeScene(C);
     freeRenderQueues(&C.rq);
+    freeBatch(C.batch);
+    C.batch = nullptr;
     cudaFree(C.traceErr);
     cudaFree(C.traceStats);
     if (C.stream) cudaStreamDestroy(C.stream);
@@ -729,6 +727,46 @@ int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
     out->closest_tris_per_ray = st[1] ? static_cast<double>(vis[1]) / st[1] : 0.0;
     out->shadow_nodes_per_ray = st[2] ? static_cast<double>(vis[2]) / st[2] : 0.0;
     out->shadow_tris_per_ray = st[2] ? static_cast<double>(vis[3]) / st[2] : 0.0;
+    return rc;
+}
+
+int spgpu_batch_prepare(spgpu_ctx *h, int32_t count, const spgpu_batch_item *items, int32_t autotune,
+                        spgpu_batch_tuning *tuning) {
+    if (!h || count <= 0 || !items) {
+        setError("spgpu_batch_prepare: invalid arguments");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(h->c.device);
+    return batchPrepare(h, &h->c.batch, count, items, autotune, tuning);
+}
+
+int64_t spgpu_batch_film_pixels(spgpu_ctx *h) { return h && h->c.batch ? batchPixels(*h->c.batch) : -1; }
+
+int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_stats *stats, void *stream) {
+    if (!h || !films || !render_ms) {
+        setError("spgpu_batch_run: invalid arguments");
+        return SPGPU_EINVAL;
+    }
+    Ctx &C = h->c;
+    if (!C.batch) {
+        setError("spgpu_batch_run: no batch prepared");
+        return SPGPU_ESTATE;
+    }
+    if (reinterpret_cast<uintptr_t>(films) & 15) {
+        setError("spgpu_batch_run: films must be 16-byte aligned");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(C.device);
+    unsigned long long st[4] = {0, 0, 0, 0};
+    float ms = 0.0f;
+    const int rc = batchRun(C, *C.batch, reinterpret_cast<float4 *>(films), render_ms, st, &ms,
+                            static_cast<cudaStream_t>(stream));
+    if (stats) {
+        stats->paths = static_cast<int64_t>(st[0]);
+        stats->rays_closest = static_cast<int64_t>(st[1]);
+        stats->rays_shadow = static_cast<int64_t>(st[2]);
+        stats->ms = ms;
+    }
     return rc;
 }
 

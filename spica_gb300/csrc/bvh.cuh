@@ -61,8 +61,8 @@ __device__ __forceinline__ float fmin3f(float a, float b, float c) {
 // land on bit 24 + (s ^ octInv), leaves on their triangle offset with 1..3 bits.
 __device__ __forceinline__ void metaDecode4(uint32_t meta4, uint32_t octInv4, uint32_t *bitIndex4,
                                            uint32_t *childBits4) {
-    const uint32_t isInner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
-    const uint32_t innerMask4 = __byte_perm(isInner4 << 3, 0u, 0xBA98u);   // 0xFF where internal
+    const uint32_t isInner4 = (meta4 & (meta4 << 1)) & 0x10101010u;   // bit 4 of each internal byte
+    const uint32_t innerMask4 = (isInner4 >> 4) * 0xFFu;               // 0xFF where internal
     *bitIndex4 = (meta4 ^ (octInv4 & innerMask4)) & 0x1F1F1F1Fu;
     *childBits4 = (meta4 >> 5) & 0x07070707u;
 }
@@ -86,7 +86,8 @@ struct TraceLane {
     bool found;
 };
 
-__device__ __forceinline__ void laneInit(TraceLane &L, float3 o, float3 d, float tmin, float tmax) {
+__device__ __forceinline__ void laneInit(TraceLane &L, float3 o, float3 d, float tmin, float tmax,
+                                         uint32_t root = 0) {
     L.o = o;
     L.d = d;
     L.idir = mk(d.x == 0.0f ? kInfT : 1.0f / d.x, d.y == 0.0f ? kInfT : 1.0f / d.y, d.z == 0.0f ? kInfT : 1.0f / d.z);
@@ -95,7 +96,7 @@ __device__ __forceinline__ void laneInit(TraceLane &L, float3 o, float3 d, float
     L.tmin = tmin;
     L.tmax = tmax;
     L.tEps = fmaxf(tmin, kEpsT);
-    L.G = make_uint2(0u, (1u << (24 + L.octInv)) | 1u);   // the root as slot 0 of a virtual parent
+    L.G = make_uint2(root, (1u << (24 + L.octInv)) | 1u);   // the root as slot 0 of a virtual parent
     L.sp = 0;
     L.visits = 0;
     L.hitSlot = -1;
@@ -222,10 +223,11 @@ template <bool ANY, bool STATS>
 __device__ __forceinline__ bool traceWide(const WideNode *__restrict__ nodes, const TriRecord *__restrict__ tris,
                                           uint32_t nNodes, uint32_t nTris, float3 o, float3 d, float tmin,
                                           float &tmax, int &hitSlot, float &hu, float &hv, uint2 *__restrict__ stack,
-                                          int stride, uint32_t *nodeCount, uint32_t *triCount, bool *overflow) {
+                                          int stride, uint32_t *nodeCount, uint32_t *triCount, bool *overflow,
+                                          uint32_t root = 0) {
     uint2 spill[kStackDepth - kStackShared];
     TraceLane L;
-    laneInit(L, o, d, tmin, tmax);
+    laneInit(L, o, d, tmin, tmax, root);
     while (!laneStep<ANY, STATS>(L, nodes, tris, nNodes, nTris, stack, stride, spill, nodeCount, triCount,
                                  overflow)) {
     }

@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/spica_gpu.h"
 #include "bvh.cuh"
 #include "common.cuh"
 
@@ -45,6 +46,7 @@ struct SceneView {
     uint32_t nNodes, nTris;
     const MaterialRecord *mats;
     const LightRecord *lights;
+    int lightBase;                // first area light of this scene in `lights`
     int nArea;                    // area lights
     int nLights;                  // nArea + (env ? 1 : 0)
     int hasEnv;
@@ -70,6 +72,9 @@ struct RenderQueues {
     uint64_t graphKey[4] = {0, 0, 0, 0};
 };
 
+struct BatchState;
+void freeBatch(BatchState *B);
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -94,6 +99,8 @@ struct Ctx {
     unsigned long long *traceStats = nullptr;
     // renderer
     RenderQueues rq;
+    // batched renders (spgpu_batch_prepare / spgpu_batch_run)
+    BatchState *batch = nullptr;
 
     SceneView view() const {
         SceneView v;
@@ -104,6 +111,7 @@ struct Ctx {
         v.nTris = static_cast<uint32_t>(bvh.ntri);
         v.mats = mats;
         v.lights = lights;
+        v.lightBase = 0;
         v.nArea = nArea;
         v.nLights = nArea + (hasEnv ? 1 : 0);
         v.hasEnv = hasEnv ? 1 : 0;
@@ -133,4 +141,18 @@ int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int samp
                   float4 *film, double *kernelMs, long long *launches, unsigned long long *statsOut,
                   unsigned long long *visitOut, cudaStream_t stream);
 
+}  // namespace spgpu
+
+// the opaque handle of include/spica_gpu.h
+struct spgpu_ctx {
+    spgpu::Ctx c;
+};
+
+namespace spgpu {
+struct BatchState;
+int batchPrepare(spgpu_ctx *self, BatchState **slot, int count, const spgpu_batch_item *items, int autotune,
+                 spgpu_batch_tuning *tuning);
+int batchRun(Ctx &C, BatchState &B, float4 *film, double *renderMs, unsigned long long *statsOut, float *msOut,
+             cudaStream_t stream);
+int64_t batchPixels(const BatchState &B);
 }  // namespace spgpu

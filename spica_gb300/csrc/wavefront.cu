@@ -32,6 +32,7 @@
 
 #include "../../include/spica_gpu.h"
 #include "ctx.cuh"
+#include "shade.cuh"
 
 namespace spgpu {
 
@@ -83,82 +84,6 @@ __device__ __forceinline__ int warpAppend(bool want, int *counter) {
     return want ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
-// ---------------------------------------------------------------- environment map
-// MipMap::bilinear on level 0 with repeat wrap (core/mipmap.cc:81-93)
-__device__ __forceinline__ float3 envTexel(const DeviceEnv &E, int s, int t) {
-    s = (s % E.w + E.w) % E.w;
-    t = (t % E.h + E.h) % E.h;
-    return xyz(__ldg(&E.tex[t * E.w + s]));
-}
-__device__ __forceinline__ float3 envLookup(const DeviceEnv &E, float u, float v) {
-    const float s = u * E.w - 0.5f, t = v * E.h - 0.5f;
-    const int si = static_cast<int>(s), ti = static_cast<int>(t);
-    const float ds = s - si, dt = t - ti;
-    return (1.0f - ds) * (1.0f - dt) * envTexel(E, si, ti) + ds * (1.0f - dt) * envTexel(E, si + 1, ti) +
-           (1.0f - ds) * dt * envTexel(E, si, ti + 1) + ds * dt * envTexel(E, si + 1, ti + 1);
-}
-__device__ __forceinline__ void dirToUV(float3 d, float *u, float *v) {
-    float phi = atan2f(d.y, d.x);
-    if (phi < 0.0f) phi += 2.0f * kPi;
-    *u = phi * (0.5f * kInvPi);
-    *v = acosf(clampf(d.z, -1.0f, 1.0f)) * kInvPi;
-}
-__device__ __forceinline__ float3 envLe(const DeviceEnv &E, float3 d) {   // Envmap::Le, envmap.cc:130
-    float u, v;
-    dirToUV(normalize(d), &u, &v);
-    return envLookup(E, u, v);
-}
-// Distribution1D::sample over cdf[0..n] / func[0..n-1] (core/sampling.cc:75)
-__device__ __forceinline__ float sample1D(const float *cdf, const float *func, int n, float integral, float u,
-                                          float *pdf, int *off) {
-    int lo = 0, hi = n;   // largest i in [0, n] with cdf[i] <= u
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(&cdf[mid]) <= u) lo = mid;
-        else hi = mid - 1;
-    }
-    const int o = min(lo, n - 1);
-    *off = o;
-    const float c0 = __ldg(&cdf[o]), c1 = __ldg(&cdf[o + 1]);
-    float du = u - c0;
-    if (c1 - c0 > 0.0f) du /= (c1 - c0);
-    *pdf = integral > 0.0f ? __ldg(&func[o]) / integral : 0.0f;
-    return (o + du) / n;
-}
-__device__ __forceinline__ float envPdf(const DeviceEnv &E, float3 d) {   // Envmap::pdfLi, envmap.cc:81
-    float u, v;
-    dirToUV(d, &u, &v);
-    const float sinTheta = sinf(v * kPi);
-    if (sinTheta == 0.0f || E.margIntegral <= 0.0f) return 0.0f;
-    const int iu = min(max(static_cast<int>(u * E.w), 0), E.w - 1);
-    const int iv = min(max(static_cast<int>(v * E.h), 0), E.h - 1);
-    return (__ldg(&E.condFunc[iv * E.w + iu]) / E.margIntegral) / (2.0f * kPi * kPi * sinTheta);
-}
-
-// Shape::pdf(Interaction, wi) for an area-light triangle (core/shape.cc:39): intersect
-// the light from the offset origin; solid-angle pdf from the hit distance.
-__device__ __forceinline__ float lightTriPdf(const LightRecord &L, float3 p, float3 n, float3 wi, float *tHit) {
-    const float3 o = offsetOrigin(p, n, wi);
-    const float3 e1 = xyz(L.e1), e2 = xyz(L.e2);
-    const float3 pv = cross(wi, e2);
-    const float det = dot(e1, pv);
-    if (det > -kEpsT && det < kEpsT) return 0.0f;
-    const float inv = 1.0f / det;
-    const float3 tv = o - xyz(L.p0);
-    const float u = dot(tv, pv) * inv;
-    if (u < 0.0f || u > 1.0f) return 0.0f;
-    const float3 qv = cross(tv, e1);
-    const float v = dot(wi, qv) * inv;
-    if (v < 0.0f || u + v > 1.0f) return 0.0f;
-    const float t = dot(e2, qv) * inv;
-    if (t <= kEpsT) return 0.0f;
-    *tHit = t;
-    const float3 hp = o + wi * t;
-    const float3 dd = p - hp;
-    const float pdf = dot(dd, dd) / (fabsf(dot(xyz(L.n), wi)) * L.p0.w);
-    return isinf(pdf) ? 0.0f : pdf;
-}
-
 // ---------------------------------------------------------------- kernels
 __global__ void k_raygen(PassArgs p) {
     const int sample = p.ctl[0];
@@ -166,21 +91,9 @@ __global__ void k_raygen(PassArgs p) {
         const int y = pix / p.W, x = pix - y * p.W;
         const int fi = y * p.W + (p.W - 1 - x);
         const Rand4 r = rand4(p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), 0xFFFFu, 0u);
-        const float fx = x + r.a, fy = y + r.b;
-        const float *M = p.cam.r2c;
-        float c[4];
-        for (int i = 0; i < 4; i++) c[i] = M[4 * i + 0] * fx + M[4 * i + 1] * fy + M[4 * i + 3];
-        if (c[3] != 1.0f) {
-            c[0] /= (c[3] + 1.0e-12f);
-            c[1] /= (c[3] + 1.0e-12f);
-            c[2] /= (c[3] + 1.0e-12f);
-        }
-        const float inv = 1.0f / sqrtf(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-        const float3 dc = mk(c[0] * inv, c[1] * inv, c[2] * inv);
-        const float *W = p.cam.c2w;
-        const float3 d = normalize(mk(W[0] * dc.x + W[1] * dc.y + W[2] * dc.z, W[4] * dc.x + W[5] * dc.y + W[6] * dc.z,
-                                      W[8] * dc.x + W[9] * dc.y + W[10] * dc.z));
-        p.rayO0[pix] = make_float4(W[3], W[7], W[11], __int_as_float(pix));
+        float3 o, d;
+        spawnCameraRay(p.cam, x, y, r.a, r.b, &o, &d);
+        p.rayO0[pix] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
         p.rayD0[pix] = make_float4(d.x, d.y, d.z, kInfT);
         p.beta[pix] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         float4 f = p.film[fi];
@@ -251,179 +164,41 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
     const float4 *rD = (b & 1) ? p.rayD1 : p.rayD0;
     float4 *nO = (b & 1) ? p.rayO0 : p.rayO1;
     float4 *nD = (b & 1) ? p.rayD0 : p.rayD1;
-    const int sample = p.ctl[0];
-    const SceneView &S = p.sv;
+    const uint32_t sample = static_cast<uint32_t>(p.ctl[0]);
     const int stride = gridDim.x * blockDim.x;
-    const int nIter = (n + stride - 1) / stride;
+    const int nIter = (n + stride - 1) / stride;   // uniform trip count keeps warps whole for the ballots
     for (int it = 0; it < nIter; it++) {
         const int j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const bool live = j < n;
-        bool cont = false, sh0 = false, sh1 = false;
-        float4 c0O, c0D, c0L, c1O, c1D, c1L, cO, cD;
+        ShadeResult R;
+        R.cont = R.sh0 = R.sh1 = false;
         int pid = 0;
-        float3 beta = mk(0, 0, 0);
-        bool spec = false;
-        if (live) {
+        if (j < n) {
             const int i = p.classQ[CLS * p.cap + j];
             const float4 o4 = rO[i], d4 = rD[i];
-            const HitRecord h = p.hits[i];
             pid = __float_as_int(o4.w);
             const float4 bt = p.beta[pid];
-            beta = xyz(bt);
-            spec = bt.w != 0.0f;
             const int fi = filmIndex(p, pid);
-            const TriRecord tr = S.tris[h.prim];
-            const float3 n = normalize(cross(xyz(tr.v1) - xyz(tr.v0), xyz(tr.v2) - xyz(tr.v0)));
-            const int2 sh = __ldg(&S.slotShade[h.prim]);
-            const MaterialRecord m = S.mats[sh.x];
-            const float3 d = xyz(d4);
-            const float3 ps = xyz(o4) + d * h.t;
-            // emitted radiance at the first hit or after a specular bounce (path.cc:58-66)
-            if ((b == 0 || spec) && sh.y >= 0) {
-                const LightRecord &L = S.lights[sh.y];
-                if (dot(n, -d) > 0.0f) filmAdd(p.film, fi, beta * xyz(L.L));
-            }
-            if (b < p.maxDepth) {
-                float3 tg, bg;
-                onb(n, &tg, &bg);
-                const float3 wo = -d;
-                const float3 woL = mk(dot(wo, tg), dot(wo, bg), dot(wo, n));
-                const Rand4 r0 = rand4(p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample),
-                                       static_cast<uint32_t>(b), 0u);
-                const Rand4 r1 = rand4(p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample),
-                                       static_cast<uint32_t>(b), 1u);
-                if (CLS != kMatDielectric && S.nLights > 0) {
-                    // ---- uniformSampleOneLight + estimateDirectLight (mis.cc:21-136)
-                    const int nL = S.nLights;
-                    const int li = min(static_cast<int>(r0.a * nL), nL - 1);
-                    const bool isEnv = li >= S.nArea;
-                    const float3 scale = beta * static_cast<float>(nL);
-                    // light sampling
-                    float3 wi = mk(0, 0, 0), Li = mk(0, 0, 0), target = mk(0, 0, 0), tn = mk(0, 0, 0);
-                    float lightPdf = 0.0f;
-                    if (!isEnv) {
-                        const LightRecord L = S.lights[li];
-                        float u0 = r0.b, u1 = r0.c;
-                        if (u0 + u1 >= 1.0f) {
-                            u0 = 1.0f - u0;
-                            u1 = 1.0f - u1;
-                        }
-                        target = xyz(L.p0) + xyz(L.e1) * u0 + xyz(L.e2) * u1;
-                        tn = xyz(L.n);
-                        wi = normalize(target - ps);
-                        float tl;
-                        lightPdf = lightTriPdf(L, ps, n, wi, &tl);
-                        if (dot(tn, -wi) > 0.0f) Li = xyz(L.L);
-                    } else {
-                        const DeviceEnv &E = S.env;
-                        float pv, pu;
-                        int vOff, uOff;
-                        const float vv = sample1D(E.margCdf, E.margFunc, E.h, E.margIntegral, r0.c, &pv, &vOff);
-                        const float uu = sample1D(E.condCdf + static_cast<int64_t>(vOff) * (E.w + 1),
-                                                  E.condFunc + static_cast<int64_t>(vOff) * E.w, E.w,
-                                                  __ldg(&E.margFunc[vOff]), r0.b, &pu, &uOff);
-                        const float mapPdf = pu * pv;
-                        if (mapPdf > 0.0f) {
-                            float st, ct, sp, cp;
-                            sincosf(vv * kPi, &st, &ct);
-                            sincosf(uu * 2.0f * kPi, &sp, &cp);
-                            wi = mk(st * cp, st * sp, ct);
-                            lightPdf = st == 0.0f ? 0.0f : mapPdf / (2.0f * kPi * kPi * st);
-                            Li = envLookup(E, uu, vv);
-                            target = ps + wi * (2.0f * E.radius);
-                        }
-                    }
-                    if (lightPdf > 0.0f && !isBlack(Li)) {
-                        const float3 wiL = mk(dot(wi, tg), dot(wi, bg), dot(wi, n));
-                        const float3 f = bsdfF(m, woL, wiL) * fabsf(dot(wi, n));
-                        if (!isBlack(f)) {
-                            const float bp = bsdfPdf(m, woL, wiL);
-                            const float w = powerHeuristic(lightPdf, bp);
-                            const float3 c = scale * f * Li * (w / lightPdf);
-                            // VisibilityTester::unoccluded via spawnRayTo (interaction.cc:88)
-                            const float3 o = offsetOrigin(ps, n, target - ps);
-                            const float3 t2 = isEnv ? mk(nextafterf(target.x, -INFINITY), nextafterf(target.y, -INFINITY),
-                                                         nextafterf(target.z, -INFINITY))
-                                                    : offsetOrigin(target, tn, o - target);
-                            const float3 dd = t2 - o;
-                            const float len = length(dd);
-                            if (len > 0.0f) {
-                                sh0 = true;
-                                c0O = make_float4(o.x, o.y, o.z, __int_as_float(fi));
-                                c0D = make_float4(dd.x / len, dd.y / len, dd.z / len, len);
-                                c0L = make_float4(c.x, c.y, c.z, 0.0f);
-                            }
-                        }
-                    }
-                    // BSDF sampling with MIS
-                    float3 wiL2;
-                    float pdf2;
-                    int type2;
-                    float3 f2 = bsdfSample(m, woL, r0.d, r1.a, &wiL2, &pdf2, &type2);
-                    if (!isBlack(f2) && pdf2 > 0.0f) {
-                        const float3 wi2 = normalize(tg * wiL2.x + bg * wiL2.y + n * wiL2.z);
-                        f2 = f2 * fabsf(dot(wi2, n));
-                        float lp = 0.0f, tl = 0.0f;
-                        float3 L2 = mk(0, 0, 0);
-                        if (!isEnv) {
-                            const LightRecord L = S.lights[li];
-                            lp = lightTriPdf(L, ps, n, wi2, &tl);
-                            if (lp > 0.0f && dot(xyz(L.n), -wi2) > 0.0f) L2 = xyz(L.L);
-                        } else {
-                            lp = envPdf(S.env, wi2);
-                            if (lp > 0.0f) L2 = envLe(S.env, wi2);
-                        }
-                        if (lp > 0.0f && !isBlack(L2) && !isBlack(f2)) {
-                            const float w = powerHeuristic(pdf2, lp);
-                            const float3 c = scale * f2 * L2 * (w / pdf2);
-                            const float3 o = offsetOrigin(ps, n, wi2);
-                            sh1 = true;
-                            c1O = make_float4(o.x, o.y, o.z, __int_as_float(fi));
-                            c1D = make_float4(wi2.x, wi2.y, wi2.z, isEnv ? kInfT : tl * (1.0f - 1.0e-5f));
-                            c1L = make_float4(c.x, c.y, c.z, 0.0f);
-                        }
-                    }
-                }
-                // ---- continuation (path.cc:82-95) and Russian roulette (path.cc:117-121)
-                float3 wiL;
-                float pdf;
-                int type;
-                const float3 f = bsdfSample(m, woL, r1.b, r1.c, &wiL, &pdf, &type);
-                if (!isBlack(f) && pdf > 0.0f) {
-                    const float3 wi = normalize(tg * wiL.x + bg * wiL.y + n * wiL.z);
-                    beta = beta * f * (fabsf(dot(wi, n)) / pdf);
-                    spec = (type & kSpecular) != 0;
-                    cont = true;
-                    if (b > 3) {
-                        const float q = fminf(0.95f, gray(beta));
-                        if (r1.d > q) cont = false;
-                        else beta = beta / q;
-                    }
-                    if (cont) {
-                        const float3 o = offsetOrigin(ps, n, wi);
-                        cO = make_float4(o.x, o.y, o.z, __int_as_float(pid));
-                        cD = make_float4(wi.x, wi.y, wi.z, kInfT);
-                    }
-                }
-            }
+            shadeHit(p.sv, p.hits[i], xyz(o4), xyz(d4), xyz(bt), bt.w != 0.0f, b, p.maxDepth, p.seed,
+                     static_cast<uint32_t>(fi), sample, fi, R);
+            if (!isBlack(R.emit)) filmAdd(p.film, fi, R.emit);
         }
-        const int k = warpAppend(cont, nextCnt);
+        const int k = warpAppend(R.cont, nextCnt);
         if (k >= 0) {
-            nO[k] = cO;
-            nD[k] = cD;
-            p.beta[pid] = make_float4(beta.x, beta.y, beta.z, spec ? 1.0f : 0.0f);
+            nO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pid));
+            nD[k] = R.cD;
+            p.beta[pid] = make_float4(R.beta.x, R.beta.y, R.beta.z, R.spec ? 1.0f : 0.0f);
         }
-        const int s0 = warpAppend(sh0, shCnt);
+        const int s0 = warpAppend(R.sh0, shCnt);
         if (s0 >= 0) {
-            p.shO[s0] = c0O;
-            p.shD[s0] = c0D;
-            p.shL[s0] = c0L;
+            p.shO[s0] = R.s0O;
+            p.shD[s0] = R.s0D;
+            p.shL[s0] = R.s0L;
         }
-        const int s1 = warpAppend(sh1, shCnt);
+        const int s1 = warpAppend(R.sh1, shCnt);
         if (s1 >= 0) {
-            p.shO[s1] = c1O;
-            p.shD[s1] = c1D;
-            p.shL[s1] = c1L;
+            p.shO[s1] = R.s1O;
+            p.shD[s1] = R.s1D;
+            p.shL[s1] = R.s1L;
         }
     }
 }

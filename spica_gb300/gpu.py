@@ -60,6 +60,16 @@ class KernelProfile(C.Structure):
 KERNEL_CLASSES = ["raygen", "extend", "shade_lambert", "shade_conductor", "shade_dielectric", "shadow", "finish"]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("ntri", C.c_int32), ("verts", C.c_void_p), ("tri_mat", C.c_void_p), ("nmat", C.c_int32),
+                ("materials", C.c_void_p), ("tri_emit", C.c_void_p), ("desc", RenderDesc)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("block", C.c_int32), ("tile_pixels", C.c_int32), ("chunk_spp", C.c_int32),
+                ("candidates", C.c_int32), ("calib_ms", C.c_double)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("reserved", C.c_int * 7)]
 
@@ -67,7 +77,8 @@ class Config(C.Structure):
 # every extern "C" symbol include/spica_gpu.h declares
 EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version", "spgpu_upload_scene",
            "spgpu_build_bvh", "spgpu_bvh_stats", "spgpu_trace", "spgpu_trace_host", "spgpu_trace_stats",
-           "spgpu_render", "spgpu_render_host", "spgpu_render_profile"]
+           "spgpu_render", "spgpu_render_host", "spgpu_render_profile", "spgpu_batch_prepare",
+           "spgpu_batch_film_pixels", "spgpu_batch_run"]
 
 _lib = None
 
@@ -96,9 +107,13 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_render.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats), vp]
     lib.spgpu_render_host.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats)]
     lib.spgpu_render_profile.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(KernelProfile), vp]
+    lib.spgpu_batch_prepare.argtypes = [vp, i32, C.POINTER(BatchItem), i32, C.POINTER(BatchTuning)]
+    lib.spgpu_batch_film_pixels.argtypes = [vp]
+    lib.spgpu_batch_run.argtypes = [vp, vp, vp, C.POINTER(RenderStats), vp]
     for name in EXPORTS:
         if name not in ("spgpu_destroy", "spgpu_last_error", "spgpu_version"):
             getattr(lib, name).restype = C.c_int
+    lib.spgpu_batch_film_pixels.restype = C.c_int64
     if path is None:
         _lib = lib
     return lib
@@ -271,3 +286,52 @@ class GpuPathIntegrator:
         d.width, d.height, d.spp = W, H, spp
         d.sample_offset, d.max_depth, d.seed = sample_offset, max_depth, self.seed & 0xFFFFFFFF
         return d
+
+
+class GpuBatch:
+    """Many small renders traced in one persistent launch (spgpu_batch_prepare / run).
+    scenes: list of scenes.Scene with width, height, spp, max_depth and camera set."""
+
+    def __init__(self, scene_list, seed: int = 0, autotune: bool = True, device: int = 0,
+                 ctx: Optional[Context] = None):
+        self.ctx = ctx or Context(device)
+        self.scenes = list(scene_list)
+        self._keep = []
+        items = (BatchItem * len(self.scenes))()
+        integ = GpuPathIntegrator(seed=seed)
+        self.offsets = []
+        off = 0
+        for i, sc in enumerate(self.scenes):
+            v = np.ascontiguousarray(sc.verts, np.float32)
+            tm = np.ascontiguousarray(sc.tri_mat, np.int32)
+            m = np.ascontiguousarray(sc.materials, np.float32)
+            e = None if sc.tri_emit is None else np.ascontiguousarray(sc.tri_emit, np.float32)
+            self._keep += [v, tm, m, e]
+            items[i].ntri = v.shape[0]
+            items[i].verts = v.ctypes.data
+            items[i].tri_mat = tm.ctypes.data
+            items[i].nmat = m.shape[0]
+            items[i].materials = m.ctypes.data
+            items[i].tri_emit = e.ctypes.data if e is not None else None
+            items[i].desc = integ.desc(sc.camera, sc.width, sc.height, sc.spp, sc.max_depth)
+            self.offsets.append(off)
+            off += sc.width * sc.height
+        self.tuning = BatchTuning()
+        _check(self.ctx.lib.spgpu_batch_prepare(self.ctx.h, len(self.scenes), items, int(autotune),
+                                                C.byref(self.tuning)), "spgpu_batch_prepare")
+        self.pixels = int(self.ctx.lib.spgpu_batch_film_pixels(self.ctx.h))
+        assert self.pixels == off
+
+    def run(self, films, stream: int = 0):
+        """films: device tensor of self.pixels x 4 float32 (accumulated).  Returns
+        (per-render completion times in ms, RenderStats)."""
+        ms = np.zeros(len(self.scenes), np.float64)
+        st = RenderStats()
+        _check(self.ctx.lib.spgpu_batch_run(self.ctx.h, _ptr(films), ms.ctypes.data, C.byref(st),
+                                            C.c_void_p(stream) if stream else None), "spgpu_batch_run")
+        return ms, st
+
+    def film(self, films_host, i):
+        sc = self.scenes[i]
+        o = self.offsets[i]
+        return films_host[o:o + sc.width * sc.height].reshape(sc.height, sc.width, 4)
