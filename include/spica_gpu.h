@@ -175,6 +175,44 @@ int spgpu_batch_prepare(spgpu_ctx *ctx, int32_t count, const spgpu_batch_item *i
 int64_t spgpu_batch_film_pixels(spgpu_ctx *ctx);
 int spgpu_batch_run(spgpu_ctx *ctx, float *films, double *render_ms, spgpu_render_stats *stats, void *stream);
 
+/* ---- learned path guiding ---------------------------------------------------------
+ * No counterpart in the reference renderer.  A 9 -> 64 -> 64 -> 64 -> 40 MLP (BF16
+ * weights, FP32 accumulation, tensor cores) maps (position, normal, outgoing direction)
+ * at a Lambertian shading point to an 8-lobe von Mises-Fisher mixture; the path tracer
+ * samples directions from the one-sample MIS mixture bsdf_fraction * BSDF +
+ * (1 - bsdf_fraction) * network for both the continuation and the BSDF strategy of
+ * next-event estimation, which keeps the estimator of PathIntegrator::Li unbiased.
+ * Training is online: spgpu_guiding_render with SPGPU_GUIDE_COLLECT records incident-
+ * radiance samples gathered by the paths it traces, spgpu_guiding_train runs Adam
+ * steps on random batches of them. */
+typedef struct {
+    float learning_rate;   /* Adam step size (0: 1e-3) */
+    float bsdf_fraction;   /* BSDF probability in the sampling mixture (clamped to >= 0.2) */
+    int32_t batch;         /* training samples per Adam step (0: 16384) */
+    uint32_t seed;         /* weight initialisation */
+    int32_t capacity;      /* training-sample ring size (0: 2^21) */
+    int32_t reserved[3];
+} spgpu_guiding_config;
+
+#define SPGPU_GUIDE_GUIDED 1   /* sample with the network mixture */
+#define SPGPU_GUIDE_COLLECT 2  /* record training samples */
+#define SPGPU_GUIDE_PARAMS 11560
+
+int spgpu_guiding_init(spgpu_ctx *ctx, const spgpu_guiding_config *cfg);
+/* one persistent launch tracing desc->spp samples per pixel (flags 0: plain BSDF
+ * sampling, the same estimator as spgpu_render); film as for spgpu_render (device) */
+int spgpu_guiding_render(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, int32_t flags,
+                         spgpu_render_stats *stats, void *stream);
+int spgpu_guiding_train(spgpu_ctx *ctx, int32_t steps, double *mean_loss);
+int64_t spgpu_guiding_samples(spgpu_ctx *ctx);   /* training samples recorded so far */
+/* parameters, fp32: each layer's weights [out][in] row-major then its bias */
+int spgpu_guiding_params(spgpu_ctx *ctx, float *params, int32_t set);
+/* network outputs for n feature rows (device: features n*9, raw n*40) */
+int spgpu_guiding_mlp(spgpu_ctx *ctx, const float *features, int32_t n, float *raw, void *stream);
+/* gradient of the training loss sum_i c_i (-log q(w_i)) / sum_i c_i for n samples of 16
+ * floats (features 9, direction 3, weight c, 3 unused) (device; grad: 11560 floats) */
+int spgpu_guiding_grad(spgpu_ctx *ctx, const float *samples, int32_t n, float *grad, double *loss, void *stream);
+
 /* Profiling (no counterpart in the reference, which has only a progress printf,
  * core/integrator.cc:92-96): the same samples as spgpu_render, launched kernel by
  * kernel without the graph and timed with CUDA events on `stream`, then repeated

@@ -10,8 +10,8 @@ The compute path is libspica_gpu.so (CUDA C++, C ABI in include/spica_gpu.h); th
 package is its host-side mirror of the reference's Accelerator/Integrator plugins.
 """
 from . import scenes  # noqa: F401
-from .gpu import (BVHInfo, Context, GpuBatch, GpuBVHAccel, GpuPathIntegrator, RenderStats,  # noqa: F401
-                  SpgpuError, TraceCounters, load_library)
+from .gpu import (BVHInfo, Context, GpuBatch, GpuBVHAccel, GpuGuide, GpuPathIntegrator,  # noqa: F401
+                  RenderStats, SpgpuError, TraceCounters, load_library)
 
-__all__ = ["scenes", "Context", "GpuBatch", "GpuBVHAccel", "GpuPathIntegrator", "SpgpuError", "load_library", "BVHInfo",
+__all__ = ["scenes", "Context", "GpuBatch", "GpuBVHAccel", "GpuGuide", "GpuPathIntegrator", "SpgpuError", "load_library", "BVHInfo",
            "RenderStats", "TraceCounters"]

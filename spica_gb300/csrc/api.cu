@@ -452,6 +452,8 @@ void spgpu_destroy(spgpu_ctx *h) {
     freeRenderQueues(&C.rq);
     freeBatch(C.batch);
     C.batch = nullptr;
+    freeGuide(C.guide);
+    C.guide = nullptr;
     cudaFree(C.traceErr);
     cudaFree(C.traceStats);
     if (C.stream) cudaStreamDestroy(C.stream);
@@ -768,6 +770,85 @@ int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_
         stats->ms = ms;
     }
     return rc;
+}
+
+int spgpu_guiding_init(spgpu_ctx *h, const spgpu_guiding_config *cfg) {
+    if (!h || !cfg) {
+        setError("spgpu_guiding_init: invalid arguments");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(h->c.device);
+    return guideInit(h->c, &h->c.guide, cfg);
+}
+
+int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, int32_t flags,
+                         spgpu_render_stats *stats, void *stream) {
+    if (!h || !d || !film || d->width <= 0 || d->height <= 0 || d->spp < 0 || d->max_depth < 0 ||
+        d->max_depth > 12 || (reinterpret_cast<uintptr_t>(film) & 15)) {
+        setError("spgpu_guiding_render: invalid arguments (max_depth <= 12, aligned film)");
+        return SPGPU_EINVAL;
+    }
+    Ctx &C = h->c;
+    if (!C.bvhReady) {
+        setError("spgpu_guiding_render: no BVH");
+        return SPGPU_ESTATE;
+    }
+    if ((flags & (SPGPU_GUIDE_GUIDED | SPGPU_GUIDE_COLLECT)) && !C.guide) {
+        setError("spgpu_guiding_render: call spgpu_guiding_init first");
+        return SPGPU_ESTATE;
+    }
+    cudaSetDevice(C.device);
+    unsigned long long st[4] = {0, 0, 0, 0};
+    float ms = 0.0f;
+    const int rc = guideRender(C, flags ? C.guide : nullptr, d, reinterpret_cast<float4 *>(film), flags, st, &ms,
+                               static_cast<cudaStream_t>(stream));
+    if (stats) {
+        stats->paths = static_cast<int64_t>(st[0]);
+        stats->rays_closest = static_cast<int64_t>(st[1]);
+        stats->rays_shadow = static_cast<int64_t>(st[2]);
+        stats->ms = ms;
+    }
+    return rc;
+}
+
+int spgpu_guiding_train(spgpu_ctx *h, int32_t steps, double *mean_loss) {
+    if (!h || steps < 0) return SPGPU_EINVAL;
+    if (!h->c.guide) {
+        setError("spgpu_guiding_train: call spgpu_guiding_init first");
+        return SPGPU_ESTATE;
+    }
+    cudaSetDevice(h->c.device);
+    return guideTrain(h->c, *h->c.guide, steps, mean_loss);
+}
+
+int64_t spgpu_guiding_samples(spgpu_ctx *h) { return h && h->c.guide ? guideSamples(*h->c.guide) : -1; }
+
+int spgpu_guiding_params(spgpu_ctx *h, float *params, int32_t set) {
+    if (!h || !params || !h->c.guide) {
+        setError("spgpu_guiding_params: invalid arguments or no guiding state");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(h->c.device);
+    return guideParams(h->c, *h->c.guide, params, set);
+}
+
+int spgpu_guiding_mlp(spgpu_ctx *h, const float *features, int32_t n, float *raw, void *stream) {
+    if (!h || !h->c.guide || n < 0 || (n > 0 && (!features || !raw))) {
+        setError("spgpu_guiding_mlp: invalid arguments or no guiding state");
+        return SPGPU_EINVAL;
+    }
+    if (n == 0) return 0;
+    cudaSetDevice(h->c.device);
+    return guideForward(h->c, *h->c.guide, features, n, raw, static_cast<cudaStream_t>(stream));
+}
+
+int spgpu_guiding_grad(spgpu_ctx *h, const float *samples, int32_t n, float *grad, double *loss, void *stream) {
+    if (!h || !h->c.guide || n <= 0 || !samples || !grad) {
+        setError("spgpu_guiding_grad: invalid arguments or no guiding state");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(h->c.device);
+    return guideGrad(h->c, *h->c.guide, samples, n, grad, loss, static_cast<cudaStream_t>(stream), false);
 }
 
 int spgpu_render_host(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_render_stats *stats) {

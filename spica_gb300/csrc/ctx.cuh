@@ -74,6 +74,8 @@ struct RenderQueues {
 
 struct BatchState;
 void freeBatch(BatchState *B);
+struct GuideState;
+void freeGuide(GuideState *G);
 
 struct Ctx {
     int device = 0;
@@ -101,6 +103,8 @@ struct Ctx {
     RenderQueues rq;
     // batched renders (spgpu_batch_prepare / spgpu_batch_run)
     BatchState *batch = nullptr;
+    // learned guiding (spgpu_guiding_*)
+    GuideState *guide = nullptr;
 
     SceneView view() const {
         SceneView v;
@@ -155,4 +159,13 @@ int batchPrepare(spgpu_ctx *self, BatchState **slot, int count, const spgpu_batc
 int batchRun(Ctx &C, BatchState &B, float4 *film, double *renderMs, unsigned long long *statsOut, float *msOut,
              cudaStream_t stream);
 int64_t batchPixels(const BatchState &B);
+int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg);
+int guideParams(Ctx &C, GuideState &G, float *host, int set);
+int guideForward(Ctx &C, GuideState &G, const float *feat, int n, float *out, cudaStream_t s);
+int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s,
+              bool accumulateOnly);
+int guideTrain(Ctx &C, GuideState &G, int steps, double *meanLoss);
+int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film, int flags,
+                unsigned long long *statsOut, float *msOut, cudaStream_t s);
+int guideSamples(const GuideState &G);
 }  // namespace spgpu

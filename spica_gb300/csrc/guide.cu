@@ -1,0 +1,1021 @@
+// guide.cu -- learned path guiding: parameter storage and packing, the fused training
+// kernel (tcgen05 forward + backward, weight gradients), Adam, and the guided path
+// tracer.  No counterpart in the reference renderer; the estimator it feeds is the
+// reference's PathIntegrator::Li with the BSDF sampling strategy replaced by a
+// one-sample MIS mixture of BSDF sampling (probability alpha >= 0.2) and the network's
+// vMF mixture, so it stays unbiased whatever the network outputs.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "../../include/spica_gpu.h"
+#include "ctx.cuh"
+#include "guide.cuh"
+#include "shade.cuh"
+
+namespace spgpu {
+
+struct GuideState {
+    float *master = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    uint8_t *packFwd = nullptr, *packBwd = nullptr;
+    float *biasPad = nullptr;
+    float *samples = nullptr;   // training ring, 16 floats per sample: x[9], w[3], c, pad
+    int capacity = 0;
+    int *ctl = nullptr;         // [0] samples written (monotonic), [1] error, [2] work counter
+    double *lossAcc = nullptr;  // [0] loss sum, [1] weight sum
+    float *wsum = nullptr;      // batch weight sum / max
+    int *batchIdx = nullptr;
+    float *batch = nullptr;
+    int batchCap = 0;
+    int step = 0;
+    spgpu_guiding_config cfg{};
+    double lastLoss = 0.0;
+    std::mt19937 rng;
+};
+
+namespace {
+
+// ------------------------------------------------------------------ packing
+// master fp32 -> bf16 canonical K-major tiles (forward and backward B operands)
+__global__ void k_guide_pack(const float *__restrict__ P, uint8_t *fwd, uint8_t *bwd, float *biasPad) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    auto put = [](uint8_t *tile, int r, int k, int K, float v) {
+        *reinterpret_cast<__nv_bfloat16 *>(tile + tc::kmajorOffset(r, k, K)) = __float2bfloat16_rn(v);
+    };
+    uint8_t *w1f = fwd, *w2f = w1f + kW1fBytes, *w3f = w2f + kW2fBytes, *w4f = w3f + kW2fBytes;
+    uint8_t *w2b = bwd, *w3b = w2b + kW2fBytes, *w4b = w3b + kW2fBytes;
+    for (int e = t; e < kGHid * kGK0; e += stride) {   // W1f [64][16]
+        const int o = e / kGK0, i = e % kGK0;
+        put(w1f, o, i, kGK0, i < kGIn ? P[kOffW1 + o * kGIn + i] : 0.0f);
+    }
+    for (int e = t; e < kGHid * kGHid; e += stride) {   // W2f, W3f [64][64] and W2b, W3b (transposed)
+        const int o = e / kGHid, i = e % kGHid;
+        put(w2f, o, i, kGHid, P[kOffW2 + e]);
+        put(w3f, o, i, kGHid, P[kOffW3 + e]);
+        put(w2b, i, o, kGHid, P[kOffW2 + e]);
+        put(w3b, i, o, kGHid, P[kOffW3 + e]);
+    }
+    for (int e = t; e < kGN4 * kGHid; e += stride) {   // W4f [48][64], W4b [64][48]
+        const int o = e / kGHid, i = e % kGHid;
+        const float w = o < kGOut ? P[kOffW4 + o * kGHid + i] : 0.0f;
+        put(w4f, o, i, kGHid, w);
+        put(w4b, i, o, kGN4, w);
+    }
+    for (int e = t; e < kBiasPad; e += stride) {
+        float b = 0.0f;
+        if (e < kGHid) b = P[kOffB1 + e];
+        else if (e < 2 * kGHid) b = P[kOffB2 + e - kGHid];
+        else if (e < 3 * kGHid) b = P[kOffB3 + e - 2 * kGHid];
+        else if (e - 3 * kGHid < kGOut) b = P[kOffB4 + e - 3 * kGHid];
+        biasPad[e] = b;
+    }
+}
+
+// ------------------------------------------------------------------ loss
+// -c * log p(w) of the mixture for raw outputs r; writes dLoss/draw into g, returns loss
+__device__ __forceinline__ float mixtureLossGrad(const float *r, float3 w, float c, float *g) {
+    float mx = -3.0e38f;
+    for (int k = 0; k < kGLobes; k++) mx = fmaxf(mx, r[5 * k + 4]);
+    float wk[kGLobes], vk[kGLobes], s = 0.0f;
+    float3 mu[kGLobes];
+    float len[kGLobes], kap[kGLobes];
+    for (int k = 0; k < kGLobes; k++) {
+        const float3 m = mk(r[5 * k], r[5 * k + 1], r[5 * k + 2]);
+        len[k] = fmaxf(sqrtf(dot(m, m)), 1.0e-6f);
+        mu[k] = m * (1.0f / len[k]);
+        kap[k] = kappaOf(r[5 * k + 3]);
+        vk[k] = vmfPdf(w, mu[k], kap[k]);
+        wk[k] = __expf(r[5 * k + 4] - mx);
+        s += wk[k];
+    }
+    float p = 0.0f;
+    for (int k = 0; k < kGLobes; k++) {
+        wk[k] /= s;
+        p += wk[k] * vk[k];
+    }
+    p = fmaxf(p, 1.0e-30f);
+    const float a = -c / p;
+    for (int k = 0; k < kGLobes; k++) {
+        const float dv = a * wk[k];   // dLoss / dv_k
+        const float kr = r[5 * k + 3];
+        const float dlogv_dk = 1.0f / kap[k] - 2.0f / expm1f(2.0f * kap[k]) + (dot(mu[k], w) - 1.0f);
+        g[5 * k + 3] = (kr > -4.0f && kr < 7.0f) ? dv * vk[k] * dlogv_dk * kap[k] : 0.0f;
+        const float3 gmu = w * (dv * vk[k] * kap[k]);
+        const float3 gm = (gmu - mu[k] * dot(mu[k], gmu)) * (1.0f / len[k]);
+        g[5 * k] = gm.x;
+        g[5 * k + 1] = gm.y;
+        g[5 * k + 2] = gm.z;
+        g[5 * k + 4] = a * wk[k] * (vk[k] - p);
+    }
+    return -c * __logf(p);
+}
+
+// ------------------------------------------------------------------ training
+constexpr int kTrainStride = 65;   // fp32 row stride of the dy tile
+struct TrainLayout {
+    static constexpr int wf = 0;
+    static constexpr int wb = wf + kPackFwdBytes;
+    static constexpr int bias = wb + kPackBwdBytes;
+    static constexpr int x = bias + kBiasPad * 4;
+    static constexpr int h1 = x + kGTile * kGK0 * 2;
+    static constexpr int h2 = h1 + kGTile * kGHid * 2;
+    static constexpr int h3 = h2 + kGTile * kGHid * 2;
+    static constexpr int dyb = h3 + kGTile * kGHid * 2;
+    static constexpr int dy = dyb + kGTile * kGHid * 2;
+    static constexpr int gw = dy + kGTile * kTrainStride * 4;
+    static constexpr int bar = gw + kGParams * 4;
+    static constexpr int tmem = bar + 8;
+    static constexpr int total = tmem + 8;
+};
+static_assert(TrainLayout::x % 16 == 0 && TrainLayout::h1 % 16 == 0 && TrainLayout::dyb % 16 == 0, "alignment");
+static_assert(TrainLayout::bar % 8 == 0, "alignment");
+
+// dW[o][i] += sum_r dy[r][o] * h[r][i] for this tile; bias[o] += sum_r dy[r][o]
+__device__ __forceinline__ void accumLayer(float *gw, int offW, int offB, int nOut, int nIn, const float *dy,
+                                           const uint8_t *h, int Kh) {
+    for (int e = threadIdx.x; e < nOut * nIn; e += kGTile) {
+        const int o = e / nIn, i = e % nIn;
+        float s = 0.0f;
+        for (int r = 0; r < kGTile; r++) s += dy[r * kTrainStride + o] * loadBf16(h, r, i, Kh);
+        gw[offW + e] += s;
+    }
+    for (int o = threadIdx.x; o < nOut; o += kGTile) {
+        float s = 0.0f;
+        for (int r = 0; r < kGTile; r++) s += dy[r * kTrainStride + o];
+        gw[offB + o] += s;
+    }
+}
+
+// backward epilogue: g = acc * relu'(h) -> dy (fp32) and dyb (bf16, K = 64)
+__device__ __forceinline__ void backEpilogue(uint32_t tmem, const uint8_t *h, float *dy, uint8_t *dyb) {
+    const uint32_t r = threadIdx.x;
+    for (uint32_t c = 0; c < kGHid; c += 16) {
+        float v[16];
+        accRow16(tmem, c, v);
+        for (int i = 0; i < 16; i++) {
+            v[i] = loadBf16(h, r, c + i, kGHid) > 0.0f ? v[i] : 0.0f;
+            dy[r * kTrainStride + c + i] = v[i];
+        }
+        storeRow8(dyb, r, c, kGHid, v);
+        storeRow8(dyb, r, c + 8, kGHid, v + 8);
+    }
+}
+
+__global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__restrict__ packFwd,
+                                                           const uint8_t *__restrict__ packBwd,
+                                                           const float *__restrict__ biasPad,
+                                                           const float *__restrict__ samples, int n, float cScale,
+                                                           float cMax, float *grad, double *lossAcc, int *err) {
+    extern __shared__ __align__(128) uint8_t sm[];
+    uint8_t *wf = sm + TrainLayout::wf, *wb = sm + TrainLayout::wb;
+    float *bias = reinterpret_cast<float *>(sm + TrainLayout::bias);
+    uint8_t *x = sm + TrainLayout::x, *h1 = sm + TrainLayout::h1, *h2 = sm + TrainLayout::h2,
+            *h3 = sm + TrainLayout::h3, *dyb = sm + TrainLayout::dyb;
+    float *dy = reinterpret_cast<float *>(sm + TrainLayout::dy);
+    float *gw = reinterpret_cast<float *>(sm + TrainLayout::gw);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + TrainLayout::bar);
+    uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + TrainLayout::tmem);
+    const int t = threadIdx.x;
+    for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
+        reinterpret_cast<uint4 *>(wf)[i] = reinterpret_cast<const uint4 *>(packFwd)[i];
+    for (int i = t; i < kPackBwdBytes / 16; i += kGTile)
+        reinterpret_cast<uint4 *>(wb)[i] = reinterpret_cast<const uint4 *>(packBwd)[i];
+    for (int i = t; i < kBiasPad; i += kGTile) bias[i] = biasPad[i];
+    for (int i = t; i < kGParams; i += kGTile) gw[i] = 0.0f;
+    if (t == 0) tc::mbarInit(bar, 1);
+    if (t < 32) {
+        tc::tmemAlloc(tmemSlot, 64);
+        tc::tmemRelinquish();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tmem = *tmemSlot;
+    uint32_t phase = 0;
+    bool ok = true;
+    float lossSum = 0.0f, wSum = 0.0f;
+    const uint8_t *w2b = wb, *w3b = wb + kW2fBytes, *w4b = wb + 2 * kW2fBytes;
+    for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
+        const int s = tile * kGTile + t;
+        float xf[16];
+        float3 w = mk(0, 0, 1);
+        float c = 0.0f;
+        for (int i = 0; i < 16; i++) xf[i] = 0.0f;
+        if (s < n) {
+            const float *S = samples + 16 * static_cast<int64_t>(s);
+            for (int i = 0; i < kGIn; i++) xf[i] = S[i];
+            w = mk(S[9], S[10], S[11]);
+            c = fminf(S[12], cMax) * cScale;
+        }
+        storeRow8(x, t, 0, kGK0, xf);
+        storeRow8(x, t, 8, kGK0, xf + 8);
+        ok = mlpForwardTile(tmem, wf, bias, x, h1, h2, h3, dy, kTrainStride, bar, phase);
+        if (!ok) break;
+        // loss gradient on this thread's row
+        {
+            float r[kGOut], g[kGN4];
+            for (int j = 0; j < kGOut; j++) r[j] = dy[t * kTrainStride + j];
+            for (int j = 0; j < kGN4; j++) g[j] = 0.0f;
+            if (s < n && c > 0.0f) {
+                lossSum += mixtureLossGrad(r, w, c, g);
+                wSum += c;
+            }
+            for (int j = 0; j < kGN4; j++) dy[t * kTrainStride + j] = g[j];
+            for (int j = 0; j < kGN4; j += 8) storeRow8(dyb, t, j, kGN4, g + j);
+        }
+        __syncthreads();
+        accumLayer(gw, kOffW4, kOffB4, kGOut, kGHid, dy, h3, kGHid);
+        ok = tileMma(tmem, dyb, w4b, kGN4, kGHid, bar, phase);   // dX3 = dY4 W4
+        if (!ok) break;
+        backEpilogue(tmem, h3, dy, dyb);
+        __syncthreads();
+        accumLayer(gw, kOffW3, kOffB3, kGHid, kGHid, dy, h2, kGHid);
+        ok = tileMma(tmem, dyb, w3b, kGHid, kGHid, bar, phase);   // dX2 = dY3 W3
+        if (!ok) break;
+        backEpilogue(tmem, h2, dy, dyb);
+        __syncthreads();
+        accumLayer(gw, kOffW2, kOffB2, kGHid, kGHid, dy, h1, kGHid);
+        ok = tileMma(tmem, dyb, w2b, kGHid, kGHid, bar, phase);   // dX1 = dY2 W2
+        if (!ok) break;
+        backEpilogue(tmem, h1, dy, dyb);
+        __syncthreads();
+        accumLayer(gw, kOffW1, kOffB1, kGHid, kGIn, dy, x, kGK0);
+        __syncthreads();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (t < 32) tc::tmemDealloc(tmem, 64);
+    if (!ok) {
+        if (t == 0) atomicOr(err, 1);
+        return;
+    }
+    for (int i = t; i < kGParams; i += kGTile) atomicAdd(&grad[i], gw[i]);
+    for (int off = 16; off > 0; off >>= 1) {
+        lossSum += __shfl_xor_sync(0xffffffffu, lossSum, off);
+        wSum += __shfl_xor_sync(0xffffffffu, wSum, off);
+    }
+    if ((t & 31) == 0) {
+        atomicAdd(&lossAcc[0], static_cast<double>(lossSum));
+        atomicAdd(&lossAcc[1], static_cast<double>(wSum));
+    }
+}
+
+// inference only (tests and tools): features [n][9] -> raw outputs [n][40]
+__global__ void __launch_bounds__(kGTile, 1) k_guide_forward(const uint8_t *__restrict__ packFwd,
+                                                             const float *__restrict__ biasPad,
+                                                             const float *__restrict__ feat, int n, float *out,
+                                                             int *err) {
+    extern __shared__ __align__(128) uint8_t sm[];
+    uint8_t *wf = sm;
+    float *bias = reinterpret_cast<float *>(sm + kPackFwdBytes);
+    uint8_t *x = sm + kPackFwdBytes + kBiasPad * 4;
+    uint8_t *h = x + kGTile * kGK0 * 2;
+    float *o = reinterpret_cast<float *>(h + kGTile * kGHid * 2);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(reinterpret_cast<uint8_t *>(o) + kGTile * 41 * 4);
+    uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int t = threadIdx.x;
+    for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
+        reinterpret_cast<uint4 *>(wf)[i] = reinterpret_cast<const uint4 *>(packFwd)[i];
+    for (int i = t; i < kBiasPad; i += kGTile) bias[i] = biasPad[i];
+    if (t == 0) tc::mbarInit(bar, 1);
+    if (t < 32) {
+        tc::tmemAlloc(tmemSlot, 64);
+        tc::tmemRelinquish();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tmem = *tmemSlot;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
+        const int s = tile * kGTile + t;
+        float xf[16];
+        for (int i = 0; i < 16; i++) xf[i] = (s < n && i < kGIn) ? feat[9 * static_cast<int64_t>(s) + i] : 0.0f;
+        storeRow8(x, t, 0, kGK0, xf);
+        storeRow8(x, t, 8, kGK0, xf + 8);
+        ok = mlpForwardTile(tmem, wf, bias, x, h, h, h, o, 41, bar, phase);
+        if (ok && s < n)
+            for (int j = 0; j < kGOut; j++) out[kGOut * static_cast<int64_t>(s) + j] = o[t * 41 + j];
+        __syncthreads();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (t < 32) tc::tmemDealloc(tmem, 64);
+    if (!ok && t == 0) atomicOr(err, 1);
+}
+constexpr int kForwardSmem = kPackFwdBytes + kBiasPad * 4 + kGTile * kGK0 * 2 + kGTile * kGHid * 2 + kGTile * 41 * 4 + 16;
+
+// ------------------------------------------------------------------ Adam
+__global__ void k_adam(float *P, float *G, float *M, float *V, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float g = G[i];
+        const float m = b1 * M[i] + (1.0f - b1) * g;
+        const float v = b2 * V[i] + (1.0f - b2) * g * g;
+        M[i] = m;
+        V[i] = v;
+        P[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+        G[i] = 0.0f;
+    }
+}
+
+// gather a random batch from the ring and its weight statistics
+__global__ void k_gather(const float *ring, const int *idx, int n, float *batch, float *wsum) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const float4 *src = reinterpret_cast<const float4 *>(ring + 16 * static_cast<int64_t>(idx[s]));
+        float4 *dst = reinterpret_cast<float4 *>(batch + 16 * static_cast<int64_t>(s));
+        for (int k = 0; k < 4; k++) dst[k] = src[k];
+        atomicAdd(&wsum[0], batch[16 * static_cast<int64_t>(s) + 12]);
+    }
+}
+
+// ------------------------------------------------------------------ guided tracer
+struct TrainRec {
+    float x[kGIn];
+    float3 w;
+    float q;
+    float3 fcos, Lafter, beta, E;
+};
+
+struct GuidedArgs {
+    SceneView sv;
+    CameraView cam;
+    int W, H, npix;
+    long long total;   // paths to trace
+    int sampleOffset;
+    int maxDepth;
+    uint32_t seed;
+    float4 *film;
+    const uint8_t *packFwd;
+    const float *biasPad;
+    float3 lo, invExt;
+    float alpha;   // BSDF probability in the one-sample MIS mixture
+    float *ring;
+    int capacity;
+    int *ctl;      // [0] samples written, [1] error, [2] path counter
+    unsigned long long *stats;
+};
+
+constexpr int kGuidedSmem = kPackFwdBytes + kBiasPad * 4 + kGTile * kGK0 * 2 + kGTile * kGHid * 2 +
+                            kGTile * 41 * 4 + kStackShared * kGTile * 8 + 16;
+constexpr int kMaxRec = 13;
+
+__device__ __forceinline__ float lum(float3 c) { return gray(c); }
+
+// one-sample MIS mixture of cosine-weighted Lambert sampling and the vMF mixture
+struct MixProposal {
+    const Mixture *M;
+    float alpha;
+    __device__ float pdf(const MaterialRecord &m, float3 woL, float3 wiL, float3 wiW) const {
+        const float pb = bsdfPdf(m, woL, wiL);
+        return M ? alpha * pb + (1.0f - alpha) * mixturePdf(*M, wiW) : pb;
+    }
+    // returns f (times nothing), world direction, pdf; false if the sample is invalid
+    __device__ bool sample(const MaterialRecord &m, float3 woL, float3 tg, float3 bg, float3 n, float uSel,
+                           float uLobe, float u1, float u2, float3 *wiW, float3 *f, float *pdf) const {
+        float3 wiL;
+        if (!M || uSel < alpha) {
+            float pb;
+            int type;
+            const float3 fb = bsdfSample(m, woL, u1, u2, &wiL, &pb, &type);
+            if (isBlack(fb) || pb <= 0.0f) return false;
+            *wiW = normalize(tg * wiL.x + bg * wiL.y + n * wiL.z);
+        } else {
+            *wiW = mixtureSample(*M, uLobe, u1, u2);
+            wiL = mk(dot(*wiW, tg), dot(*wiW, bg), dot(*wiW, n));
+        }
+        *f = bsdfF(m, woL, wiL);
+        *pdf = this->pdf(m, woL, wiL, *wiW);
+        return *pdf > 0.0f;
+    }
+};
+
+template <bool GUIDED, bool COLLECT>
+__global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
+    extern __shared__ __align__(128) uint8_t sm[];
+    uint8_t *wf = sm;
+    float *bias = reinterpret_cast<float *>(sm + kPackFwdBytes);
+    uint8_t *x = sm + kPackFwdBytes + kBiasPad * 4;
+    uint8_t *h = x + kGTile * kGK0 * 2;
+    float *out = reinterpret_cast<float *>(h + kGTile * kGHid * 2);
+    uint2 *stack = reinterpret_cast<uint2 *>(reinterpret_cast<uint8_t *>(out) + kGTile * 41 * 4);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(stack + kStackShared * kGTile);
+    uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int t = threadIdx.x;
+    const SceneView &S = a.sv;
+    uint32_t tmem = 0, phase = 0;
+    if (GUIDED) {
+        for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
+            reinterpret_cast<uint4 *>(wf)[i] = reinterpret_cast<const uint4 *>(a.packFwd)[i];
+        for (int i = t; i < kBiasPad; i += kGTile) bias[i] = a.biasPad[i];
+        if (t == 0) tc::mbarInit(bar, 1);
+        if (t < 32) {
+            tc::tmemAlloc(tmemSlot, 64);
+            tc::tmemRelinquish();
+        }
+        tc::fenceBeforeSync();
+        __syncthreads();
+        tc::fenceAfterSync();
+        tmem = *tmemSlot;
+    }
+    bool overflow = false, mmaOk = true;
+    uint32_t dummy = 0;
+    unsigned long long nPaths = 0, nClosest = 0, nShadow = 0;
+    // path state
+    bool active = false, exhausted = false;
+    int fi = 0, b = 0;
+    uint32_t sample = 0;
+    float3 o = mk(0, 0, 0), d = mk(0, 0, 1), beta = mk(1, 1, 1), L = mk(0, 0, 0);
+    bool spec = false;
+    TrainRec rec[COLLECT ? kMaxRec : 1];
+    int nrec = 0;
+    while (true) {
+        // ---- start new paths in idle lanes
+        const bool want = !active && !exhausted;
+        const unsigned wmask = __ballot_sync(0xffffffffu, want);
+        if (wmask) {
+            const int lane = t & 31, leader = __ffs(wmask) - 1;
+            long long base = 0;
+            if (lane == leader) base = atomicAdd(reinterpret_cast<unsigned long long *>(&a.ctl[2]),
+                                                 static_cast<unsigned long long>(__popc(wmask)));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (want) {
+                const long long id = base + __popc(wmask & ((1u << lane) - 1u));
+                if (id < a.total) {
+                    const int pix = static_cast<int>(id % a.npix);
+                    sample = static_cast<uint32_t>(a.sampleOffset + id / a.npix);
+                    const int y = pix / a.W, xx = pix - y * a.W;
+                    fi = y * a.W + (a.W - 1 - xx);
+                    const Rand4 r = rand4(a.seed, static_cast<uint32_t>(fi), sample, 0xFFFFu, 0u);
+                    spawnCameraRay(a.cam, xx, y, r.a, r.b, &o, &d);
+                    beta = mk(1, 1, 1);
+                    L = mk(0, 0, 0);
+                    spec = false;
+                    b = 0;
+                    nrec = 0;
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__syncthreads_and(!active)) break;
+        // ---- extend
+        HitRecord hr;
+        bool hit = false;
+        if (active) {
+            float tmax = kInfT, u, v;
+            int slot = -1;
+            nClosest++;
+            hit = traceWide<false, false>(S.nodes, S.tris, S.nNodes, S.nTris, o, d, 0.0f, tmax, slot, u, v,
+                                          stack + t, kGTile, &dummy, &dummy, &overflow);
+            hr.t = tmax;
+            hr.prim = slot;
+            hr.u = u;
+            hr.v = v;
+        }
+        bool ends = false;
+        float3 n = mk(0, 0, 1), ps = mk(0, 0, 0);
+        MaterialRecord m;
+        m.type = -1;
+        int lightOf = -1;
+        if (active) {
+            if (!hit) {
+                const float3 Le = S.hasEnv ? envLe(S.env, d) : mk(0, 0, 0);
+                if (b == 0 || spec) L = L + beta * Le;
+                if (COLLECT && nrec > 0) rec[nrec - 1].E = Le;   // direct radiance along the last sampled dir
+                ends = true;
+            } else {
+                const TriRecord tr = S.tris[hr.prim];
+                n = normalize(cross(xyz(tr.v1) - xyz(tr.v0), xyz(tr.v2) - xyz(tr.v0)));
+                const int2 sh = __ldg(&S.slotShade[hr.prim]);
+                m = S.mats[sh.x];
+                lightOf = sh.y;
+                ps = o + d * hr.t;
+                if (COLLECT && nrec > 0 && lightOf >= 0 && dot(n, -d) > 0.0f) rec[nrec - 1].E = xyz(S.lights[lightOf].L);
+                if (b >= a.maxDepth) {
+                    if ((b == 0 || spec) && lightOf >= 0 && dot(n, -d) > 0.0f) L = L + beta * xyz(S.lights[lightOf].L);
+                    ends = true;
+                }
+            }
+        }
+        const bool guideMe = GUIDED && active && !ends && m.type == kMatLambert;
+        // ---- network inference for the whole CTA (rows of other lanes are zero)
+        Mixture mix;
+        if (GUIDED) {
+            float xf[16];
+            for (int i = 0; i < 16; i++) xf[i] = 0.0f;
+            if (guideMe) guideFeatures(ps, n, -d, a.lo, a.invExt, xf);
+            storeRow8(x, t, 0, kGK0, xf);
+            storeRow8(x, t, 8, kGK0, xf + 8);
+            if (__syncthreads_or(guideMe) && mmaOk)
+                mmaOk = mlpForwardTile(tmem, wf, bias, x, h, h, h, out, 41, bar, phase);
+            if (guideMe && mmaOk) mixtureFromRaw(out + t * 41, mix);
+        }
+        // ---- shade
+        if (active && !ends) {
+            ShadeResult R;
+            if (!guideMe || !mmaOk) {
+                shadeHit(S, hr, o, d, beta, spec, b, a.maxDepth, a.seed, static_cast<uint32_t>(fi), sample, fi, R);
+            } else {
+                // the wavefront's shadeHit for a Lambert hit, with the BSDF strategy replaced
+                // by the mixture proposal (NEE weights use its pdf too)
+                R.emit = mk(0, 0, 0);
+                R.cont = R.sh0 = R.sh1 = false;
+                if ((b == 0 || spec) && lightOf >= 0 && dot(n, -d) > 0.0f) R.emit = beta * xyz(S.lights[lightOf].L);
+                MixProposal P{&mix, a.alpha};
+                float3 tg, bg;
+                onb(n, &tg, &bg);
+                const float3 wo = -d;
+                const float3 woL = mk(dot(wo, tg), dot(wo, bg), dot(wo, n));
+                const Rand4 r0 = rand4(a.seed, static_cast<uint32_t>(fi), sample, static_cast<uint32_t>(b), 0u);
+                const Rand4 r1 = rand4(a.seed, static_cast<uint32_t>(fi), sample, static_cast<uint32_t>(b), 1u);
+                const Rand4 r2 = rand4(a.seed, static_cast<uint32_t>(fi), sample, static_cast<uint32_t>(b), 2u);
+                if (S.nLights > 0) {
+                    const int nL = S.nLights;
+                    const int li = min(static_cast<int>(r0.a * nL), nL - 1);
+                    const bool isEnv = li >= S.nArea;
+                    const float3 scale = beta * static_cast<float>(nL);
+                    float3 wi = mk(0, 0, 0), Li = mk(0, 0, 0), target = mk(0, 0, 0), tn = mk(0, 0, 0);
+                    float lightPdf = 0.0f;
+                    if (!isEnv) {
+                        const LightRecord Lr = S.lights[S.lightBase + li];
+                        float u0 = r0.b, u1 = r0.c;
+                        if (u0 + u1 >= 1.0f) {
+                            u0 = 1.0f - u0;
+                            u1 = 1.0f - u1;
+                        }
+                        target = xyz(Lr.p0) + xyz(Lr.e1) * u0 + xyz(Lr.e2) * u1;
+                        tn = xyz(Lr.n);
+                        wi = normalize(target - ps);
+                        float tl;
+                        lightPdf = lightTriPdf(Lr, ps, n, wi, &tl);
+                        if (dot(tn, -wi) > 0.0f) Li = xyz(Lr.L);
+                    } else {
+                        const DeviceEnv &E = S.env;
+                        float pv, pu;
+                        int vOff, uOff;
+                        const float vv = sample1D(E.margCdf, E.margFunc, E.h, E.margIntegral, r0.c, &pv, &vOff);
+                        const float uu = sample1D(E.condCdf + static_cast<int64_t>(vOff) * (E.w + 1),
+                                                  E.condFunc + static_cast<int64_t>(vOff) * E.w, E.w,
+                                                  __ldg(&E.margFunc[vOff]), r0.b, &pu, &uOff);
+                        const float mapPdf = pu * pv;
+                        if (mapPdf > 0.0f) {
+                            float st, ct, sp, cp;
+                            sincosf(vv * kPi, &st, &ct);
+                            sincosf(uu * 2.0f * kPi, &sp, &cp);
+                            wi = mk(st * cp, st * sp, ct);
+                            lightPdf = st == 0.0f ? 0.0f : mapPdf / (2.0f * kPi * kPi * st);
+                            Li = envLookup(E, uu, vv);
+                            target = ps + wi * (2.0f * E.radius);
+                        }
+                    }
+                    if (lightPdf > 0.0f && !isBlack(Li)) {
+                        const float3 wiL = mk(dot(wi, tg), dot(wi, bg), dot(wi, n));
+                        const float3 f = bsdfF(m, woL, wiL) * fabsf(dot(wi, n));
+                        if (!isBlack(f)) {
+                            const float w = powerHeuristic(lightPdf, P.pdf(m, woL, wiL, wi));
+                            const float3 c = scale * f * Li * (w / lightPdf);
+                            const float3 oo = offsetOrigin(ps, n, target - ps);
+                            const float3 t2 = isEnv ? mk(nextafterf(target.x, -INFINITY),
+                                                         nextafterf(target.y, -INFINITY),
+                                                         nextafterf(target.z, -INFINITY))
+                                                    : offsetOrigin(target, tn, oo - target);
+                            const float3 dd = t2 - oo;
+                            const float len = length(dd);
+                            if (len > 0.0f) {
+                                R.sh0 = true;
+                                R.s0O = make_float4(oo.x, oo.y, oo.z, 0.0f);
+                                R.s0D = make_float4(dd.x / len, dd.y / len, dd.z / len, len);
+                                R.s0L = make_float4(c.x, c.y, c.z, 0.0f);
+                            }
+                        }
+                    }
+                    // the mixture strategy of MIS
+                    float3 wi2, f2;
+                    float pdf2;
+                    if (P.sample(m, woL, tg, bg, n, r2.a, r2.b, r0.d, r1.a, &wi2, &f2, &pdf2) && !isBlack(f2)) {
+                        f2 = f2 * fabsf(dot(wi2, n));
+                        float lp = 0.0f, tl = 0.0f;
+                        float3 L2 = mk(0, 0, 0);
+                        if (!isEnv) {
+                            const LightRecord Lr = S.lights[S.lightBase + li];
+                            lp = lightTriPdf(Lr, ps, n, wi2, &tl);
+                            if (lp > 0.0f && dot(xyz(Lr.n), -wi2) > 0.0f) L2 = xyz(Lr.L);
+                        } else {
+                            lp = envPdf(S.env, wi2);
+                            if (lp > 0.0f) L2 = envLe(S.env, wi2);
+                        }
+                        if (lp > 0.0f && !isBlack(L2)) {
+                            const float w = powerHeuristic(pdf2, lp);
+                            const float3 c = scale * f2 * L2 * (w / pdf2);
+                            const float3 oo = offsetOrigin(ps, n, wi2);
+                            R.sh1 = true;
+                            R.s1O = make_float4(oo.x, oo.y, oo.z, 0.0f);
+                            R.s1D = make_float4(wi2.x, wi2.y, wi2.z, isEnv ? kInfT : tl * (1.0f - 1.0e-5f));
+                            R.s1L = make_float4(c.x, c.y, c.z, 0.0f);
+                        }
+                    }
+                }
+                // continuation from the mixture, Russian roulette
+                float3 wi, f;
+                float pdf;
+                R.beta = beta;
+                R.spec = false;
+                if (P.sample(m, woL, tg, bg, n, r2.c, r2.d, r1.b, r1.c, &wi, &f, &pdf) && !isBlack(f)) {
+                    const float3 fc = f * fabsf(dot(wi, n));
+                    R.beta = beta * fc * (1.0f / pdf);
+                    R.cont = true;
+                    if (b > 3) {
+                        const float q = fminf(0.95f, gray(R.beta));
+                        if (r1.d > q) R.cont = false;
+                        else R.beta = R.beta / q;
+                    }
+                    if (R.cont) {
+                        const float3 oo = offsetOrigin(ps, n, wi);
+                        R.cO = make_float4(oo.x, oo.y, oo.z, 0.0f);
+                        R.cD = make_float4(wi.x, wi.y, wi.z, kInfT);
+                        if (COLLECT && nrec < kMaxRec) {
+                            TrainRec &T = rec[nrec++];
+                            guideFeatures(ps, n, wo, a.lo, a.invExt, T.x);
+                            T.w = wi;
+                            T.q = pdf;
+                            T.fcos = fc;
+                            T.beta = R.beta;
+                            T.E = mk(0, 0, 0);
+                        }
+                    }
+                }
+            }
+            L = L + R.emit;
+            float u, v, tmx;
+            int slot;
+            if (R.sh0) {
+                nShadow++;
+                tmx = R.s0D.w;
+                if (!traceWide<true, false>(S.nodes, S.tris, S.nNodes, S.nTris, xyz(R.s0O), xyz(R.s0D), 0.0f, tmx,
+                                            slot, u, v, stack + t, kGTile, &dummy, &dummy, &overflow))
+                    L = L + xyz(R.s0L);
+            }
+            if (R.sh1) {
+                nShadow++;
+                tmx = R.s1D.w;
+                if (!traceWide<true, false>(S.nodes, S.tris, S.nNodes, S.nTris, xyz(R.s1O), xyz(R.s1D), 0.0f, tmx,
+                                            slot, u, v, stack + t, kGTile, &dummy, &dummy, &overflow))
+                    L = L + xyz(R.s1L);
+            }
+            if (COLLECT && guideMe && R.cont && nrec > 0) rec[nrec - 1].Lafter = L;
+            if (R.cont) {
+                o = xyz(R.cO);
+                d = xyz(R.cD);
+                beta = R.beta;
+                spec = R.spec;
+                b++;
+            } else {
+                ends = true;
+            }
+        }
+        if (active && ends) {
+            atomicAdd(&a.film[fi], make_float4(L.x, L.y, L.z, 1.0f));
+            nPaths++;
+            if (COLLECT) {
+                // incident radiance along each guided direction: direct radiance found by the
+                // continuation ray plus everything the path gathered afterwards, divided by
+                // the throughput at that point
+                for (int k = 0; k < nrec; k++) {
+                    const TrainRec &T = rec[k];
+                    float3 Li = T.E;
+                    const float3 rest = L - T.Lafter;
+                    Li.x += T.beta.x > 0.0f ? rest.x / T.beta.x : 0.0f;
+                    Li.y += T.beta.y > 0.0f ? rest.y / T.beta.y : 0.0f;
+                    Li.z += T.beta.z > 0.0f ? rest.z / T.beta.z : 0.0f;
+                    const float c = lum(T.fcos * Li) / T.q;
+                    if (!(c > 0.0f) || !isfinite(c)) continue;
+                    const int slotIdx = atomicAdd(&a.ctl[0], 1) % a.capacity;
+                    float *D = a.ring + 16 * static_cast<int64_t>(slotIdx);
+                    for (int i = 0; i < kGIn; i++) D[i] = T.x[i];
+                    D[9] = T.w.x;
+                    D[10] = T.w.y;
+                    D[11] = T.w.z;
+                    D[12] = c;
+                }
+            }
+            active = false;
+        }
+    }
+    if (GUIDED) {
+        tc::fenceBeforeSync();
+        __syncthreads();
+        if (t < 32) tc::tmemDealloc(tmem, 64);
+    }
+    if (overflow || !mmaOk) atomicOr(&a.ctl[1], 1);
+    atomicAdd(&a.stats[0], nPaths);
+    atomicAdd(&a.stats[1], nClosest);
+    atomicAdd(&a.stats[2], nShadow);
+}
+
+template <class T>
+T *galloc(size_t n) {
+    T *p = nullptr;
+    return cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)) == cudaSuccess ? p : nullptr;
+}
+
+int packWeights(GuideState &G, cudaStream_t s) {
+    k_guide_pack<<<32, 256, 0, s>>>(G.master, G.packFwd, G.packBwd, G.biasPad);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : cudaFail("guide pack", e);
+}
+
+}  // namespace
+
+void freeGuide(GuideState *G) {
+    if (!G) return;
+    cudaFree(G->master);
+    cudaFree(G->grad);
+    cudaFree(G->m);
+    cudaFree(G->v);
+    cudaFree(G->packFwd);
+    cudaFree(G->packBwd);
+    cudaFree(G->biasPad);
+    cudaFree(G->samples);
+    cudaFree(G->ctl);
+    cudaFree(G->lossAcc);
+    cudaFree(G->wsum);
+    cudaFree(G->batchIdx);
+    cudaFree(G->batch);
+    delete G;
+}
+
+int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg) {
+    freeGuide(*slot);
+    *slot = nullptr;
+    auto *G = new GuideState();
+    G->cfg = *cfg;
+    if (G->cfg.learning_rate <= 0.0f) G->cfg.learning_rate = 1.0e-3f;
+    if (G->cfg.bsdf_fraction < 0.2f) G->cfg.bsdf_fraction = 0.2f;
+    if (G->cfg.batch <= 0) G->cfg.batch = 16384;
+    if (G->cfg.capacity <= 0) G->cfg.capacity = 1 << 21;
+    G->capacity = G->cfg.capacity;
+    G->batchCap = ((G->cfg.batch + kGTile - 1) / kGTile) * kGTile;
+    G->rng.seed(G->cfg.seed);
+    G->master = galloc<float>(kGParams);
+    G->grad = galloc<float>(kGParams);
+    G->m = galloc<float>(kGParams);
+    G->v = galloc<float>(kGParams);
+    G->packFwd = galloc<uint8_t>(kPackFwdBytes);
+    G->packBwd = galloc<uint8_t>(kPackBwdBytes);
+    G->biasPad = galloc<float>(kBiasPad);
+    G->samples = galloc<float>(static_cast<size_t>(G->capacity) * 16);
+    G->ctl = galloc<int>(4);
+    G->lossAcc = galloc<double>(2);
+    G->wsum = galloc<float>(2);
+    G->batchIdx = galloc<int>(G->batchCap);
+    G->batch = galloc<float>(static_cast<size_t>(G->batchCap) * 16);
+    if (!G->master || !G->grad || !G->m || !G->v || !G->packFwd || !G->packBwd || !G->biasPad || !G->samples ||
+        !G->ctl || !G->lossAcc || !G->wsum || !G->batchIdx || !G->batch) {
+        freeGuide(G);
+        setError("spgpu_guiding_init: device allocation failed");
+        return SPGPU_ENOMEM;
+    }
+    // He-uniform initialisation of the weights, zero biases
+    std::vector<float> P(kGParams, 0.0f);
+    auto fill = [&](int off, int nOut, int nIn) {
+        std::uniform_real_distribution<float> U(-1.0f, 1.0f);
+        const float s = std::sqrt(6.0f / nIn);
+        for (int i = 0; i < nOut * nIn; i++) P[off + i] = s * U(G->rng);
+    };
+    fill(kOffW1, kGHid, kGIn);
+    fill(kOffW2, kGHid, kGHid);
+    fill(kOffW3, kGHid, kGHid);
+    fill(kOffW4, kGOut, kGHid);
+    for (int i = 0; i < kGOut * kGHid; i++) P[kOffW4 + i] *= 0.1f;   // start near a broad, uniform mixture
+    cudaMemcpy(G->master, P.data(), sizeof(float) * kGParams, cudaMemcpyHostToDevice);
+    cudaMemset(G->grad, 0, sizeof(float) * kGParams);
+    cudaMemset(G->m, 0, sizeof(float) * kGParams);
+    cudaMemset(G->v, 0, sizeof(float) * kGParams);
+    cudaMemset(G->ctl, 0, sizeof(int) * 4);
+    cudaMemset(G->samples, 0, sizeof(float) * 16 * static_cast<size_t>(G->capacity));
+    int rc = packWeights(*G, C.stream);
+    if (rc == 0 && cudaStreamSynchronize(C.stream) != cudaSuccess) rc = cudaFail("spgpu_guiding_init", cudaGetLastError());
+    if (rc) {
+        freeGuide(G);
+        return rc;
+    }
+    static bool attrsSet = false;
+    if (!attrsSet) {
+        cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TrainLayout::total);
+        cudaFuncSetAttribute(k_guide_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kForwardSmem);
+        cudaFuncSetAttribute(k_guided<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
+        cudaFuncSetAttribute(k_guided<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
+        cudaFuncSetAttribute(k_guided<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
+        attrsSet = true;
+    }
+    *slot = G;
+    return 0;
+}
+
+int guideParams(Ctx &C, GuideState &G, float *host, int set) {
+    cudaError_t e;
+    if (set) {
+        e = cudaMemcpy(G.master, host, sizeof(float) * kGParams, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cudaFail("spgpu_guiding_params", e);
+        int rc = packWeights(G, C.stream);
+        if (rc) return rc;
+        e = cudaStreamSynchronize(C.stream);
+    } else {
+        e = cudaMemcpy(host, G.master, sizeof(float) * kGParams, cudaMemcpyDeviceToHost);
+    }
+    return e == cudaSuccess ? 0 : cudaFail("spgpu_guiding_params", e);
+}
+
+int guideForward(Ctx &C, GuideState &G, const float *feat, int n, float *out, cudaStream_t s) {
+    cudaMemsetAsync(G.ctl + 1, 0, sizeof(int), s);
+    const int tiles = (n + kGTile - 1) / kGTile;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
+    k_guide_forward<<<std::min(tiles, sms), kGTile, kForwardSmem, s>>>(G.packFwd, G.biasPad, feat, n, out, G.ctl + 1);
+    int err = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, G.ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cudaFail("spgpu_guiding_mlp", e);
+    if (err) {
+        setError("spgpu_guiding_mlp: tensor-core wait timed out");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
+}
+
+// gradient of the batch loss (mean of c_i * -log p(w_i), c normalised by its sum)
+int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s,
+              bool accumulateOnly) {
+    if (n <= 0) return 0;
+    // weight sum for normalisation
+    cudaMemsetAsync(G.wsum, 0, 2 * sizeof(float), s);
+    cudaMemsetAsync(G.lossAcc, 0, 2 * sizeof(double), s);
+    cudaMemsetAsync(G.ctl + 1, 0, sizeof(int), s);
+    std::vector<float> hs(1);
+    // sum of c over the batch (host round trip is fine: a few KB per step)
+    std::vector<float> cs(static_cast<size_t>(n));
+    cudaMemcpy2DAsync(cs.data(), sizeof(float), samples + 12, 16 * sizeof(float), sizeof(float), n,
+                      cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    double sum = 0.0;
+    for (float c : cs) sum += c;
+    if (!(sum > 0.0)) {
+        if (loss) *loss = 0.0;
+        return 0;
+    }
+    const float cMax = static_cast<float>(50.0 * sum / n);
+    const int tiles = (n + kGTile - 1) / kGTile;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
+    float *grad = gradOut ? gradOut : G.grad;
+    if (gradOut && !accumulateOnly) cudaMemsetAsync(gradOut, 0, sizeof(float) * kGParams, s);
+    k_guide_train<<<std::min(tiles, sms), kGTile, TrainLayout::total, s>>>(
+        G.packFwd, G.packBwd, G.biasPad, samples, n, static_cast<float>(1.0 / sum), cMax, grad, G.lossAcc, G.ctl + 1);
+    double la[2] = {0, 0};
+    int err = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(la, G.lossAcc, sizeof(la), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, G.ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cudaFail("guiding gradient", e);
+    if (err) {
+        setError("guiding gradient: tensor-core wait timed out");
+        return SPGPU_EKERNEL;
+    }
+    if (loss) *loss = la[0];
+    return 0;
+}
+
+int guideTrain(Ctx &C, GuideState &G, int steps, double *meanLoss) {
+    int written = 0;
+    cudaMemcpy(&written, G.ctl, sizeof(int), cudaMemcpyDeviceToHost);
+    const int avail = std::min(written, G.capacity);
+    if (avail <= 0) {
+        setError("spgpu_guiding_train: no training samples collected yet");
+        return SPGPU_ESTATE;
+    }
+    const int n = std::min(G.batchCap, avail);
+    std::vector<int> idx(n);
+    double lossSum = 0.0;
+    for (int st = 0; st < steps; st++) {
+        std::uniform_int_distribution<int> U(0, avail - 1);
+        for (int i = 0; i < n; i++) idx[i] = U(G.rng);
+        cudaMemcpyAsync(G.batchIdx, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, C.stream);
+        cudaMemsetAsync(G.wsum, 0, 2 * sizeof(float), C.stream);
+        k_gather<<<64, 256, 0, C.stream>>>(G.samples, G.batchIdx, n, G.batch, G.wsum);
+        double l = 0.0;
+        int rc = guideGrad(C, G, G.batch, n, nullptr, &l, C.stream, false);
+        if (rc) return rc;
+        lossSum += l;
+        G.step++;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.0f - std::pow(b1, static_cast<float>(G.step));
+        const float c2 = 1.0f - std::pow(b2, static_cast<float>(G.step));
+        k_adam<<<32, 256, 0, C.stream>>>(G.master, G.grad, G.m, G.v, kGParams, G.cfg.learning_rate, b1, b2, 1.0e-8f,
+                                         c1, c2);
+        rc = packWeights(G, C.stream);
+        if (rc) return rc;
+    }
+    cudaError_t e = cudaStreamSynchronize(C.stream);
+    if (e != cudaSuccess) return cudaFail("spgpu_guiding_train", e);
+    G.lastLoss = steps ? lossSum / steps : 0.0;
+    if (meanLoss) *meanLoss = G.lastLoss;
+    return 0;
+}
+
+int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film, int flags,
+                unsigned long long *statsOut, float *msOut, cudaStream_t s) {
+    const bool guided = (flags & 1) && G;
+    const bool collect = (flags & 2) && G;
+    GuidedArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.sv = C.view();
+    a.cam = makeCamera(d->camera, d->width, d->height);
+    a.W = d->width;
+    a.H = d->height;
+    a.npix = d->width * d->height;
+    a.total = static_cast<long long>(a.npix) * d->spp;
+    a.sampleOffset = d->sample_offset;
+    a.maxDepth = d->max_depth;
+    a.seed = d->seed;
+    a.film = film;
+    a.lo = C.bvh.lo;
+    const float3 ext = C.bvh.hi - C.bvh.lo;
+    a.invExt = mk(ext.x > 0 ? 1.0f / ext.x : 0.0f, ext.y > 0 ? 1.0f / ext.y : 0.0f, ext.z > 0 ? 1.0f / ext.z : 0.0f);
+    a.alpha = G ? G->cfg.bsdf_fraction : 1.0f;
+    unsigned long long *stats = nullptr;
+    int *ctl = nullptr;
+    if (G) {
+        a.packFwd = G->packFwd;
+        a.biasPad = G->biasPad;
+        a.ring = G->samples;
+        a.capacity = G->capacity;
+        ctl = G->ctl;
+    }
+    // plain runs without guiding state use the render queues' counters
+    static thread_local int *plainCtl = nullptr;
+    static thread_local unsigned long long *plainStats = nullptr;
+    if (!plainCtl) {
+        cudaMalloc(&plainCtl, 4 * sizeof(int));
+        cudaMalloc(&plainStats, 4 * sizeof(unsigned long long));
+    }
+    if (!ctl) ctl = plainCtl;
+    stats = plainStats;
+    a.ctl = ctl;
+    a.stats = stats;
+    cudaMemsetAsync(ctl + 1, 0, 3 * sizeof(int), s);
+    cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s);
+    int sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
+    if (!G) {
+        cudaFuncSetAttribute(k_guided<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
+    }
+    if (guided && collect) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<true, true>, kGTile, kGuidedSmem);
+    else if (guided) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<true, false>, kGTile, kGuidedSmem);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<false, false>, kGTile, kGuidedSmem);
+    // at most 8 TMEM allocations of 64 columns fit an SM's 512 columns
+    const int grid = sms * std::max(1, std::min(occ, 8));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    if (guided && collect) k_guided<true, true><<<grid, kGTile, kGuidedSmem, s>>>(a);
+    else if (guided) k_guided<true, false><<<grid, kGTile, kGuidedSmem, s>>>(a);
+    else k_guided<false, false><<<grid, kGTile, kGuidedSmem, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    cudaEventRecord(e1, s);
+    unsigned long long st[4] = {0, 0, 0, 0};
+    int err = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cudaFail("spgpu_guiding_render", e);
+    for (int k = 0; k < 3; k++) statsOut[k] = st[k];
+    *msOut = ms;
+    if (err) {
+        setError("spgpu_guiding_render: traversal overflow or tensor-core wait timed out");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
+}
+
+int guideSamples(const GuideState &G) {
+    int w = 0;
+    cudaMemcpy(&w, G.ctl, sizeof(int), cudaMemcpyDeviceToHost);
+    return w;
+}
+
+}  // namespace spgpu

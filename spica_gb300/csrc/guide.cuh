@@ -1,0 +1,200 @@
+// guide.cuh -- the learned path-guiding proposal: a 9 -> 64 -> 64 -> 64 -> 40 MLP
+// (BF16 weights, FP32 accumulation) mapping (position, normal, outgoing direction) at a
+// shading point to an 8-lobe von Mises-Fisher mixture over incident directions.
+// This part has no counterpart in the reference renderer.
+//
+// The dense layers run on the 5th-generation tensor cores: a CTA of 128 threads
+// evaluates a tile of 128 samples; each layer is tcgen05.mma (M = 128, N = 64 or 48,
+// K = 16 per instruction) from bf16 operands in shared memory into an FP32 accumulator
+// in tensor memory, whose epilogue (tcgen05.ld, bias, ReLU, bf16) writes the next
+// layer's operand back to shared memory.
+#pragma once
+
+#include "common.cuh"
+#include "tc.cuh"
+
+namespace spgpu {
+
+constexpr int kGIn = 9;      // inputs
+constexpr int kGK0 = 16;     // inputs padded to the MMA's K step
+constexpr int kGHid = 64;    // hidden width
+constexpr int kGOut = 40;    // outputs: 8 lobes x (direction 3, log-concentration, weight logit)
+constexpr int kGN4 = 48;     // outputs padded to a multiple of 16
+constexpr int kGLobes = 8;
+constexpr int kGTile = 128;  // samples per CTA tile (= MMA M)
+
+// fp32 master parameters, each layer [out][in] row-major followed by its bias
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kGHid * kGIn;
+constexpr int kOffW2 = kOffB1 + kGHid;
+constexpr int kOffB2 = kOffW2 + kGHid * kGHid;
+constexpr int kOffW3 = kOffB2 + kGHid;
+constexpr int kOffB3 = kOffW3 + kGHid * kGHid;
+constexpr int kOffW4 = kOffB3 + kGHid;
+constexpr int kOffB4 = kOffW4 + kGOut * kGHid;
+constexpr int kGParams = kOffB4 + kGOut;   // 11,560
+
+// packed bf16 MMA operands (canonical K-major tiles, tc.cuh):
+//   forward  B_l = W_l as [N = out][K = in]:  W1f 64x16 | W2f 64x64 | W3f 64x64 | W4f 48x64
+//   backward B_l = W_l^T as [N = in][K = out]:            W2b 64x64 | W3b 64x64 | W4b 64x48
+constexpr int kW1fBytes = kGHid * kGK0 * 2;
+constexpr int kW2fBytes = kGHid * kGHid * 2;
+constexpr int kW4fBytes = kGN4 * kGHid * 2;
+constexpr int kPackFwdBytes = kW1fBytes + 2 * kW2fBytes + kW4fBytes;   // 24,576
+constexpr int kW4bBytes = kGHid * kGN4 * 2;
+constexpr int kPackBwdBytes = 2 * kW2fBytes + kW4bBytes;               // 22,528
+constexpr int kBiasPad = 3 * kGHid + kGN4;                             // 240
+
+constexpr uint32_t kMmaWaitTries = 1u << 22;
+
+// ---------------------------------------------------------------- vMF mixture
+struct Mixture {
+    float3 mu[kGLobes];
+    float kappa[kGLobes];
+    float w[kGLobes];
+};
+
+__device__ __forceinline__ float vmfNorm(float kappa) {   // kappa / (2 pi (1 - exp(-2 kappa)))
+    return kappa / (2.0f * kPi * -expm1f(-2.0f * kappa));
+}
+__device__ __forceinline__ float vmfPdf(float3 w, float3 mu, float kappa) {
+    return vmfNorm(kappa) * __expf(kappa * (dot(mu, w) - 1.0f));
+}
+__device__ __forceinline__ float kappaOf(float raw) { return __expf(clampf(raw, -4.0f, 7.0f)); }
+
+// raw network outputs -> mixture (unit lobe axes, concentrations, softmax weights)
+__device__ __forceinline__ void mixtureFromRaw(const float *raw, Mixture &M) {
+    float mx = -3.0e38f;
+    for (int k = 0; k < kGLobes; k++) mx = fmaxf(mx, raw[5 * k + 4]);
+    float s = 0.0f;
+    for (int k = 0; k < kGLobes; k++) {
+        const float3 m = mk(raw[5 * k], raw[5 * k + 1], raw[5 * k + 2]);
+        const float len = sqrtf(dot(m, m));
+        M.mu[k] = len > 1.0e-12f ? m * (1.0f / len) : mk(0.0f, 0.0f, 1.0f);
+        M.kappa[k] = kappaOf(raw[5 * k + 3]);
+        M.w[k] = __expf(raw[5 * k + 4] - mx);
+        s += M.w[k];
+    }
+    for (int k = 0; k < kGLobes; k++) M.w[k] /= s;
+}
+__device__ __forceinline__ float mixturePdf(const Mixture &M, float3 w) {
+    float p = 0.0f;
+    for (int k = 0; k < kGLobes; k++) p += M.w[k] * vmfPdf(w, M.mu[k], M.kappa[k]);
+    return p;
+}
+// Sampling a vMF lobe with the numerically stable inversion of W. Jakob, "Numerically
+// stable sampling of the von Mises Fisher distribution on S^2 (and other tricks)" (2012).
+__device__ __forceinline__ float3 vmfSample(float3 mu, float kappa, float u1, float u2) {
+    const float e = __expf(-2.0f * kappa);
+    const float c = 1.0f + __logf(u1 + (1.0f - u1) * e) / kappa;
+    const float cc = clampf(c, -1.0f, 1.0f);
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - cc * cc));
+    float sp, cp;
+    __sincosf(2.0f * kPi * u2, &sp, &cp);
+    float3 t, b;
+    onb(mu, &t, &b);
+    return normalize(t * (s * cp) + b * (s * sp) + mu * cc);
+}
+__device__ __forceinline__ float3 mixtureSample(const Mixture &M, float uLobe, float u1, float u2) {
+    int k = 0;
+    float acc = M.w[0];
+    while (k < kGLobes - 1 && uLobe >= acc) {
+        k++;
+        acc += M.w[k];
+    }
+    return vmfSample(M.mu[k], M.kappa[k], u1, u2);
+}
+
+// network inputs: position normalised to the scene box, shading normal, outgoing dir
+__device__ __forceinline__ void guideFeatures(float3 p, float3 n, float3 wo, float3 lo, float3 invExt, float *x) {
+    x[0] = (p.x - lo.x) * invExt.x;
+    x[1] = (p.y - lo.y) * invExt.y;
+    x[2] = (p.z - lo.z) * invExt.z;
+    x[3] = n.x;
+    x[4] = n.y;
+    x[5] = n.z;
+    x[6] = wo.x;
+    x[7] = wo.y;
+    x[8] = wo.z;
+}
+
+// ---------------------------------------------------------------- tile MLP
+// write row r of a bf16 K-major canonical tile from 8 floats (one core-matrix row)
+__device__ __forceinline__ void storeRow8(uint8_t *tile, uint32_t r, uint32_t k0, uint32_t K, const float *v) {
+    __nv_bfloat162 p[4];
+    for (int i = 0; i < 4; i++) p[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    *reinterpret_cast<uint4 *>(tile + tc::kmajorOffset(r, k0, K)) = *reinterpret_cast<uint4 *>(p);
+}
+__device__ __forceinline__ float loadBf16(const uint8_t *tile, uint32_t r, uint32_t k, uint32_t K) {
+    return __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(tile + tc::kmajorOffset(r, k, K)));
+}
+
+// D = A x B over K (multiple of 16), issued by thread 0; returns once the tensor core
+// is done (all threads wait on the barrier).  Returns false on a timed-out wait (the
+// CTA-wide result is uniform).
+__device__ __forceinline__ bool tileMma(uint32_t tmem, const uint8_t *a, const uint8_t *b, uint32_t K, uint32_t N,
+                                        uint64_t *bar, uint32_t &phase) {
+    tc::fenceBeforeSync();
+    tc::fenceAsyncShared();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc::fenceAfterSync();
+        const uint32_t sbo = (K / 8) * 128;
+        const uint32_t idesc = tc::instrDescBf16(128, N);
+        const uint32_t aAddr = tc::smemAddr(a), bAddr = tc::smemAddr(b);
+        for (uint32_t j = 0; j < K / 16; j++)
+            tc::mmaBf16(tmem, tc::smemDesc(aAddr + 256 * j, 128, sbo), tc::smemDesc(bAddr + 256 * j, 128, sbo), idesc,
+                        j > 0 ? 1u : 0u);
+        tc::mmaCommit(bar);
+    }
+    const bool ok = tc::mbarWait(bar, phase, kMmaWaitTries);
+    phase ^= 1u;
+    const bool allOk = __syncthreads_and(ok) != 0;
+    tc::fenceAfterSync();
+    return allOk;
+}
+
+// this thread's row (its TMEM lane) of the accumulator, columns [c0, c0 + 16)
+__device__ __forceinline__ void accRow16(uint32_t tmem, uint32_t c0, float (&v)[16]) {
+    const uint32_t warp = threadIdx.x >> 5;
+    tc::tmemLoad16(tmem + ((warp * 32u) << 16) + c0, v);
+}
+
+// hidden-layer epilogue: relu(acc + bias) -> bf16 tile (K = 64); keeps fp32 copy if asked
+__device__ __forceinline__ void hiddenEpilogue(uint32_t tmem, const float *bias, uint8_t *out) {
+    const uint32_t r = threadIdx.x;
+    for (uint32_t c = 0; c < kGHid; c += 16) {
+        float v[16];
+        accRow16(tmem, c, v);
+        for (int i = 0; i < 16; i++) v[i] = fmaxf(v[i] + bias[c + i], 0.0f);
+        storeRow8(out, r, c, kGHid, v);
+        storeRow8(out, r, c + 8, kGHid, v + 8);
+    }
+}
+
+// Full forward of one tile: x (bf16 [128][16]) -> raw outputs (fp32, out[r * stride + j],
+// j < 40).  h1..h3 receive the hidden activations (may alias for inference).
+__device__ __forceinline__ bool mlpForwardTile(uint32_t tmem, const uint8_t *wf, const float *bias, const uint8_t *x,
+                                               uint8_t *h1, uint8_t *h2, uint8_t *h3, float *out, int stride,
+                                               uint64_t *bar, uint32_t &phase) {
+    const uint8_t *w1 = wf, *w2 = wf + kW1fBytes, *w3 = w2 + kW2fBytes, *w4 = w3 + kW2fBytes;
+    if (!tileMma(tmem, x, w1, kGK0, kGHid, bar, phase)) return false;
+    hiddenEpilogue(tmem, bias, h1);
+    if (!tileMma(tmem, h1, w2, kGHid, kGHid, bar, phase)) return false;
+    hiddenEpilogue(tmem, bias + kGHid, h2);
+    if (!tileMma(tmem, h2, w3, kGHid, kGHid, bar, phase)) return false;
+    hiddenEpilogue(tmem, bias + 2 * kGHid, h3);
+    if (!tileMma(tmem, h3, w4, kGHid, kGN4, bar, phase)) return false;
+    const uint32_t r = threadIdx.x;
+    for (uint32_t c = 0; c < kGN4; c += 16) {
+        float v[16];
+        accRow16(tmem, c, v);
+        for (int i = 0; i < 16; i++)
+            if (c + i < kGOut) out[r * stride + c + i] = v[i] + bias[3 * kGHid + c + i];
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    return true;
+}
+
+}  // namespace spgpu

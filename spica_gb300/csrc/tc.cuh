@@ -29,6 +29,7 @@ __host__ __device__ __forceinline__ uint32_t kmajorOffset(uint32_t r, uint32_t k
 // ---------------------------------------------------------------- mbarrier
 __device__ __forceinline__ void mbarInit(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");   // visible to the async proxy
 }
 __device__ __forceinline__ bool mbarTryWait(uint64_t *bar, uint32_t phase) {
     uint32_t ok;

@@ -70,6 +70,15 @@ class BatchTuning(C.Structure):
                 ("candidates", C.c_int32), ("calib_ms", C.c_double)]
 
 
+class GuidingConfig(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("bsdf_fraction", C.c_float), ("batch", C.c_int32),
+                ("seed", C.c_uint32), ("capacity", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+GUIDE_GUIDED, GUIDE_COLLECT = 1, 2
+GUIDE_PARAMS = 11560
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("reserved", C.c_int * 7)]
 
@@ -78,7 +87,9 @@ class Config(C.Structure):
 EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version", "spgpu_upload_scene",
            "spgpu_build_bvh", "spgpu_bvh_stats", "spgpu_trace", "spgpu_trace_host", "spgpu_trace_stats",
            "spgpu_render", "spgpu_render_host", "spgpu_render_profile", "spgpu_batch_prepare",
-           "spgpu_batch_film_pixels", "spgpu_batch_run"]
+           "spgpu_batch_film_pixels", "spgpu_batch_run", "spgpu_guiding_init", "spgpu_guiding_render",
+           "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_params", "spgpu_guiding_mlp",
+           "spgpu_guiding_grad"]
 
 _lib = None
 
@@ -110,10 +121,18 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_batch_prepare.argtypes = [vp, i32, C.POINTER(BatchItem), i32, C.POINTER(BatchTuning)]
     lib.spgpu_batch_film_pixels.argtypes = [vp]
     lib.spgpu_batch_run.argtypes = [vp, vp, vp, C.POINTER(RenderStats), vp]
+    lib.spgpu_guiding_init.argtypes = [vp, C.POINTER(GuidingConfig)]
+    lib.spgpu_guiding_render.argtypes = [vp, C.POINTER(RenderDesc), vp, i32, C.POINTER(RenderStats), vp]
+    lib.spgpu_guiding_train.argtypes = [vp, i32, C.POINTER(C.c_double)]
+    lib.spgpu_guiding_samples.argtypes = [vp]
+    lib.spgpu_guiding_params.argtypes = [vp, vp, i32]
+    lib.spgpu_guiding_mlp.argtypes = [vp, vp, i32, vp, vp]
+    lib.spgpu_guiding_grad.argtypes = [vp, vp, i32, vp, C.POINTER(C.c_double), vp]
     for name in EXPORTS:
         if name not in ("spgpu_destroy", "spgpu_last_error", "spgpu_version"):
             getattr(lib, name).restype = C.c_int
     lib.spgpu_batch_film_pixels.restype = C.c_int64
+    lib.spgpu_guiding_samples.restype = C.c_int64
     if path is None:
         _lib = lib
     return lib
@@ -335,3 +354,54 @@ class GpuBatch:
         sc = self.scenes[i]
         o = self.offsets[i]
         return films_host[o:o + sc.width * sc.height].reshape(sc.height, sc.width, 4)
+
+
+class GpuGuide:
+    """Learned guiding on a constructed accelerator's scene (spgpu_guiding_*)."""
+
+    def __init__(self, accel: GpuBVHAccel, lr: float = 1e-3, bsdf_fraction: float = 0.3, batch: int = 16384,
+                 seed: int = 0, capacity: int = 1 << 21):
+        self.accel = accel
+        self.ctx = accel.ctx
+        cfg = GuidingConfig(learning_rate=lr, bsdf_fraction=bsdf_fraction, batch=batch, seed=seed,
+                            capacity=capacity)
+        _check(self.ctx.lib.spgpu_guiding_init(self.ctx.h, C.byref(cfg)), "spgpu_guiding_init")
+
+    def params(self):
+        p = np.zeros(GUIDE_PARAMS, np.float32)
+        _check(self.ctx.lib.spgpu_guiding_params(self.ctx.h, p.ctypes.data, 0), "spgpu_guiding_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == GUIDE_PARAMS
+        _check(self.ctx.lib.spgpu_guiding_params(self.ctx.h, p.ctypes.data, 1), "spgpu_guiding_params")
+
+    def mlp(self, features_dev, raw_dev, stream: int = 0):
+        _check(self.ctx.lib.spgpu_guiding_mlp(self.ctx.h, _ptr(features_dev), features_dev.shape[0], _ptr(raw_dev),
+                                              C.c_void_p(stream) if stream else None), "spgpu_guiding_mlp")
+
+    def grad(self, samples_dev, grad_dev, stream: int = 0) -> float:
+        loss = C.c_double(0.0)
+        _check(self.ctx.lib.spgpu_guiding_grad(self.ctx.h, _ptr(samples_dev), samples_dev.shape[0], _ptr(grad_dev),
+                                               C.byref(loss), C.c_void_p(stream) if stream else None),
+               "spgpu_guiding_grad")
+        return loss.value
+
+    def render(self, camera, params: dict, film_dev, flags: int, seed: int = 0, sample_offset: int = 0,
+               stream: int = 0) -> RenderStats:
+        integ = GpuPathIntegrator(seed=seed)
+        d = integ.desc(camera, int(params["width"]), int(params["height"]), int(params["sampleCount"]),
+                       int(params.get("maxDepth", 12)), sample_offset)
+        st = RenderStats()
+        _check(self.ctx.lib.spgpu_guiding_render(self.ctx.h, C.byref(d), _ptr(film_dev), flags, C.byref(st),
+                                                 C.c_void_p(stream) if stream else None), "spgpu_guiding_render")
+        return st
+
+    def train(self, steps: int) -> float:
+        loss = C.c_double(0.0)
+        _check(self.ctx.lib.spgpu_guiding_train(self.ctx.h, steps, C.byref(loss)), "spgpu_guiding_train")
+        return loss.value
+
+    def samples(self) -> int:
+        return int(self.ctx.lib.spgpu_guiding_samples(self.ctx.h))

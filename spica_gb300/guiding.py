@@ -1,0 +1,63 @@
+"""Equal-time comparison of guided and plain rendering (the learned-guiding workload).
+
+relmse(I, R) = mean over pixels and channels of (I - R)^2 / (R^2 + 1e-2), against a
+high-sample plain reference R.  render_equal_time() spends the same device time on
+either method: the guided run trains online for the first `train_fraction` of it
+(collection passes + Adam steps), then renders with the trained proposal; only the
+samples of the rendering phase enter its image.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from .gpu import GUIDE_COLLECT, GUIDE_GUIDED, GpuBVHAccel, GpuGuide
+
+
+def relmse(img, ref):
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def _mean(film):
+    f = film.detach().cpu().numpy() if hasattr(film, "detach") else film
+    return f[..., :3] / np.maximum(f[..., 3:4], 1)
+
+
+def render_reference(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, spp, seed=777, chunk=256):
+    """Plain high-sample reference (same estimator, plain BSDF sampling)."""
+    film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    done = 0
+    while done < spp:
+        n = min(chunk, spp - done)
+        guide.render(scene.camera, {"width": W, "height": H, "sampleCount": n, "maxDepth": scene.max_depth}, film, 0,
+                     seed=seed, sample_offset=done)
+        done += n
+    torch.cuda.synchronize()
+    return _mean(film)
+
+
+def render_equal_time(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, budget_ms, guided: bool,
+                      train_fraction=0.25, train_steps=8, seed=1):
+    """Render for budget_ms of device time; returns (mean image, info)."""
+    p = {"width": W, "height": H, "maxDepth": scene.max_depth}
+    film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    spent, passes, trained, offset = 0.0, 0, 0, 0
+    if guided:
+        scratch = torch.zeros_like(film)
+        while spent < train_fraction * budget_ms:
+            st = guide.render(scene.camera, dict(p, sampleCount=1), scratch, GUIDE_GUIDED | GUIDE_COLLECT,
+                              seed=seed + 1000, sample_offset=offset)
+            offset += 1
+            t0 = time.perf_counter()
+            guide.train(train_steps)
+            torch.cuda.synchronize()
+            spent += st.ms + 1e3 * (time.perf_counter() - t0)
+            trained += train_steps
+    flags = GUIDE_GUIDED if guided else 0
+    while spent < budget_ms:
+        st = guide.render(scene.camera, dict(p, sampleCount=1), film, flags, seed=seed, sample_offset=passes)
+        spent += st.ms
+        passes += 1
+    torch.cuda.synchronize()
+    return _mean(film), {"ms": spent, "render_spp": passes, "adam_steps": trained, "training_passes": offset}

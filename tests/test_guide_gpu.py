@@ -1,0 +1,136 @@
+"""The guiding network on the tensor cores against its CPU oracle (forward and
+gradient), unbiasedness of the guided estimator, and its gain over plain sampling at
+equal device time on the indirect-lit room."""
+import numpy as np
+import pytest
+
+from oracle import guide_oracle as go
+from parity import zscores
+from spica_gb300 import GpuBVHAccel, GpuGuide, scenes
+from spica_gb300.gpu import GUIDE_COLLECT, GUIDE_GUIDED
+
+pytestmark = pytest.mark.gpu
+
+
+def _room(n_boxes=200, **kw):
+    return scenes.guiding_room(n_boxes=n_boxes, **kw)
+
+
+def _random_params(seed):
+    rng = np.random.default_rng(seed)
+    p = go.init_params(seed)
+    p[go.N_PARAMS - 40:] = (rng.normal(size=40) * 0.5).astype(np.float32)
+    for off, n in ((576, 64), (4736, 64), (8896, 64)):
+        p[off:off + n] = (rng.normal(size=n) * 0.1).astype(np.float32)
+    return p
+
+
+def test_mlp_forward_matches_oracle(gpulib):
+    import torch
+    acc = GpuBVHAccel(_room(10)).construct()
+    g = GpuGuide(acc, seed=3)
+    p = _random_params(5)
+    g.set_params(p)
+    assert np.array_equal(g.params(), p)
+    rng = np.random.default_rng(2)
+    n = 1000   # not a multiple of the 128-sample tile
+    x = rng.random((n, 9)).astype(np.float32)
+    x[:, 3:] = x[:, 3:] * 2 - 1
+    out = torch.zeros((n, 40), dtype=torch.float32, device="cuda")
+    g.mlp(torch.from_numpy(x).cuda(), out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    want, _ = go.forward(p, x, emulate_bf16=True)
+    scale = np.abs(want).max()
+    assert np.abs(got - want).max() <= 2e-2 * scale, np.abs(got - want).max() / scale
+
+
+def test_gradient_matches_oracle(gpulib):
+    import torch
+    acc = GpuBVHAccel(_room(10)).construct()
+    g = GpuGuide(acc, seed=3)
+    p = _random_params(7)
+    g.set_params(p)
+    rng = np.random.default_rng(3)
+    n = 700
+    S = np.zeros((n, 16), np.float32)
+    S[:, :9] = rng.random((n, 9))
+    S[:, 3:9] = S[:, 3:9] * 2 - 1
+    w = rng.normal(size=(n, 3))
+    S[:, 9:12] = w / np.linalg.norm(w, axis=1, keepdims=True)
+    S[:, 12] = rng.random(n) + 0.05
+    grad = torch.zeros(go.N_PARAMS, dtype=torch.float32, device="cuda")
+    loss = g.grad(torch.from_numpy(S).cuda(), grad)
+    gg = grad.cpu().numpy().astype(np.float64)
+    want = go.grad(p, S[:, :9], S[:, 9:12], S[:, 12], emulate_bf16=True)
+    cos = gg @ want / (np.linalg.norm(gg) * np.linalg.norm(want))
+    assert cos > 0.995, cos
+    assert abs(np.linalg.norm(gg) / np.linalg.norm(want) - 1) < 0.03
+    ref_loss = go.loss(p, S[:, :9], S[:, 9:12], S[:, 12], emulate_bf16=True)
+    assert abs(loss - ref_loss) <= 0.02 * abs(ref_loss) + 1e-3, (loss, ref_loss)
+
+
+def test_training_reduces_loss_and_guided_render_is_unbiased(gpulib):
+    import torch
+    sc = _room(60)
+    W, H = 64, 36
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=1, batch=8192)
+    p = {"width": W, "height": H, "maxDepth": sc.max_depth}
+    scratch = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    losses = []
+    for k in range(12):
+        g.render(sc.camera, dict(p, sampleCount=4), scratch, GUIDE_GUIDED | GUIDE_COLLECT, seed=50, sample_offset=4 * k)
+        losses.append(g.train(10))
+    assert g.samples() > 0
+    assert np.mean(losses[-3:]) < np.mean(losses[:3]), losses
+    # guided and plain estimates agree per pixel (batch means, 16 x 128 spp each)
+    means = {}
+    for flags in (0, GUIDE_GUIDED):
+        ms = []
+        for b in range(16):
+            f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+            g.render(sc.camera, dict(p, sampleCount=128), f, flags, seed=9 + flags, sample_offset=128 * b)
+            fh = f.cpu().numpy()
+            ms.append(fh[..., :3] / fh[..., 3:])
+        m = np.stack(ms)
+        means[flags] = (m.mean(0), m.var(0, ddof=1) / 16)
+    z = zscores(means[0][0], means[0][1], means[GUIDE_GUIDED][0], means[GUIDE_GUIDED][1])
+    assert (np.abs(z) > 3).mean() < 0.02, ((np.abs(z) > 3).mean(), np.abs(z).max())
+
+
+def test_plain_megakernel_matches_wavefront(gpulib):
+    """flags 0 is the same estimator as spgpu_render: same film from the same streams."""
+    import torch
+    from spica_gb300 import GpuPathIntegrator
+    sc = _room(20)
+    W, H = 48, 32
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=1)
+    f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    g.render(sc.camera, {"width": W, "height": H, "sampleCount": 16, "maxDepth": sc.max_depth}, f, 0, seed=4)
+    ref = GpuPathIntegrator(seed=4).render(sc.camera, acc, {"width": W, "height": H, "sampleCount": 16,
+                                                            "maxDepth": sc.max_depth})
+    got = f.cpu().numpy()
+    assert np.array_equal(got[..., 3], ref[..., 3])
+    np.testing.assert_allclose(got[..., :3], ref[..., :3], rtol=2e-3, atol=2e-3)
+
+
+def test_guided_beats_plain_at_equal_time(gpulib):
+    """Indirect-lit room: relMSE against a high-sample plain reference, same device time."""
+    import torch
+    from spica_gb300 import guiding
+    sc = _room()
+    W, H = 160, 90
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=2)
+    ref = guiding.render_reference(torch, acc, g, sc, W, H, spp=16384)
+    # budget: the time of 256 plain samples per pixel
+    f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    st = g.render(sc.camera, {"width": W, "height": H, "sampleCount": 256, "maxDepth": sc.max_depth}, f, 0, seed=3)
+    budget = st.ms
+    plain, pi = guiding.render_equal_time(torch, acc, g, sc, W, H, budget, guided=False, seed=11)
+    guided, gi = guiding.render_equal_time(torch, acc, g, sc, W, H, budget, guided=True, seed=11)
+    e_plain, e_guided = guiding.relmse(plain, ref), guiding.relmse(guided, ref)
+    print({"relmse_plain": e_plain, "relmse_guided": e_guided, "plain": pi, "guided": gi})
+    assert e_guided * 2.0 <= e_plain, (e_plain, e_guided, pi, gi)
