@@ -240,6 +240,32 @@ def batch_bench(torch, GpuBatch, scenes, reps=3):
             "prepare_s": prep_s}
 
 
+def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=512, ref_spp=4096):
+    """Learned guiding on the indirect-lit room: relMSE against a plain reference at
+    equal device time (the time of budget_spp plain samples per pixel), the guided run
+    training online for the first 25% of it; plus the same comparison at equal samples."""
+    from spica_gb300 import guiding
+    from spica_gb300.gpu import GpuGuide
+    sc = scenes.guiding_room(width=W, height=H)
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=2)
+    ref = guiding.render_reference(torch, acc, g, sc, W, H, spp=ref_spp)
+    f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    p = {"width": W, "height": H, "sampleCount": 8, "maxDepth": sc.max_depth}
+    ms8 = min(g.render(sc.camera, p, f, 0, seed=3).ms for _ in range(3))
+    budget = ms8 / 8 * budget_spp
+    plain, pi = guiding.render_equal_time(torch, acc, g, sc, W, H, budget, guided=False, seed=11)
+    gg = GpuGuide(acc, seed=2)
+    img, gi = guiding.render_equal_time(torch, acc, gg, sc, W, H, budget, guided=True, seed=11, train_steps=64)
+    e_p, e_g = guiding.relmse(plain, ref), guiding.relmse(img, ref)
+    return {"scene": "indirect-lit room, 2418 tris", "width": W, "height": H, "reference_spp": ref_spp,
+            "budget_ms": budget, "relmse_plain": e_p, "relmse_guided": e_g, "equal_time_gain": e_p / e_g,
+            "per_sample_gain": e_p * pi["render_spp"] / (e_g * gi["render_spp"]),
+            "plain_spp": pi["render_spp"], "guided_spp": gi["render_spp"], "adam_steps": gi["adam_steps"],
+            "training_spp": gi["training_spp"], "train_fraction": 0.25,
+            "plain_ms_per_spp": ms8 / 8}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -250,6 +276,7 @@ def main():
     ap.add_argument("--no-micro", action="store_true", help="skip the intersection microbench")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-renders measurement")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-API measurement")
+    ap.add_argument("--no-guiding", action="store_true", help="skip the learned-guiding comparison")
     ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel profile (roofline)")
     ap.add_argument("--width", type=int, default=1920, help="film width (profiling cases only)")
     ap.add_argument("--height", type=int, default=1080, help="film height (profiling cases only)")
@@ -369,6 +396,8 @@ def main():
         line["microbench"] = microbench(torch, GpuBVHAccel, scenes)
     if not args.no_batch:
         line["batch"] = batch_bench(torch, GpuBatch, scenes)
+    if not args.no_guiding:
+        line["guiding"] = guiding_bench(torch, GpuBVHAccel, scenes)
     if not args.no_cpu and ws == 1:
         v, kind, cores, desc, build_s = cpu_sample(scene)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc,

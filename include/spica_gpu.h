@@ -204,13 +204,17 @@ int spgpu_guiding_init(spgpu_ctx *ctx, const spgpu_guiding_config *cfg);
 int spgpu_guiding_render(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, int32_t flags,
                          spgpu_render_stats *stats, void *stream);
 int spgpu_guiding_train(spgpu_ctx *ctx, int32_t steps, double *mean_loss);
-int64_t spgpu_guiding_samples(spgpu_ctx *ctx);   /* training samples recorded so far */
+int64_t spgpu_guiding_samples(spgpu_ctx *ctx);   /* training samples recorded so far (mod 2^32) */
+/* copy up to max_samples entries of the training ring (host, 16 floats each: features 9,
+ * direction 3, weight c, proposal pdf q, 2 unused) into dst; *count = entries copied */
+int spgpu_guiding_ring(spgpu_ctx *ctx, float *dst, int32_t max_samples, int32_t *count);
 /* parameters, fp32: each layer's weights [out][in] row-major then its bias */
 int spgpu_guiding_params(spgpu_ctx *ctx, float *params, int32_t set);
 /* network outputs for n feature rows (device: features n*9, raw n*40) */
 int spgpu_guiding_mlp(spgpu_ctx *ctx, const float *features, int32_t n, float *raw, void *stream);
 /* gradient of the training loss sum_i c_i (-log q(w_i)) / sum_i c_i for n samples of 16
- * floats (features 9, direction 3, weight c, 3 unused) (device; grad: 11560 floats) */
+ * floats laid out as the ring's (only features, direction and c are read) (device;
+ * grad: 11560 floats) */
 int spgpu_guiding_grad(spgpu_ctx *ctx, const float *samples, int32_t n, float *grad, double *loss, void *stream);
 
 /* Profiling (no counterpart in the reference, which has only a progress printf,

@@ -823,6 +823,15 @@ int spgpu_guiding_train(spgpu_ctx *h, int32_t steps, double *mean_loss) {
 
 int64_t spgpu_guiding_samples(spgpu_ctx *h) { return h && h->c.guide ? guideSamples(*h->c.guide) : -1; }
 
+int spgpu_guiding_ring(spgpu_ctx *h, float *dst, int32_t max_samples, int32_t *count) {
+    if (!h || !h->c.guide || max_samples < 0 || (max_samples > 0 && !dst) || !count) {
+        setError("spgpu_guiding_ring: invalid arguments or no guiding state");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(h->c.device);
+    return guideRing(*h->c.guide, dst, max_samples, count);
+}
+
 int spgpu_guiding_params(spgpu_ctx *h, float *params, int32_t set) {
     if (!h || !params || !h->c.guide) {
         setError("spgpu_guiding_params: invalid arguments or no guiding state");

@@ -165,7 +165,8 @@ int guideForward(Ctx &C, GuideState &G, const float *feat, int n, float *out, cu
 int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s,
               bool accumulateOnly);
 int guideTrain(Ctx &C, GuideState &G, int steps, double *meanLoss);
+int guideRing(const GuideState &G, float *dst, int maxSamples, int *count);
 int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film, int flags,
                 unsigned long long *statsOut, float *msOut, cudaStream_t s);
-int guideSamples(const GuideState &G);
+long long guideSamples(const GuideState &G);
 }  // namespace spgpu

@@ -28,13 +28,12 @@ struct GuideState {
     int *ctl = nullptr;         // [0] samples written (monotonic), [1] error, [2] work counter
     double *lossAcc = nullptr;  // [0] loss sum, [1] weight sum
     float *wsum = nullptr;      // batch weight sum / max
-    int *batchIdx = nullptr;
     float *batch = nullptr;
     int batchCap = 0;
     int step = 0;
     spgpu_guiding_config cfg{};
     double lastLoss = 0.0;
-    std::mt19937 rng;
+    std::mt19937 rng;   // weight initialisation
 };
 
 namespace {
@@ -169,8 +168,9 @@ __device__ __forceinline__ void backEpilogue(uint32_t tmem, const uint8_t *h, fl
 __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__restrict__ packFwd,
                                                            const uint8_t *__restrict__ packBwd,
                                                            const float *__restrict__ biasPad,
-                                                           const float *__restrict__ samples, int n, float cScale,
-                                                           float cMax, float *grad, double *lossAcc, int *err) {
+                                                           const float *__restrict__ samples, int n,
+                                                           const float *__restrict__ wsum, float *grad,
+                                                           double *lossAcc, int *err) {
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t *wf = sm + TrainLayout::wf, *wb = sm + TrainLayout::wb;
     float *bias = reinterpret_cast<float *>(sm + TrainLayout::bias);
@@ -181,6 +181,11 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + TrainLayout::bar);
     uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + TrainLayout::tmem);
     const int t = threadIdx.x;
+    // c is normalised by the batch's weight sum and clamped at 1000x its mean (rare,
+    // bright indirect paths are the signal; only extreme outliers are cut)
+    const float cSum = wsum[0];
+    const float cScale = cSum > 0.0f ? 1.0f / cSum : 0.0f;
+    const float cMax = 1000.0f * cSum / static_cast<float>(n);
     for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
         reinterpret_cast<uint4 *>(wf)[i] = reinterpret_cast<const uint4 *>(packFwd)[i];
     for (int i = t; i < kPackBwdBytes / 16; i += kGTile)
@@ -325,14 +330,34 @@ __global__ void k_adam(float *P, float *G, float *M, float *V, int n, float lr, 
     }
 }
 
-// gather a random batch from the ring and its weight statistics
-__global__ void k_gather(const float *ring, const int *idx, int n, float *batch, float *wsum) {
+// gather a random batch of n samples from the first `avail` ring entries (indices from
+// Philox keyed by (seed, step)) and sum their weights
+__global__ void k_gather(const float *ring, int avail, uint32_t seed, uint32_t step, int n, float *batch,
+                         float *wsum) {
+    float part = 0.0f;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-        const float4 *src = reinterpret_cast<const float4 *>(ring + 16 * static_cast<int64_t>(idx[s]));
+        const uint4 r = philox4x32_10(make_uint4(static_cast<uint32_t>(s), step, 0x47415448u, 0u), make_uint2(seed, 0u));
+        const int idx = static_cast<int>(__umulhi(r.x, static_cast<uint32_t>(avail)));
+        const float4 *src = reinterpret_cast<const float4 *>(ring + 16 * static_cast<int64_t>(idx));
         float4 *dst = reinterpret_cast<float4 *>(batch + 16 * static_cast<int64_t>(s));
-        for (int k = 0; k < 4; k++) dst[k] = src[k];
-        atomicAdd(&wsum[0], batch[16 * static_cast<int64_t>(s) + 12]);
+        const float4 q0 = src[0], q1 = src[1], q2 = src[2], q3 = src[3];
+        dst[0] = q0;
+        dst[1] = q1;
+        dst[2] = q2;
+        dst[3] = q3;
+        part += q3.x;   // element 12: the weight c
     }
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0 && part != 0.0f) atomicAdd(&wsum[0], part);
+}
+
+// weight sum of a caller-supplied batch
+__global__ void k_csum(const float *samples, int n, float *wsum) {
+    float part = 0.0f;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        part += samples[16 * static_cast<int64_t>(s) + 12];
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0 && part != 0.0f) atomicAdd(&wsum[0], part);
 }
 
 // ------------------------------------------------------------------ guided tracer
@@ -364,6 +389,7 @@ struct GuidedArgs {
 
 constexpr int kGuidedSmem = kPackFwdBytes + kBiasPad * 4 + kGTile * kGK0 * 2 + kGTile * kGHid * 2 +
                             kGTile * 41 * 4 + kStackShared * kGTile * 8 + 16;
+constexpr int kPlainSmem = kStackShared * kGTile * 8;
 constexpr int kMaxRec = 13;
 
 __device__ __forceinline__ float lum(float3 c) { return gray(c); }
@@ -404,7 +430,9 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
     uint8_t *x = sm + kPackFwdBytes + kBiasPad * 4;
     uint8_t *h = x + kGTile * kGK0 * 2;
     float *out = reinterpret_cast<float *>(h + kGTile * kGHid * 2);
-    uint2 *stack = reinterpret_cast<uint2 *>(reinterpret_cast<uint8_t *>(out) + kGTile * 41 * 4);
+    // the plain kernel keeps only the traversal stacks in shared memory
+    uint2 *stack = GUIDED ? reinterpret_cast<uint2 *>(reinterpret_cast<uint8_t *>(out) + kGTile * 41 * 4)
+                          : reinterpret_cast<uint2 *>(sm);
     uint64_t *bar = reinterpret_cast<uint64_t *>(stack + kStackShared * kGTile);
     uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
     const int t = threadIdx.x;
@@ -435,6 +463,7 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
     bool spec = false;
     TrainRec rec[COLLECT ? kMaxRec : 1];
     int nrec = 0;
+    bool recLast = false;   // the current ray is the direction of rec[nrec - 1]
     while (true) {
         // ---- start new paths in idle lanes
         const bool want = !active && !exhausted;
@@ -459,6 +488,7 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
                     spec = false;
                     b = 0;
                     nrec = 0;
+                    recLast = false;
                     active = true;
                 } else {
                     exhausted = true;
@@ -489,7 +519,11 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
             if (!hit) {
                 const float3 Le = S.hasEnv ? envLe(S.env, d) : mk(0, 0, 0);
                 if (b == 0 || spec) L = L + beta * Le;
-                if (COLLECT && nrec > 0) rec[nrec - 1].E = Le;   // direct radiance along the last sampled dir
+                // direct radiance along the last guided direction, times the MIS weight of the
+                // guided strategy against light sampling: the share of it that guided samples
+                // estimate (a sun that light sampling finds is not worth learning)
+                if (COLLECT && recLast && S.hasEnv)
+                    rec[nrec - 1].E = Le * powerHeuristic(rec[nrec - 1].q, envPdf(S.env, d));
                 ends = true;
             } else {
                 const TriRecord tr = S.tris[hr.prim];
@@ -498,7 +532,11 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
                 m = S.mats[sh.x];
                 lightOf = sh.y;
                 ps = o + d * hr.t;
-                if (COLLECT && nrec > 0 && lightOf >= 0 && dot(n, -d) > 0.0f) rec[nrec - 1].E = xyz(S.lights[lightOf].L);
+                if (COLLECT && recLast && lightOf >= 0 && dot(n, -d) > 0.0f) {
+                    const LightRecord &Lr = S.lights[lightOf];
+                    const float lp = hr.t * hr.t / (dot(n, -d) * Lr.p0.w);
+                    rec[nrec - 1].E = xyz(Lr.L) * powerHeuristic(rec[nrec - 1].q, lp);
+                }
                 if (b >= a.maxDepth) {
                     if ((b == 0 || spec) && lightOf >= 0 && dot(n, -d) > 0.0f) L = L + beta * xyz(S.lights[lightOf].L);
                     ends = true;
@@ -523,6 +561,7 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
             ShadeResult R;
             if (!guideMe || !mmaOk) {
                 shadeHit(S, hr, o, d, beta, spec, b, a.maxDepth, a.seed, static_cast<uint32_t>(fi), sample, fi, R);
+                recLast = false;
             } else {
                 // the wavefront's shadeHit for a Lambert hit, with the BSDF strategy replaced
                 // by the mixture proposal (NEE weights use its pdf too)
@@ -628,6 +667,7 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
                 float pdf;
                 R.beta = beta;
                 R.spec = false;
+                if (COLLECT) recLast = false;
                 if (P.sample(m, woL, tg, bg, n, r2.c, r2.d, r1.b, r1.c, &wi, &f, &pdf) && !isBlack(f)) {
                     const float3 fc = f * fabsf(dot(wi, n));
                     R.beta = beta * fc * (1.0f / pdf);
@@ -649,6 +689,7 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
                             T.fcos = fc;
                             T.beta = R.beta;
                             T.E = mk(0, 0, 0);
+                            recLast = true;
                         }
                     }
                 }
@@ -697,13 +738,15 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
                     Li.z += T.beta.z > 0.0f ? rest.z / T.beta.z : 0.0f;
                     const float c = lum(T.fcos * Li) / T.q;
                     if (!(c > 0.0f) || !isfinite(c)) continue;
-                    const int slotIdx = atomicAdd(&a.ctl[0], 1) % a.capacity;
+                    const unsigned slotIdx =
+                        atomicAdd(reinterpret_cast<unsigned *>(&a.ctl[0]), 1u) % static_cast<unsigned>(a.capacity);
                     float *D = a.ring + 16 * static_cast<int64_t>(slotIdx);
                     for (int i = 0; i < kGIn; i++) D[i] = T.x[i];
                     D[9] = T.w.x;
                     D[10] = T.w.y;
                     D[11] = T.w.z;
                     D[12] = c;
+                    D[13] = T.q;
                 }
             }
             active = false;
@@ -747,7 +790,6 @@ void freeGuide(GuideState *G) {
     cudaFree(G->ctl);
     cudaFree(G->lossAcc);
     cudaFree(G->wsum);
-    cudaFree(G->batchIdx);
     cudaFree(G->batch);
     delete G;
 }
@@ -775,10 +817,9 @@ int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg) {
     G->ctl = galloc<int>(4);
     G->lossAcc = galloc<double>(2);
     G->wsum = galloc<float>(2);
-    G->batchIdx = galloc<int>(G->batchCap);
     G->batch = galloc<float>(static_cast<size_t>(G->batchCap) * 16);
     if (!G->master || !G->grad || !G->m || !G->v || !G->packFwd || !G->packBwd || !G->biasPad || !G->samples ||
-        !G->ctl || !G->lossAcc || !G->wsum || !G->batchIdx || !G->batch) {
+        !G->ctl || !G->lossAcc || !G->wsum || !G->batch) {
         freeGuide(G);
         setError("spgpu_guiding_init: device allocation failed");
         return SPGPU_ENOMEM;
@@ -813,7 +854,6 @@ int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg) {
         cudaFuncSetAttribute(k_guide_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kForwardSmem);
         cudaFuncSetAttribute(k_guided<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
         cudaFuncSetAttribute(k_guided<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
-        cudaFuncSetAttribute(k_guided<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
         attrsSet = true;
     }
     *slot = G;
@@ -852,81 +892,97 @@ int guideForward(Ctx &C, GuideState &G, const float *feat, int n, float *out, cu
     return 0;
 }
 
-// gradient of the batch loss (mean of c_i * -log p(w_i), c normalised by its sum)
-int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s,
-              bool accumulateOnly) {
-    if (n <= 0) return 0;
-    // weight sum for normalisation
-    cudaMemsetAsync(G.wsum, 0, 2 * sizeof(float), s);
-    cudaMemsetAsync(G.lossAcc, 0, 2 * sizeof(double), s);
-    cudaMemsetAsync(G.ctl + 1, 0, sizeof(int), s);
-    std::vector<float> hs(1);
-    // sum of c over the batch (host round trip is fine: a few KB per step)
-    std::vector<float> cs(static_cast<size_t>(n));
-    cudaMemcpy2DAsync(cs.data(), sizeof(float), samples + 12, 16 * sizeof(float), sizeof(float), n,
-                      cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    double sum = 0.0;
-    for (float c : cs) sum += c;
-    if (!(sum > 0.0)) {
-        if (loss) *loss = 0.0;
-        return 0;
-    }
-    const float cMax = static_cast<float>(50.0 * sum / n);
+// Launch the gradient of the batch loss (sum_i c_i * -log p(w_i), c normalised by the
+// batch's weight sum in G.wsum[0]) into grad; the c-weighted loss is added to
+// G.lossAcc[0].  No host synchronisation.
+static int launchGrad(Ctx &C, GuideState &G, const float *samples, int n, float *grad, cudaStream_t s) {
     const int tiles = (n + kGTile - 1) / kGTile;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
-    float *grad = gradOut ? gradOut : G.grad;
-    if (gradOut && !accumulateOnly) cudaMemsetAsync(gradOut, 0, sizeof(float) * kGParams, s);
-    k_guide_train<<<std::min(tiles, sms), kGTile, TrainLayout::total, s>>>(
-        G.packFwd, G.packBwd, G.biasPad, samples, n, static_cast<float>(1.0 / sum), cMax, grad, G.lossAcc, G.ctl + 1);
+    k_guide_train<<<std::min(tiles, sms), kGTile, TrainLayout::total, s>>>(G.packFwd, G.packBwd, G.biasPad, samples,
+                                                                           n, G.wsum, grad, G.lossAcc, G.ctl + 1);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : cudaFail("guiding gradient", e);
+}
+
+static int readLoss(GuideState &G, double *loss, cudaStream_t s, const char *what) {
     double la[2] = {0, 0};
     int err = 0;
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(la, G.lossAcc, sizeof(la), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaMemcpyAsync(la, G.lossAcc, sizeof(la), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&err, G.ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cudaFail("guiding gradient", e);
+    if (e != cudaSuccess) return cudaFail(what, e);
     if (err) {
-        setError("guiding gradient: tensor-core wait timed out");
+        setError(std::string(what) + ": tensor-core wait timed out");
         return SPGPU_EKERNEL;
     }
     if (loss) *loss = la[0];
     return 0;
 }
 
+int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s,
+              bool accumulateOnly) {
+    if (n <= 0) {
+        if (loss) *loss = 0.0;
+        return 0;
+    }
+    cudaMemsetAsync(G.wsum, 0, 2 * sizeof(float), s);
+    cudaMemsetAsync(G.lossAcc, 0, 2 * sizeof(double), s);
+    cudaMemsetAsync(G.ctl + 1, 0, sizeof(int), s);
+    k_csum<<<64, 256, 0, s>>>(samples, n, G.wsum);
+    float *grad = gradOut ? gradOut : G.grad;
+    if (gradOut && !accumulateOnly) cudaMemsetAsync(gradOut, 0, sizeof(float) * kGParams, s);
+    const int rc = launchGrad(C, G, samples, n, grad, s);
+    return rc ? rc : readLoss(G, loss, s, "spgpu_guiding_grad");
+}
+
+// ring entries holding samples: the write counter wraps as an unsigned 32-bit value
+static int ringAvail(const GuideState &G) {
+    unsigned written = 0;
+    cudaMemcpy(&written, G.ctl, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    return static_cast<int>(std::min<unsigned>(written, static_cast<unsigned>(G.capacity)));
+}
+
+int guideRing(const GuideState &G, float *dst, int maxSamples, int *count) {
+    const int n = std::min(ringAvail(G), maxSamples);
+    *count = 0;
+    if (n > 0) {
+        const cudaError_t e = cudaMemcpy(dst, G.samples, sizeof(float) * 16 * static_cast<size_t>(n),
+                                         cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cudaFail("spgpu_guiding_ring", e);
+    }
+    *count = n;
+    return 0;
+}
+
 int guideTrain(Ctx &C, GuideState &G, int steps, double *meanLoss) {
-    int written = 0;
-    cudaMemcpy(&written, G.ctl, sizeof(int), cudaMemcpyDeviceToHost);
-    const int avail = std::min(written, G.capacity);
+    const int avail = ringAvail(G);
     if (avail <= 0) {
         setError("spgpu_guiding_train: no training samples collected yet");
         return SPGPU_ESTATE;
     }
     const int n = std::min(G.batchCap, avail);
-    std::vector<int> idx(n);
-    double lossSum = 0.0;
+    cudaStream_t s = C.stream;
+    cudaMemsetAsync(G.lossAcc, 0, 2 * sizeof(double), s);
+    cudaMemsetAsync(G.ctl + 1, 0, sizeof(int), s);
     for (int st = 0; st < steps; st++) {
-        std::uniform_int_distribution<int> U(0, avail - 1);
-        for (int i = 0; i < n; i++) idx[i] = U(G.rng);
-        cudaMemcpyAsync(G.batchIdx, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, C.stream);
-        cudaMemsetAsync(G.wsum, 0, 2 * sizeof(float), C.stream);
-        k_gather<<<64, 256, 0, C.stream>>>(G.samples, G.batchIdx, n, G.batch, G.wsum);
-        double l = 0.0;
-        int rc = guideGrad(C, G, G.batch, n, nullptr, &l, C.stream, false);
+        cudaMemsetAsync(G.wsum, 0, 2 * sizeof(float), s);
+        k_gather<<<std::min(64, (n + 255) / 256), 256, 0, s>>>(G.samples, avail, G.cfg.seed,
+                                                                static_cast<uint32_t>(G.step), n, G.batch, G.wsum);
+        int rc = launchGrad(C, G, G.batch, n, G.grad, s);
         if (rc) return rc;
-        lossSum += l;
         G.step++;
         const float b1 = 0.9f, b2 = 0.999f;
         const float c1 = 1.0f - std::pow(b1, static_cast<float>(G.step));
         const float c2 = 1.0f - std::pow(b2, static_cast<float>(G.step));
-        k_adam<<<32, 256, 0, C.stream>>>(G.master, G.grad, G.m, G.v, kGParams, G.cfg.learning_rate, b1, b2, 1.0e-8f,
-                                         c1, c2);
-        rc = packWeights(G, C.stream);
+        k_adam<<<32, 256, 0, s>>>(G.master, G.grad, G.m, G.v, kGParams, G.cfg.learning_rate, b1, b2, 1.0e-8f, c1,
+                                  c2);
+        rc = packWeights(G, s);
         if (rc) return rc;
     }
-    cudaError_t e = cudaStreamSynchronize(C.stream);
-    if (e != cudaSuccess) return cudaFail("spgpu_guiding_train", e);
+    double lossSum = 0.0;
+    const int rc = readLoss(G, &lossSum, s, "spgpu_guiding_train");
+    if (rc) return rc;
     G.lastLoss = steps ? lossSum / steps : 0.0;
     if (meanLoss) *meanLoss = G.lastLoss;
     return 0;
@@ -976,21 +1032,18 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
     cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s);
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
-    if (!G) {
-        cudaFuncSetAttribute(k_guided<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
-    }
     if (guided && collect) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<true, true>, kGTile, kGuidedSmem);
     else if (guided) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<true, false>, kGTile, kGuidedSmem);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<false, false>, kGTile, kGuidedSmem);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<false, false>, kGTile, kPlainSmem);
     // at most 8 TMEM allocations of 64 columns fit an SM's 512 columns
-    const int grid = sms * std::max(1, std::min(occ, 8));
+    const int grid = sms * std::max(1, guided ? std::min(occ, 8) : occ);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
     if (guided && collect) k_guided<true, true><<<grid, kGTile, kGuidedSmem, s>>>(a);
     else if (guided) k_guided<true, false><<<grid, kGTile, kGuidedSmem, s>>>(a);
-    else k_guided<false, false><<<grid, kGTile, kGuidedSmem, s>>>(a);
+    else k_guided<false, false><<<grid, kGTile, kPlainSmem, s>>>(a);
     cudaError_t e = cudaGetLastError();
     cudaEventRecord(e1, s);
     unsigned long long st[4] = {0, 0, 0, 0};
@@ -1012,10 +1065,10 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
     return 0;
 }
 
-int guideSamples(const GuideState &G) {
-    int w = 0;
-    cudaMemcpy(&w, G.ctl, sizeof(int), cudaMemcpyDeviceToHost);
-    return w;
+long long guideSamples(const GuideState &G) {
+    unsigned written = 0;
+    cudaMemcpy(&written, G.ctl, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    return written;
 }
 
 }  // namespace spgpu

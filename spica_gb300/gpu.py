@@ -88,7 +88,7 @@ EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version",
            "spgpu_build_bvh", "spgpu_bvh_stats", "spgpu_trace", "spgpu_trace_host", "spgpu_trace_stats",
            "spgpu_render", "spgpu_render_host", "spgpu_render_profile", "spgpu_batch_prepare",
            "spgpu_batch_film_pixels", "spgpu_batch_run", "spgpu_guiding_init", "spgpu_guiding_render",
-           "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_params", "spgpu_guiding_mlp",
+           "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_ring", "spgpu_guiding_params", "spgpu_guiding_mlp",
            "spgpu_guiding_grad"]
 
 _lib = None
@@ -125,6 +125,7 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_guiding_render.argtypes = [vp, C.POINTER(RenderDesc), vp, i32, C.POINTER(RenderStats), vp]
     lib.spgpu_guiding_train.argtypes = [vp, i32, C.POINTER(C.c_double)]
     lib.spgpu_guiding_samples.argtypes = [vp]
+    lib.spgpu_guiding_ring.argtypes = [vp, vp, i32, C.POINTER(i32)]
     lib.spgpu_guiding_params.argtypes = [vp, vp, i32]
     lib.spgpu_guiding_mlp.argtypes = [vp, vp, i32, vp, vp]
     lib.spgpu_guiding_grad.argtypes = [vp, vp, i32, vp, C.POINTER(C.c_double), vp]
@@ -405,3 +406,11 @@ class GpuGuide:
 
     def samples(self) -> int:
         return int(self.ctx.lib.spgpu_guiding_samples(self.ctx.h))
+
+    def ring(self, max_samples: int):
+        """Training ring entries (n, 16): features 9, direction 3, weight c, proposal pdf q."""
+        out = np.zeros((max_samples, 16), np.float32)
+        cnt = C.c_int32(0)
+        _check(self.ctx.lib.spgpu_guiding_ring(self.ctx.h, out.ctypes.data, max_samples, C.byref(cnt)),
+               "spgpu_guiding_ring")
+        return out[:cnt.value]

@@ -38,26 +38,28 @@ def render_reference(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, sp
 
 
 def render_equal_time(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, budget_ms, guided: bool,
-                      train_fraction=0.25, train_steps=8, seed=1):
-    """Render for budget_ms of device time; returns (mean image, info)."""
+                      train_fraction=0.25, train_steps=16, collect_spp=2, chunk_spp=8, seed=1):
+    """Render for budget_ms of device time (training included for the guided run);
+    returns (mean image, info).  Launches carry chunk_spp samples per pixel."""
     p = {"width": W, "height": H, "maxDepth": scene.max_depth}
     film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
-    spent, passes, trained, offset = 0.0, 0, 0, 0
+    spent, spp, trained, offset, losses = 0.0, 0, 0, 0, []
     if guided:
         scratch = torch.zeros_like(film)
         while spent < train_fraction * budget_ms:
-            st = guide.render(scene.camera, dict(p, sampleCount=1), scratch, GUIDE_GUIDED | GUIDE_COLLECT,
+            st = guide.render(scene.camera, dict(p, sampleCount=collect_spp), scratch, GUIDE_GUIDED | GUIDE_COLLECT,
                               seed=seed + 1000, sample_offset=offset)
-            offset += 1
+            offset += collect_spp
             t0 = time.perf_counter()
-            guide.train(train_steps)
+            losses.append(guide.train(train_steps))
             torch.cuda.synchronize()
             spent += st.ms + 1e3 * (time.perf_counter() - t0)
             trained += train_steps
     flags = GUIDE_GUIDED if guided else 0
     while spent < budget_ms:
-        st = guide.render(scene.camera, dict(p, sampleCount=1), film, flags, seed=seed, sample_offset=passes)
+        st = guide.render(scene.camera, dict(p, sampleCount=chunk_spp), film, flags, seed=seed, sample_offset=spp)
         spent += st.ms
-        passes += 1
+        spp += chunk_spp
     torch.cuda.synchronize()
-    return _mean(film), {"ms": spent, "render_spp": passes, "adam_steps": trained, "training_passes": offset}
+    return _mean(film), {"ms": spent, "render_spp": spp, "adam_steps": trained, "training_spp": offset,
+                         "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None}

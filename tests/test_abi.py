@@ -29,6 +29,16 @@ def test_library_exports_every_declared_symbol():
     assert set(gpu.EXPORTS) <= declared
 
 
+def test_binding_declares_argument_types_for_every_export():
+    """ctypes passes undeclared integer arguments as C int: a 64-bit pointer would be
+    truncated, so every exported function that takes arguments declares them."""
+    from spica_gb300 import gpu
+    lib = gpu.load_library()
+    no_args = {"spgpu_last_error", "spgpu_version"}
+    undeclared = [n for n in gpu.EXPORTS if n not in no_args and getattr(lib, n).argtypes is None]
+    assert not undeclared, undeclared
+
+
 def test_loader_fails_loudly_without_library(tmp_path):
     import pytest
     from spica_gb300 import gpu
