@@ -126,6 +126,19 @@ int spgpu_trace(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float 
                 void *stream);                                                       /* device pointers */
 int spgpu_trace_host(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
                      void *out);                                                     /* host pointers   */
+/* spgpu_trace_host without any device allocation (no counterpart in the reference).
+ * spgpu_trace_host allocates its device ray and hit buffers per call from the
+ * stream-ordered pool; this variant stages them instead in a static device array
+ * reserved with the library on each device (3 MiB + 256 bytes), so it suits callers whose
+ * device memory is fully held by their own allocator or arena, or that must not grow
+ * or trim a memory pool in a latency-critical loop.
+ * Limit: at most 65,536 rays per call; larger n returns SPGPU_EINVAL (split the batch).
+ * The first call on a device looks up the scratch address (set-up); make that first
+ * call before any stream capture.  The scratch is shared by every context on the
+ * device: calls that overlap in time (other threads, other contexts) race on it.
+ * Blocking, like spgpu_trace_host; same arguments and results. */
+int spgpu_trace_host_noalloc(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
+                             void *out);
 /* same as spgpu_trace on device pointers, counting node and triangle visits */
 int spgpu_trace_stats(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
                       void *out, spgpu_trace_counters *counters);

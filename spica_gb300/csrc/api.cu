@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -288,6 +289,45 @@ int checkKernelError(Ctx &C, cudaStream_t s) {
         setError("spgpu_trace: traversal stack overflow or malformed tree");
         return SPGPU_EKERNEL;
     }
+    return 0;
+}
+
+// ---------------------------------------------------------------- static scratch
+// Staging scratch of spgpu_trace_host_noalloc, reserved with the module on every device
+// it is loaded on: the trace kernel's two control words (error flag, ray counter), then
+// kNoAllocMaxRays origins+tmin, directions+tmax and hit records (16 bytes each).
+constexpr int64_t kNoAllocMaxRays = int64_t(1) << 16;   // 65,536 rays per call
+constexpr size_t kNoAllocCtlBytes = 256;
+constexpr size_t kNoAllocRayBytes = static_cast<size_t>(kNoAllocMaxRays) * 16;
+constexpr size_t kNoAllocScratchBytes = kNoAllocCtlBytes + 3 * kNoAllocRayBytes;   // 3 MiB + 256 B
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocSlot {
+    std::once_flag once;
+    unsigned char *base = nullptr;
+    cudaError_t err = cudaSuccess;
+};
+NoAllocSlot g_noallocSlots[kNoAllocMaxDevices];
+
+// Device address of the scratch on `device`, looked up once per device with that device
+// current (the caller has made it current).
+int noallocScratch(int device, unsigned char **base) {
+    if (device < 0 || device >= kNoAllocMaxDevices) {
+        setError("spgpu_trace_host_noalloc: device ordinal out of range");
+        return SPGPU_EINVAL;
+    }
+    NoAllocSlot &S = g_noallocSlots[device];
+    std::call_once(S.once, [&S] {
+        void *p = nullptr;
+        S.err = cudaGetSymbolAddress(&p, g_noallocScratch);
+        S.base = static_cast<unsigned char *>(p);
+    });
+    if (S.err != cudaSuccess || !S.base) {
+        return cudaFail("spgpu_trace_host_noalloc: cudaGetSymbolAddress",
+                        S.err != cudaSuccess ? S.err : cudaErrorInvalidSymbol);
+    }
+    *base = S.base;
     return 0;
 }
 
@@ -662,6 +702,64 @@ int spgpu_trace_host(spgpu_ctx *h, int any_hit, const float *org_tmin, const flo
     cudaFreeAsync(dOut, C.stream);
     if (rc == 0) rc = checkKernelError(C, C.stream);
     return rc;
+}
+
+int spgpu_trace_host_noalloc(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
+                             void *out) {
+    if (!h) return SPGPU_EINVAL;
+    Ctx &C = h->c;
+    if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
+        setError("spgpu_trace_host_noalloc: invalid arguments");
+        return SPGPU_EINVAL;
+    }
+    if (n > kNoAllocMaxRays) {
+        setError("spgpu_trace_host_noalloc: " + std::to_string(n) + " rays exceed the static scratch limit of " +
+                 std::to_string(kNoAllocMaxRays) + " rays per call (split the batch or use spgpu_trace_host)");
+        return SPGPU_EINVAL;
+    }
+    if (!C.bvhReady) {
+        setError("spgpu_trace_host_noalloc: no BVH (call spgpu_upload_scene and spgpu_build_bvh first)");
+        return SPGPU_ESTATE;
+    }
+    if (n == 0) return 0;
+    cudaSetDevice(C.device);
+    unsigned char *base = nullptr;
+    int rc = noallocScratch(C.device, &base);
+    if (rc) return rc;
+    int *ctl = reinterpret_cast<int *>(base);
+    float4 *dO = reinterpret_cast<float4 *>(base + kNoAllocCtlBytes);
+    float4 *dD = reinterpret_cast<float4 *>(base + kNoAllocCtlBytes + kNoAllocRayBytes);
+    unsigned char *dOut = base + kNoAllocCtlBytes + 2 * kNoAllocRayBytes;
+    const size_t rayBytes = static_cast<size_t>(n) * 16;
+    const size_t outBytes = static_cast<size_t>(n) * (any_hit ? 4 : 16);
+    cudaStream_t s = C.stream;
+    // the error flag and the ray counter start at zero
+    cudaError_t e = cudaMemsetAsync(ctl, 0, 2 * sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dO, org_tmin, rayBytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dir_tmax, rayBytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc", e);
+    const int64_t blocksNeeded = (n + kTraceBlock - 1) / kTraceBlock;
+    const int grid = static_cast<int>(std::min<int64_t>(blocksNeeded, static_cast<int64_t>(residentTraceBlocks(C.device))));
+    const uint32_t NN = static_cast<uint32_t>(C.bvh.n_nodes), NT = static_cast<uint32_t>(C.bvh.ntri);
+    if (any_hit)
+        k_trace<true, false><<<grid, kTraceBlock, 0, s>>>(dO, dD, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN, NT,
+                                                          nullptr, reinterpret_cast<uint32_t *>(dOut), ctl, nullptr);
+    else
+        k_trace<false, false><<<grid, kTraceBlock, 0, s>>>(dO, dD, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN,
+                                                           NT, reinterpret_cast<spgpu_hit *>(dOut), nullptr, ctl,
+                                                           nullptr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc: launch", e);
+    int flag = 0;
+    e = cudaMemcpyAsync(out, dOut, outBytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, ctl, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc", e);
+    if (flag) {
+        setError("spgpu_trace_host_noalloc: traversal stack overflow or malformed tree");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
 }
 
 int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_render_stats *stats, void *stream) {

@@ -86,6 +86,7 @@ class Config(C.Structure):
 # every extern "C" symbol include/spica_gpu.h declares
 EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version", "spgpu_upload_scene",
            "spgpu_build_bvh", "spgpu_bvh_stats", "spgpu_trace", "spgpu_trace_host", "spgpu_trace_stats",
+           "spgpu_trace_host_noalloc",
            "spgpu_render", "spgpu_render_host", "spgpu_render_profile", "spgpu_batch_prepare",
            "spgpu_batch_film_pixels", "spgpu_batch_run", "spgpu_guiding_init", "spgpu_guiding_render",
            "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_ring", "spgpu_guiding_params", "spgpu_guiding_mlp",
@@ -114,6 +115,7 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_bvh_stats.argtypes = [vp, C.POINTER(BVHInfo)]
     lib.spgpu_trace.argtypes = [vp, C.c_int, vp, vp, i64, vp, vp]
     lib.spgpu_trace_host.argtypes = [vp, C.c_int, vp, vp, i64, vp]
+    lib.spgpu_trace_host_noalloc.argtypes = [vp, C.c_int, vp, vp, i64, vp]
     lib.spgpu_trace_stats.argtypes = [vp, C.c_int, vp, vp, i64, vp, C.POINTER(TraceCounters)]
     lib.spgpu_render.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats), vp]
     lib.spgpu_render_host.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats)]
@@ -242,6 +244,20 @@ class GpuBVHAccel:
         _check(self.ctx.lib.spgpu_trace_host(self.ctx.h, 1, ot.ctypes.data, dt.ctypes.data, ot.shape[0],
                                              out.ctypes.data), "spgpu_trace_host")
         return out.astype(bool)
+
+    NOALLOC_MAX_RAYS = 65536
+
+    def intersect_noalloc(self, org, dir, tmax=None, tmin=None, any_hit=False):
+        """intersect / intersect_any through spgpu_trace_host_noalloc (no device
+        allocation; at most NOALLOC_MAX_RAYS rays per call)."""
+        ot, dt = _pack_rays(org, dir, tmax, tmin)
+        out = np.zeros(ot.shape[0], np.uint32) if any_hit else np.zeros((ot.shape[0], 4), np.float32)
+        _check(self.ctx.lib.spgpu_trace_host_noalloc(self.ctx.h, 1 if any_hit else 0, ot.ctypes.data, dt.ctypes.data,
+                                                     ot.shape[0], out.ctypes.data), "spgpu_trace_host_noalloc")
+        if any_hit:
+            return out.astype(bool)
+        prim = out[:, 1].view(np.int32).copy()
+        return prim, out[:, 0].copy(), out[:, 2].copy(), out[:, 3].copy()
 
 
 def _pack_rays(org, dir, tmax=None, tmin=None):
