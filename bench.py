@@ -260,7 +260,7 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=512, ref_
     e_p, e_g = guiding.relmse(plain, ref), guiding.relmse(img, ref)
     return {"scene": "indirect-lit room, 2418 tris", "width": W, "height": H, "reference_spp": ref_spp,
             "budget_ms": budget, "relmse_plain": e_p, "relmse_guided": e_g, "equal_time_gain": e_p / e_g,
-            "per_sample_gain": e_p * pi["render_spp"] / (e_g * gi["render_spp"]),
+            "per_sample_gain": e_p * pi["render_spp"] / (e_g * gi["render_spp"]) if gi["render_spp"] else None,
             "plain_spp": pi["render_spp"], "guided_spp": gi["render_spp"], "adam_steps": gi["adam_steps"],
             "training_spp": gi["training_spp"], "train_fraction": 0.25,
             "plain_ms_per_spp": ms8 / 8}
@@ -280,6 +280,8 @@ def main():
     ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel profile (roofline)")
     ap.add_argument("--width", type=int, default=1920, help="film width (profiling cases only)")
     ap.add_argument("--height", type=int, default=1080, help="film height (profiling cases only)")
+    ap.add_argument("--guiding-only", action="store_true",
+                    help="only the learned-guiding comparison, on a small case (320x180, profiling)")
     ap.add_argument("--micro-only", type=int, default=0, metavar="RAYS",
                     help="only the intersection microbench, on RAYS rays (profiling cases)")
     args = ap.parse_args()
@@ -297,6 +299,10 @@ def main():
 
     if args.micro_only:
         print(json.dumps({"microbench": microbench(torch, GpuBVHAccel, scenes, rays=args.micro_only)}), flush=True)
+        return 0
+    if args.guiding_only:
+        print(json.dumps({"guiding": guiding_bench(torch, GpuBVHAccel, scenes, W=320, H=180, budget_spp=64,
+                                                   ref_spp=512)}), flush=True)
         return 0
     scene = scenes.mid_scale(width=args.width, height=args.height)
     W, H, md = scene.width, scene.height, scene.max_depth
