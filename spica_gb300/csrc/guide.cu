@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <vector>
 
@@ -387,8 +388,15 @@ struct GuidedArgs {
     unsigned long long *stats;
 };
 
-constexpr int kGuidedSmem = kPackFwdBytes + kBiasPad * 4 + kGTile * kGK0 * 2 + kGTile * kGHid * 2 +
-                            kGTile * 41 * 4 + kStackShared * kGTile * 8 + 16;
+// guided kernel shared memory: packed forward weights | biases | input/hidden tile (bf16
+// [128][64]; the [128][16] input tile aliases its start) | traversal stacks | mbarrier,
+// TMEM slot
+constexpr int kGuidedSmOffBias = kPackFwdBytes;
+constexpr int kGuidedSmOffXH = kGuidedSmOffBias + 1024;   // biases (960 bytes), padded
+constexpr int kGuidedSmOffStack = kGuidedSmOffXH + kGTile * kGHid * 2;
+constexpr int kGuidedSmOffBar = kGuidedSmOffStack + kStackShared * kGTile * 8;
+constexpr int kGuidedSmem = kGuidedSmOffBar + 16;
+static_assert(kBiasPad * 4 <= 1024 && kGuidedSmOffXH % 128 == 0 && kGuidedSmOffStack % 16 == 0 && kGuidedSmOffBar % 8 == 0, "alignment");
 constexpr int kPlainSmem = kStackShared * kGTile * 8;
 constexpr int kMaxRec = 13;
 
@@ -426,14 +434,11 @@ template <bool GUIDED, bool COLLECT>
 __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t *wf = sm;
-    float *bias = reinterpret_cast<float *>(sm + kPackFwdBytes);
-    uint8_t *x = sm + kPackFwdBytes + kBiasPad * 4;
-    uint8_t *h = x + kGTile * kGK0 * 2;
-    float *out = reinterpret_cast<float *>(h + kGTile * kGHid * 2);
+    float *bias = reinterpret_cast<float *>(sm + kGuidedSmOffBias);
+    uint8_t *xh = sm + kGuidedSmOffXH;
     // the plain kernel keeps only the traversal stacks in shared memory
-    uint2 *stack = GUIDED ? reinterpret_cast<uint2 *>(reinterpret_cast<uint8_t *>(out) + kGTile * 41 * 4)
-                          : reinterpret_cast<uint2 *>(sm);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(stack + kStackShared * kGTile);
+    uint2 *stack = reinterpret_cast<uint2 *>(GUIDED ? sm + kGuidedSmOffStack : sm);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kGuidedSmOffBar);
     uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
     const int t = threadIdx.x;
     const SceneView &S = a.sv;
@@ -550,11 +555,13 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
             float xf[16];
             for (int i = 0; i < 16; i++) xf[i] = 0.0f;
             if (guideMe) guideFeatures(ps, n, -d, a.lo, a.invExt, xf);
-            storeRow8(x, t, 0, kGK0, xf);
-            storeRow8(x, t, 8, kGK0, xf + 8);
-            if (__syncthreads_or(guideMe) && mmaOk)
-                mmaOk = mlpForwardTile(tmem, wf, bias, x, h, h, h, out, 41, bar, phase);
-            if (guideMe && mmaOk) mixtureFromRaw(out + t * 41, mix);
+            storeRow8(xh, t, 0, kGK0, xf);
+            storeRow8(xh, t, 8, kGK0, xf + 8);
+            if (__syncthreads_or(guideMe) && mmaOk) {
+                float raw[kGOut];
+                mmaOk = mlpForwardRow(tmem, wf, bias, xh, bar, phase, raw);
+                if (guideMe && mmaOk) mixtureFromRaw(raw, mix);
+            }
         }
         // ---- shade
         if (active && !ends) {
@@ -763,6 +770,52 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
     atomicAdd(&a.stats[2], nShadow);
 }
 
+// Dynamic shared-memory limits, and the largest shared-memory carveout for the persistent
+// megakernels: with the default carveout the occupancy query (and the hardware) would
+// fit a single 58 KB guided CTA per SM.
+void setGuideKernelAttributes() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TrainLayout::total);
+        cudaFuncSetAttribute(k_guide_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kForwardSmem);
+        cudaFuncSetAttribute(k_guided<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
+        cudaFuncSetAttribute(k_guided<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
+        cudaFuncSetAttribute(k_guided<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_guided<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_guided<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        cudaGetLastError();
+    });
+}
+
+// CTAs of a guided megakernel (kGTile threads, kGuidedSmem bytes of dynamic shared
+// memory, one 64-column TMEM allocation) that fit one SM at once, from the kernel's
+// register count and the device's limits.  (The occupancy API reports a single CTA
+// per SM for kernels that allocate tensor memory; co-resident CTAs are fine as long as
+// their allocations fit the SM's 512 TMEM columns, which the last term ensures.)
+int tmemKernelResidentCtas(const void *kernel, int device) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    int regsSM = 0, smemSM = 0, smemReserved = 0, thrSM = 0, blkSM = 0;
+    cudaDeviceGetAttribute(&regsSM, cudaDevAttrMaxRegistersPerMultiprocessor, device);
+    cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+    cudaDeviceGetAttribute(&smemReserved, cudaDevAttrReservedSharedMemoryPerBlock, device);
+    cudaDeviceGetAttribute(&thrSM, cudaDevAttrMaxThreadsPerMultiProcessor, device);
+    cudaDeviceGetAttribute(&blkSM, cudaDevAttrMaxBlocksPerMultiprocessor, device);
+    const int warps = kGTile / 32;
+    const int regsPerWarp = ((fa.numRegs * 32 + 255) / 256) * 256;
+    const int byRegs = regsPerWarp > 0 ? regsSM / (regsPerWarp * warps) : 1;
+    const int bySmem = smemSM / (kGuidedSmem + static_cast<int>(fa.sharedSizeBytes) + smemReserved);
+    const int byThreads = thrSM / kGTile;
+    constexpr int byTmem = 512 / 64;
+    return std::max(1, std::min(std::min(byRegs, bySmem), std::min(std::min(byThreads, blkSM), byTmem)));
+}
+
 template <class T>
 T *galloc(size_t n) {
     T *p = nullptr;
@@ -848,14 +901,7 @@ int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg) {
         freeGuide(G);
         return rc;
     }
-    static bool attrsSet = false;
-    if (!attrsSet) {
-        cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TrainLayout::total);
-        cudaFuncSetAttribute(k_guide_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kForwardSmem);
-        cudaFuncSetAttribute(k_guided<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
-        cudaFuncSetAttribute(k_guided<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuidedSmem);
-        attrsSet = true;
-    }
+    setGuideKernelAttributes();
     *slot = G;
     return 0;
 }
@@ -1032,11 +1078,11 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
     cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s);
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
-    if (guided && collect) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<true, true>, kGTile, kGuidedSmem);
-    else if (guided) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<true, false>, kGTile, kGuidedSmem);
+    setGuideKernelAttributes();
+    if (guided && collect) occ = tmemKernelResidentCtas(reinterpret_cast<const void *>(k_guided<true, true>), C.device);
+    else if (guided) occ = tmemKernelResidentCtas(reinterpret_cast<const void *>(k_guided<true, false>), C.device);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_guided<false, false>, kGTile, kPlainSmem);
-    // at most 8 TMEM allocations of 64 columns fit an SM's 512 columns
-    const int grid = sms * std::max(1, guided ? std::min(occ, 8) : occ);
+    const int grid = sms * std::max(1, occ);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

@@ -197,4 +197,30 @@ __device__ __forceinline__ bool mlpForwardTile(uint32_t tmem, const uint8_t *wf,
     return true;
 }
 
+// Forward of one tile with the outputs left in registers: thread r receives row r's 40
+// raw outputs.  xh holds the bf16 input tile [128][16] on entry and is reused for the
+// hidden activations (each layer's epilogue runs after the MMA that read it completed).
+__device__ __forceinline__ bool mlpForwardRow(uint32_t tmem, const uint8_t *wf, const float *bias, uint8_t *xh,
+                                              uint64_t *bar, uint32_t &phase, float (&raw)[kGOut]) {
+    const uint8_t *w1 = wf, *w2 = wf + kW1fBytes, *w3 = w2 + kW2fBytes, *w4 = w3 + kW2fBytes;
+    if (!tileMma(tmem, xh, w1, kGK0, kGHid, bar, phase)) return false;
+    hiddenEpilogue(tmem, bias, xh);
+    if (!tileMma(tmem, xh, w2, kGHid, kGHid, bar, phase)) return false;
+    hiddenEpilogue(tmem, bias + kGHid, xh);
+    if (!tileMma(tmem, xh, w3, kGHid, kGHid, bar, phase)) return false;
+    hiddenEpilogue(tmem, bias + 2 * kGHid, xh);
+    if (!tileMma(tmem, xh, w4, kGHid, kGN4, bar, phase)) return false;
+#pragma unroll
+    for (uint32_t c = 0; c < kGN4; c += 16) {
+        float v[16];
+        accRow16(tmem, c, v);
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            if (c + i < kGOut) raw[c + i] = v[i] + bias[3 * kGHid + c + i];
+    }
+    // the next MMA on this accumulator starts with a CTA barrier (tileMma), which
+    // orders it after every thread's tcgen05.ld above
+    return true;
+}
+
 }  // namespace spgpu
