@@ -240,10 +240,11 @@ def batch_bench(torch, GpuBatch, scenes, reps=3):
             "prepare_s": prep_s}
 
 
-def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=512, ref_spp=4096):
+def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=1024, ref_spp=4096):
     """Learned guiding on the indirect-lit room: relMSE against a plain reference at
     equal device time (the time of budget_spp plain samples per pixel), the guided run
-    training online for the first 25% of it; plus the same comparison at equal samples."""
+    training online for the first 25% of it (its collection passes' samples kept in the
+    image); plus the per-sample gain of the same two images."""
     from spica_gb300 import guiding
     from spica_gb300.gpu import GpuGuide
     sc = scenes.guiding_room(width=W, height=H)
@@ -256,12 +257,15 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=512, ref_
     budget = ms8 / 8 * budget_spp
     plain, pi = guiding.render_equal_time(torch, acc, g, sc, W, H, budget, guided=False, seed=11)
     gg = GpuGuide(acc, seed=2)
-    img, gi = guiding.render_equal_time(torch, acc, gg, sc, W, H, budget, guided=True, seed=11, train_steps=64)
+    img, gi = guiding.render_equal_time(torch, acc, gg, sc, W, H, budget, guided=True, seed=11, train_steps=32,
+                                        keep_training_samples=1.0)
     e_p, e_g = guiding.relmse(plain, ref), guiding.relmse(img, ref)
     return {"scene": "indirect-lit room, 2418 tris", "width": W, "height": H, "reference_spp": ref_spp,
             "budget_ms": budget, "relmse_plain": e_p, "relmse_guided": e_g, "equal_time_gain": e_p / e_g,
-            "per_sample_gain": e_p * pi["render_spp"] / (e_g * gi["render_spp"]) if gi["render_spp"] else None,
-            "plain_spp": pi["render_spp"], "guided_spp": gi["render_spp"], "adam_steps": gi["adam_steps"],
+            "per_sample_gain": (e_p * pi["render_spp"] / (e_g * (gi["render_spp"] + gi["kept_training_spp"]))
+                                if gi["render_spp"] else None),
+            "plain_spp": pi["render_spp"], "guided_spp": gi["render_spp"] + gi["kept_training_spp"],
+            "adam_steps": gi["adam_steps"],
             "training_spp": gi["training_spp"], "train_fraction": 0.25,
             "plain_ms_per_spp": ms8 / 8}
 

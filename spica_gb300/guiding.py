@@ -38,18 +38,27 @@ def render_reference(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, sp
 
 
 def render_equal_time(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, budget_ms, guided: bool,
-                      train_fraction=0.25, train_steps=16, collect_spp=2, chunk_spp=8, seed=1):
+                      train_fraction=0.25, train_steps=16, collect_spp=2, chunk_spp=8, seed=1,
+                      keep_training_samples=0.0):
     """Render for budget_ms of device time (training included for the guided run);
-    returns (mean image, info).  Launches carry chunk_spp samples per pixel."""
+    returns (mean image, info).  Launches carry chunk_spp samples per pixel.
+
+    The guided run's collection passes are unbiased renders too: with
+    keep_training_samples = f > 0, the samples of the last fraction f of the training
+    passes (by time) are kept in the image, the earlier ones (from a barely trained
+    network) only feed the training ring."""
     p = {"width": W, "height": H, "maxDepth": scene.max_depth}
     film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
-    spent, spp, trained, offset, losses = 0.0, 0, 0, 0, []
+    spent, spp, trained, offset, losses, kept = 0.0, 0, 0, 0, [], 0
     if guided:
         scratch = torch.zeros_like(film)
-        while spent < train_fraction * budget_ms:
-            st = guide.render(scene.camera, dict(p, sampleCount=collect_spp), scratch, GUIDE_GUIDED | GUIDE_COLLECT,
-                              seed=seed + 1000, sample_offset=offset)
+        t_train = train_fraction * budget_ms
+        while spent < t_train:
+            keep = keep_training_samples > 0 and spent >= (1.0 - keep_training_samples) * t_train
+            st = guide.render(scene.camera, dict(p, sampleCount=collect_spp), film if keep else scratch,
+                              GUIDE_GUIDED | GUIDE_COLLECT, seed=seed + 1000, sample_offset=offset)
             offset += collect_spp
+            kept += collect_spp if keep else 0
             t0 = time.perf_counter()
             losses.append(guide.train(train_steps))
             torch.cuda.synchronize()
@@ -62,4 +71,5 @@ def render_equal_time(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, b
         spp += chunk_spp
     torch.cuda.synchronize()
     return _mean(film), {"ms": spent, "render_spp": spp, "adam_steps": trained, "training_spp": offset,
+                         "kept_training_spp": kept,
                          "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None}
