@@ -11,9 +11,10 @@ timed region; each step's working set (~0.6 GB of queues plus ~0.12 GB of scene)
 larger than the 129 MB L2.
 
 The JSON line carries, besides the headline path samples/s:
-  e2e        the same metric through the host entry point spgpu_render_host: every
-             step copies the film (float4 per pixel) host->device, renders, and copies
-             it back, from pinned host memory
+  e2e        the same metric through the host entry point spgpu_render_host, in render
+             calls of 16 samples per pixel (the reference renders a frame's samples in
+             one call): every call copies the film (float4 per pixel) host->device from
+             pinned host memory, renders, and copies it back
   roofline   the closest-hit traversal kernel ("extend"), measured live: algorithmic
              bytes = rays x (32 B ray + 16 B hit + nodes/ray x 80 B + triangles/ray x
              48 B) per launch over its CUDA-event duration, against the measured HBM
@@ -46,6 +47,9 @@ CONFIG = {"workload": "mid-scale plain render: 500 instances, ~2.03M triangles, 
                       "1920x1080, max depth 16, 1 sample per pixel per step",
           "scene_seed": 0, "width": 1920, "height": 1080, "max_depth": 16,
           "l2": "per-step working set larger than L2 (no flush)", "parallelism": "replicas"}
+
+
+E2E_SPP = 16   # samples per pixel per host-API render call in the end-to-end measurement
 
 
 def dist_env():
@@ -343,20 +347,24 @@ def main():
     value = ws * args.steps * npix / (ms / 1e3)
     rays = st.rays_closest + st.rays_shadow
 
-    # end to end through the host entry point, pinned host film copied both ways per step
+    # end to end through the host entry point: render calls of E2E_SPP samples per pixel
+    # (the reference renders all of a frame's samples in one call), each copying the
+    # pinned host film to the device and back
     film_bytes = npix * 16
     e2e_value = None
+    e2e_calls = max(1, (args.steps + E2E_SPP - 1) // E2E_SPP)
     if not args.no_e2e:
         host_film = torch.zeros((H, W, 4), dtype=torch.float32).pin_memory()
         hf = host_film.numpy()
-        integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=1 << 16)
+        integ.render(scene.camera, acc, dict(params, sampleCount=E2E_SPP), film=hf, sample_offset=1 << 16)
         barrier()
         t0 = time.perf_counter()
-        for k in range(args.steps):
-            integ.render(scene.camera, acc, dict(params, sampleCount=1), film=hf, sample_offset=(1 << 16) + 1 + k)
+        for k in range(e2e_calls):
+            integ.render(scene.camera, acc, dict(params, sampleCount=E2E_SPP), film=hf,
+                         sample_offset=(1 << 16) + E2E_SPP * (k + 1))
         barrier()
         e2e_s = time.perf_counter() - t0
-        e2e_value = ws * args.steps * npix / e2e_s
+        e2e_value = ws * e2e_calls * E2E_SPP * npix / e2e_s
 
     if rank != 0:
         return 0
@@ -398,8 +406,9 @@ def main():
             "mrays_s": ws * args.steps * rays / max(st.paths, 1) * npix / (ms / 1e3) / 1e6 if st.paths else None,
             "rays_per_path": rays / max(st.paths, 1),
             "e2e": None if e2e_value is None else {"value": e2e_value, "unit": UNIT,
-                                                   "h2d_bytes_per_step": film_bytes + 80,
-                                                   "d2h_bytes_per_step": film_bytes},
+                                                   "h2d_bytes_per_step": (film_bytes + 80) / E2E_SPP,
+                                                   "d2h_bytes_per_step": film_bytes / E2E_SPP,
+                                                   "samples_per_call": E2E_SPP, "calls": e2e_calls},
             "gpu_launches": int(args.steps * (2 + 5 * (md + 1))), "clocks": clk, "roofline": roofline,
             "kernels": kernels}
     if not args.no_micro:

@@ -42,7 +42,10 @@ typedef struct spgpu_ctx spgpu_ctx;
 
 typedef struct {
     int device;          /* CUDA device ordinal */
-    int reserved[7];
+    int pass_lanes;      /* spgpu_render: sample passes in flight at once, each with its own
+                            wavefront queues (~200 bytes per pixel) and stream; 0 = 8,
+                            at most 8 */
+    int reserved[6];
 } spgpu_config;
 
 typedef struct {

@@ -470,8 +470,19 @@ int spgpu_create(const spgpu_config *cfg, spgpu_ctx **out) {
     auto *h = new spgpu_ctx();
     Ctx &C = h->c;
     C.device = cfg ? cfg->device : 0;
+    if (cfg && (cfg->pass_lanes < 0 || cfg->pass_lanes > Ctx::kPassLanes)) {
+        setError("spgpu_create: pass_lanes must be 0 (default) or 1.." + std::to_string(Ctx::kPassLanes));
+        delete h;
+        return SPGPU_EINVAL;
+    }
+    C.passLanes = cfg && cfg->pass_lanes > 0 ? cfg->pass_lanes : Ctx::kPassLanes;
     cudaError_t e = cudaSetDevice(C.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking);
+    for (int k = 0; k < Ctx::kPassLanes - 1 && e == cudaSuccess; k++) {
+        e = cudaStreamCreateWithFlags(&C.laneStream[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&C.laneJoin[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&C.laneFork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&C.traceErr, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&C.traceStats, 4 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
@@ -490,6 +501,12 @@ void spgpu_destroy(spgpu_ctx *h) {
     if (C.stream) cudaStreamSynchronize(C.stream);
     freeScene(C);
     freeRenderQueues(&C.rq);
+    for (int k = 0; k < Ctx::kPassLanes - 1; k++) {
+        freeRenderQueues(&C.rqLane[k]);
+        if (C.laneStream[k]) cudaStreamDestroy(C.laneStream[k]);
+        if (C.laneJoin[k]) cudaEventDestroy(C.laneJoin[k]);
+    }
+    if (C.laneFork) cudaEventDestroy(C.laneFork);
     freeBatch(C.batch);
     C.batch = nullptr;
     freeGuide(C.guide);
@@ -624,6 +641,7 @@ int spgpu_build_bvh(spgpu_ctx *h) {
     C.buildMs = ms;
     C.bvhReady = true;
     freeRenderQueues(&C.rq);   // cached graphs refer to the old tree
+    for (int k = 0; k < Ctx::kPassLanes - 1; k++) freeRenderQueues(&C.rqLane[k]);
     return 0;
 }
 

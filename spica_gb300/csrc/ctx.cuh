@@ -100,7 +100,15 @@ struct Ctx {
     int *traceErr = nullptr;
     unsigned long long *traceStats = nullptr;
     // renderer
-    RenderQueues rq;
+    // Render pass lanes: consecutive sample passes alternate between kPassLanes queue
+    // sets (each with its own pass graph), lane k > 0 on laneStream[k - 1], so one
+    // pass's latency-bound last bounces overlap the next pass's first ones.
+    static constexpr int kPassLanes = 8;   // most lanes a context can use
+    int passLanes = kPassLanes;            // lanes in use (spgpu_config::pass_lanes)
+    RenderQueues rq;                          // lane 0 (also the profiling pass)
+    RenderQueues rqLane[kPassLanes - 1];      // lanes 1..
+    cudaStream_t laneStream[kPassLanes - 1] = {};
+    cudaEvent_t laneFork = nullptr, laneJoin[kPassLanes - 1] = {};
     // batched renders (spgpu_batch_prepare / spgpu_batch_run)
     BatchState *batch = nullptr;
     // learned guiding (spgpu_guiding_*)

@@ -57,6 +57,7 @@ struct PassArgs {
     int *counters;     // per bounce: [0] rays in, [1..3] class counts, [4] shadow rays,
                        // [5] / [6] extend / shadow ray-fetch counters
     int *ctl;          // [0] sample index of the pass
+    int ctlStride;     // sample-index step from one pass of this queue set to its next
     unsigned long long *stats;
     unsigned long long *visit;   // [0..1] extend nodes / triangles, [2..3] shadow nodes / triangles
     int *err;
@@ -96,9 +97,7 @@ __global__ void k_raygen(PassArgs p) {
         p.rayO0[pix] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
         p.rayD0[pix] = make_float4(d.x, d.y, d.z, kInfT);
         p.beta[pix] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        float4 f = p.film[fi];
-        f.w += 1.0f;
-        p.film[fi] = f;
+        atomicAdd(&p.film[fi].w, 1.0f);   // passes of other lanes may add to this pixel concurrently
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) p.counters[0] = p.npix;
 }
@@ -239,7 +238,7 @@ __global__ void k_finish(PassArgs p) {
     p.stats[0] += static_cast<unsigned long long>(p.npix);
     p.stats[1] += rays;
     p.stats[2] += shadow;
-    p.ctl[0] += 1;
+    p.ctl[0] += p.ctlStride;
 }
 
 template <class T>
@@ -363,8 +362,8 @@ void freeRenderQueues(RenderQueues *q) {
 }
 
 namespace {
-int setupPass(Ctx &C, const float *camera, int W, int H, int maxDepth, uint32_t seed, float4 *film, PassArgs *out) {
-    RenderQueues &q = C.rq;
+int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int maxDepth, uint32_t seed, float4 *film,
+              int ctlStride, PassArgs *out) {
     const int64_t npix = static_cast<int64_t>(W) * H;
     int rc = ensureQueues(q, npix, maxDepth);
     if (rc) return rc;
@@ -394,6 +393,36 @@ int setupPass(Ctx &C, const float *camera, int W, int H, int maxDepth, uint32_t 
     a.stats = q.stats;
     a.visit = q.stats + 4;
     a.err = q.err;
+    a.ctlStride = ctlStride;
+    return 0;
+}
+
+// (re)capture the pass graph of queue set q when anything baked into it changes
+int ensurePassGraph(Ctx &C, RenderQueues &q, const PassArgs &a, int W, int H, int maxDepth, uint32_t seed,
+                    float4 *film) {
+    uint64_t key[4];
+    key[0] = hashBytes(&a, sizeof(a));
+    key[1] = static_cast<uint64_t>(W) << 32 | static_cast<uint32_t>(H);
+    key[2] = static_cast<uint64_t>(maxDepth) << 32 | seed;
+    key[3] = reinterpret_cast<uint64_t>(film);
+    if (q.graph && std::memcmp(key, q.graphKey, sizeof(key)) == 0) return 0;
+    if (q.graph) {
+        cudaGraphExecDestroy(q.graph);
+        q.graph = nullptr;
+    }
+    const Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
+    const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;
+    cudaStream_t cs = C.stream;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cudaFail("cudaStreamBeginCapture", e);
+    launchPass<false>(a, gr, cs, ctrBytes, nullptr, nullptr, nullptr);
+    e = cudaStreamEndCapture(cs, &g);
+    if (e != cudaSuccess) return cudaFail("cudaStreamEndCapture", e);
+    e = cudaGraphInstantiate(&q.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cudaFail("cudaGraphInstantiate", e);
+    std::memcpy(q.graphKey, key, sizeof(key));
     return 0;
 }
 }  // namespace
@@ -401,59 +430,62 @@ int setupPass(Ctx &C, const float *camera, int W, int H, int maxDepth, uint32_t 
 int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
                 float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
     Ctx &C = *ctx;
-    RenderQueues &q = C.rq;
-    const int64_t npix = static_cast<int64_t>(W) * H;
-    PassArgs a;
-    int rc = setupPass(C, camera, W, H, maxDepth, seed, film, &a);
-    if (rc) return rc;
-
-    // (re)capture the pass graph when anything baked into it changes
-    uint64_t key[4];
-    key[0] = hashBytes(&a, sizeof(a));
-    key[1] = static_cast<uint64_t>(W) << 32 | static_cast<uint32_t>(H);
-    key[2] = static_cast<uint64_t>(maxDepth) << 32 | seed;
-    key[3] = reinterpret_cast<uint64_t>(film);
-    if (!q.graph || std::memcmp(key, q.graphKey, sizeof(key)) != 0) {
-        if (q.graph) {
-            cudaGraphExecDestroy(q.graph);
-            q.graph = nullptr;
-        }
-        const Grids gr = passGrids(C.device, npix);
-        const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;
-        cudaStream_t cs = C.stream;
-        cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) return cudaFail("cudaStreamBeginCapture", e);
-        launchPass<false>(a, gr, cs, ctrBytes, nullptr, nullptr, nullptr);
-        e = cudaStreamEndCapture(cs, &g);
-        if (e != cudaSuccess) return cudaFail("cudaStreamEndCapture", e);
-        e = cudaGraphInstantiate(&q.graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cudaFail("cudaGraphInstantiate", e);
-        std::memcpy(q.graphKey, key, sizeof(key));
+    // pass lanes in use: one per pass up to the context's setting
+    const int lanes = std::max(1, std::min(spp, C.passLanes));
+    RenderQueues *qs[Ctx::kPassLanes];
+    cudaStream_t ss[Ctx::kPassLanes];
+    qs[0] = &C.rq;
+    ss[0] = stream;
+    for (int k = 1; k < lanes; k++) {
+        qs[k] = &C.rqLane[k - 1];
+        ss[k] = C.laneStream[k - 1];
+    }
+    for (int k = 0; k < lanes; k++) {
+        PassArgs a;
+        int rc = setupPass(C, *qs[k], camera, W, H, maxDepth, seed, film, lanes, &a);
+        if (!rc) rc = ensurePassGraph(C, *qs[k], a, W, H, maxDepth, seed, film);
+        if (rc) return rc;
     }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    cudaError_t e = cudaMemsetAsync(q.stats, 0, 8 * sizeof(unsigned long long), stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(q.err, 0, sizeof(int), stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(a.ctl, &sampleOffset, sizeof(int), cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) e = cudaEventRecord(e0, stream);
-    for (int s = 0; s < spp && e == cudaSuccess; s++) e = cudaGraphLaunch(q.graph, stream);
+    cudaError_t e = cudaEventRecord(e0, stream);
+    if (e == cudaSuccess && lanes > 1) e = cudaEventRecord(C.laneFork, stream);
+    for (int k = 0; k < lanes && e == cudaSuccess; k++) {
+        RenderQueues &q = *qs[k];
+        if (k > 0) e = cudaStreamWaitEvent(ss[k], C.laneFork, 0);
+        const int first = sampleOffset + k;   // lane k renders samples first, first + lanes, ...
+        int *ctl = q.counters + (q.maxDepth + 2) * kCountersPerBounce;
+        if (e == cudaSuccess) e = cudaMemsetAsync(q.stats, 0, 8 * sizeof(unsigned long long), ss[k]);
+        if (e == cudaSuccess) e = cudaMemsetAsync(q.err, 0, sizeof(int), ss[k]);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, &first, sizeof(int), cudaMemcpyHostToDevice, ss[k]);
+    }
+    for (int s = 0; s < spp && e == cudaSuccess; s++) e = cudaGraphLaunch(qs[s % lanes]->graph, ss[s % lanes]);
+    for (int k = 1; k < lanes && e == cudaSuccess; k++) {
+        e = cudaEventRecord(C.laneJoin[k - 1], ss[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, C.laneJoin[k - 1], 0);
+    }
     if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
-    unsigned long long st[4] = {0, 0, 0, 0};
-    int err = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(st, q.stats, sizeof(st), cudaMemcpyDeviceToHost, stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, q.err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    unsigned long long st[Ctx::kPassLanes][4] = {};
+    int err[Ctx::kPassLanes] = {};
+    for (int k = 0; k < lanes && e == cudaSuccess; k++) {
+        e = cudaMemcpyAsync(st[k], qs[k]->stats, sizeof(st[k]), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&err[k], qs[k]->err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     float ms = 0.0f;
     if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cudaFail("spgpu_render", e);
-    for (int k = 0; k < 4; k++) statsOut[k] = st[k];
+    int anyErr = 0;
+    for (int j = 0; j < 4; j++) statsOut[j] = 0;
+    for (int k = 0; k < lanes; k++) {
+        for (int j = 0; j < 4; j++) statsOut[j] += st[k][j];
+        anyErr |= err[k];
+    }
     *msOut = ms;
-    if (err) {
+    if (anyErr) {
         setError("spgpu_render: traversal stack overflow");
         return SPGPU_EKERNEL;
     }
@@ -466,7 +498,7 @@ int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int samp
     Ctx &C = *ctx;
     RenderQueues &q = C.rq;
     PassArgs a;
-    int rc = setupPass(C, camera, W, H, maxDepth, seed, film, &a);
+    int rc = setupPass(C, q, camera, W, H, maxDepth, seed, film, 1, &a);
     if (rc) return rc;
     const Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
     const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;

@@ -80,7 +80,7 @@ GUIDE_PARAMS = 11560
 
 
 class Config(C.Structure):
-    _fields_ = [("device", C.c_int), ("reserved", C.c_int * 7)]
+    _fields_ = [("device", C.c_int), ("pass_lanes", C.c_int), ("reserved", C.c_int * 6)]
 
 
 # every extern "C" symbol include/spica_gpu.h declares
@@ -157,9 +157,9 @@ def _ptr(a) -> int:
 class Context:
     """One device, one scene and its BVH (spgpu_ctx)."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, pass_lanes: int = 0):
         self.lib = load_library()
-        cfg = Config(device=device)
+        cfg = Config(device=device, pass_lanes=pass_lanes)
         h = C.c_void_p()
         _check(self.lib.spgpu_create(C.byref(cfg), C.byref(h)), "spgpu_create")
         self.h = h

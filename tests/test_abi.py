@@ -39,6 +39,18 @@ def test_binding_declares_argument_types_for_every_export():
     assert not undeclared, undeclared
 
 
+def test_create_rejects_invalid_pass_lanes():
+    """The configuration is validated before any device call (so this runs without a
+    GPU): pass_lanes outside 0..8 is refused with SPGPU_EINVAL and a message."""
+    from spica_gb300 import gpu
+    lib = gpu.load_library()
+    for bad in (-1, 9):
+        h = ctypes.c_void_p()
+        rc = lib.spgpu_create(ctypes.byref(gpu.Config(device=0, pass_lanes=bad)), ctypes.byref(h))
+        assert rc == -1 and not h.value
+        assert b"pass_lanes" in lib.spgpu_last_error()
+
+
 def test_loader_fails_loudly_without_library(tmp_path):
     import pytest
     from spica_gb300 import gpu
