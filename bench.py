@@ -50,6 +50,7 @@ CONFIG = {"workload": "mid-scale plain render: 500 instances, ~2.03M triangles, 
 
 
 E2E_SPP = 16   # samples per pixel per host-API render call in the end-to-end measurement
+EXTEND_DRAM_BYTES_PER_LAUNCH = 29.48e6   # measured with ncu on the 1920x1080 workload
 
 
 def dist_env():
@@ -391,12 +392,10 @@ def main():
                 "traffic": None, "bytes_per_ray": bytes_per_ray, "rays_per_launch": rays_per_launch,
                 "ms_per_launch": ext_ms_per_launch, "nodes_per_ray": pr.closest_nodes_per_ray,
                 "tris_per_ray": pr.closest_tris_per_ray}
-    traffic_file = os.path.join(ROOT, "profiles", "extend_traffic.json")
-    if os.path.exists(traffic_file):
-        try:
-            roofline["traffic"] = json.load(open(traffic_file))["bytes_per_launch_full"]
-        except Exception:
-            pass
+    if (W, H) == (1920, 1080):
+        # ncu dram__bytes_read.sum + dram__bytes_write.sum of the 17 extend launches of a
+        # full-size pass, averaged per launch (profiles/extend_traffic_midscale_1080p.md)
+        roofline["traffic"] = EXTEND_DRAM_BYTES_PER_LAUNCH
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
