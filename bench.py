@@ -53,6 +53,20 @@ E2E_SPP = 16   # samples per pixel per host-API render call in the end-to-end me
 EXTEND_DRAM_BYTES_PER_LAUNCH = 29.48e6   # measured with ncu on the 1920x1080 workload
 
 
+def max_over_ranks(torch, x: float, ws: int, device: str = "cuda") -> float:
+    """The largest of every rank's x (the job's time is its slowest replica's)."""
+    if ws <= 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(ws: int, units_per_rank: int, ms: float) -> float:
+    """Whole-job units/s: every rank processed units_per_rank in at most ms."""
+    return ws * units_per_rank / (ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -340,12 +354,8 @@ def main():
     ev1.record()
     barrier()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * args.steps * npix / (ms / 1e3)
+    ms = max_over_ranks(torch, ev0.elapsed_time(ev1), ws, device="cuda")
+    value = replica_throughput(ws, args.steps * npix, ms)
     rays = st.rays_closest + st.rays_shadow
 
     # end to end through the host entry point: render calls of E2E_SPP samples per pixel

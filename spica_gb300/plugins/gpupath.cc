@@ -55,6 +55,7 @@ class GpuPathIntegrator : public Integrator {
 public:
     explicit GpuPathIntegrator(RenderParams &params)
         : device_{params.getInt("gpuDevice", 0, true)},
+          passLanes_{params.getInt("gpuPassLanes", 0, true)},
           seed_{static_cast<uint32_t>(params.getInt("seed", 0, true))} {}
 
     void render(const std::shared_ptr<const Camera> &camera, const Scene &scene, RenderParams &params) override {
@@ -100,7 +101,7 @@ public:
                 }
         }
         spgpu_ctx *ctx = nullptr;
-        spgpu_config cfg = {device_, {0}};
+        spgpu_config cfg = {device_, passLanes_, {0}};
         check(spgpu_create(&cfg, &ctx));
         check(spgpu_upload_scene(ctx, static_cast<int32_t>(triMat.size()), verts.data(), triMat.data(),
                                  static_cast<int32_t>(mats.size() / 8), mats.data(), emit.data(), ew, eh,
@@ -184,6 +185,7 @@ private:
     }
 
     int device_;
+    int passLanes_;   // sample passes in flight (spgpu_config::pass_lanes; 0 = default)
     uint32_t seed_;
 };
 
