@@ -233,12 +233,12 @@ def microbench(torch, GpuBVHAccel, scenes, reps=3, rays=16 << 20):
             "any_tris_per_ray": ca.tris_per_ray, "bvh_build_ms": info.build_ms, "wide_nodes": int(info.wide_nodes)}
 
 
-def batch_bench(torch, GpuBatch, scenes, reps=3):
+def batch_bench(torch, GpuBatch, scenes, reps=3, count=64, autotune=True):
     """64 seeded box-room variants (resolution 64..512 squared, 16..256 spp) in one
     persistent graph-captured launch; launch shape from the autotuner."""
-    vs = scenes.batch_variants(64, seed=0)
+    vs = scenes.batch_variants(count, seed=0)
     t0 = time.perf_counter()
-    b = GpuBatch(vs, seed=7, autotune=True)
+    b = GpuBatch(vs, seed=7, autotune=autotune)
     prep_s = time.perf_counter() - t0
     films = torch.zeros((b.pixels, 4), dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
@@ -303,6 +303,9 @@ def main():
     ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel profile (roofline)")
     ap.add_argument("--width", type=int, default=1920, help="film width (profiling cases only)")
     ap.add_argument("--height", type=int, default=1080, help="film height (profiling cases only)")
+    ap.add_argument("--batch-only", type=int, default=0, metavar="RENDERS",
+                    help="only the batched-renders measurement on the first RENDERS variants, default launch "
+                         "shape (profiling cases)")
     ap.add_argument("--guiding-only", action="store_true",
                     help="only the learned-guiding comparison, on a small case (320x180, profiling)")
     ap.add_argument("--micro-only", type=int, default=0, metavar="RAYS",
@@ -322,6 +325,10 @@ def main():
 
     if args.micro_only:
         print(json.dumps({"microbench": microbench(torch, GpuBVHAccel, scenes, rays=args.micro_only)}), flush=True)
+        return 0
+    if args.batch_only:
+        print(json.dumps({"batch": batch_bench(torch, GpuBatch, scenes, reps=1, count=args.batch_only,
+                                               autotune=False)}), flush=True)
         return 0
     if args.guiding_only:
         print(json.dumps({"guiding": guiding_bench(torch, GpuBVHAccel, scenes, W=320, H=180, budget_spp=64,
