@@ -83,6 +83,43 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def path_bytes(pr) -> float:
+    """Algorithmic HBM bytes per path sample of the wavefront pass, from the kernels' own
+    counters and this implementation's queue layout: camera ray + path state written by
+    raygen (48 B) and the film count (4 B); per closest ray its traversal bytes (32 B ray,
+    16 B hit, 80 B per node, 48 B per triangle), the class-queue index (4 B), the shading
+    gathers (index 4 + hit 16 + ray 32 + path state 16 B) and the continuation ray and
+    path state (48 B); per shadow ray its 48 B queue record written by shading and read
+    back, 80 B per node and 48 B per triangle, and the film atomic (16 B)."""
+    if not pr.paths:
+        return 0.0
+    c = pr.rays_closest / pr.paths
+    sh = pr.rays_shadow / pr.paths
+    closest = 32 + 16 + 80 * pr.closest_nodes_per_ray + 48 * pr.closest_tris_per_ray + 4 + 68 + 48
+    shadow = 48 + 48 + 80 * pr.shadow_nodes_per_ray + 48 * pr.shadow_tris_per_ray + 16
+    return 52 + c * closest + sh * shadow
+
+
 class ClockSampler:
     """nvidia-smi samples every 200 ms while the timed region runs."""
 
@@ -131,7 +168,7 @@ def cpu_oracle():
     kind = "reference" if spo.available("ref") else "port"
     if kind == "port" and not spo.available("port"):
         spo.build("port")
-    return spo.Oracle(kind), kind
+    return spo.Oracle("ref" if kind == "reference" else "port"), kind
 
 
 def cpu_sample(scene, seconds: float = 15.0, threads: int = 0):
@@ -188,13 +225,33 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(CONFIG, step=f"{rows} film rows x {W} px, 1 sample per pixel"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": f"{args.steps} steps of {rows} rows x {W} px"},
+                             "sample": f"{args.steps} steps of {rows} rows x {W} px", "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def microbench(torch, GpuBVHAccel, scenes, reps=3, rays=16 << 20):
+def cpu_trace_sample(sph, org, d, tmax, n_sample=1 << 20):
+    """Closest- and any-hit Mrays/s of the CPU oracle on every host thread, on an evenly
+    strided sample of the microbench's rays (coherent and incoherent halves alike)."""
+    o, kind = cpu_oracle()
+    t0 = time.perf_counter()
+    sc = o.scene(sph)
+    build_s = time.perf_counter() - t0
+    idx = np.linspace(0, org.shape[0] - 1, n_sample).astype(np.int64)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    sc.trace(org[idx], d[idx], nthreads=threads)
+    tc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sc.trace(org[idx], d[idx], tmax[idx], any_hit=True, nthreads=threads)
+    ta = time.perf_counter() - t0
+    return {"closest_mrays_s": n_sample / tc / 1e6, "any_mrays_s": n_sample / ta / 1e6, "cores": threads,
+            "kind": kind, "sample": f"{n_sample} of the rays (every {org.shape[0] // n_sample}th)",
+            "bvh_build_s": build_s}
+
+
+def microbench(torch, GpuBVHAccel, scenes, reps=3, rays=16 << 20, cpu=False):
     sph = scenes.displaced_sphere(levels=9, seed=0)
     acc = GpuBVHAccel(sph).construct()
     org, d, tmax = scenes.microbench_rays(sph, rays // 2, rays - rays // 2, 4096, 2048, seed=0)
@@ -227,10 +284,13 @@ def microbench(torch, GpuBVHAccel, scenes, reps=3, rays=16 << 20):
     ms_a = timed(lambda: acc.intersect_device(ot, dt, anyo, any_hit=True, stream=stream))
     ca = acc.intersect_stats(ot, dt, anyo, any_hit=True)
     info = acc.info()
-    return {"triangles": int(sph.ntri), "rays": int(n), "closest_mrays_s": n / ms_c / 1e3,
-            "any_mrays_s": n / ms_a / 1e3, "closest_nodes_per_ray": cc.nodes_per_ray,
-            "closest_tris_per_ray": cc.tris_per_ray, "any_nodes_per_ray": ca.nodes_per_ray,
-            "any_tris_per_ray": ca.tris_per_ray, "bvh_build_ms": info.build_ms, "wide_nodes": int(info.wide_nodes)}
+    out = {"triangles": int(sph.ntri), "rays": int(n), "closest_mrays_s": n / ms_c / 1e3,
+           "any_mrays_s": n / ms_a / 1e3, "closest_nodes_per_ray": cc.nodes_per_ray,
+           "closest_tris_per_ray": cc.tris_per_ray, "any_nodes_per_ray": ca.nodes_per_ray,
+           "any_tris_per_ray": ca.tris_per_ray, "bvh_build_ms": info.build_ms, "wide_nodes": int(info.wide_nodes)}
+    if cpu:
+        out["cpu_baseline"] = cpu_trace_sample(sph, org, d, tmax)
+    return out
 
 
 def batch_bench(torch, GpuBatch, scenes, reps=3, count=64, autotune=True):
@@ -279,6 +339,20 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=1024, ref
     img, gi = guiding.render_equal_time(torch, acc, gg, sc, W, H, budget, guided=True, seed=11, train_steps=32,
                                         keep_training_samples=1.0)
     e_p, e_g = guiding.relmse(plain, ref), guiding.relmse(img, ref)
+    # training kernel throughput: 64 Adam steps on the trained ring, CUDA events
+    steps = 64
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    gg.train(steps)
+    ev1.record()
+    torch.cuda.synchronize()
+    step_ms = ev0.elapsed_time(ev1) / steps
+    flop = 16384 * (22656 + 45312)   # batch x (forward + backward) per step; Adam is O(params)
+    peak, src = bf16_peak()
+    train_roof = {"bound": "tensor", "achieved": flop / (step_ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                  "frac": flop / (step_ms / 1e3) / 1e12 / peak, "peak_source": src, "ms_per_step": step_ms,
+                  "flop_per_step": flop}
     return {"scene": "indirect-lit room, 2418 tris", "width": W, "height": H, "reference_spp": ref_spp,
             "budget_ms": budget, "relmse_plain": e_p, "relmse_guided": e_g, "equal_time_gain": e_p / e_g,
             "per_sample_gain": (e_p * pi["render_spp"] / (e_g * (gi["render_spp"] + gi["kept_training_spp"]))
@@ -286,7 +360,7 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=1024, ref
             "plain_spp": pi["render_spp"], "guided_spp": gi["render_spp"] + gi["kept_training_spp"],
             "adam_steps": gi["adam_steps"],
             "training_spp": gi["training_spp"], "train_fraction": 0.25,
-            "plain_ms_per_spp": ms8 / 8}
+            "plain_ms_per_spp": ms8 / 8, "training_roofline": train_roof}
 
 
 def main():
@@ -414,6 +488,9 @@ def main():
         # full-size pass, averaged per launch (profiles/extend_traffic_midscale_1080p.md)
         roofline["traffic"] = EXTEND_DRAM_BYTES_PER_LAUNCH
 
+    pb = path_bytes(pr)
+    path_roof = {"bound": "hbm", "bytes_per_path": pb, "achieved": value / ws * pb / 1e9, "peak": hbm, "unit": "GB/s",
+                 "frac": value / ws * pb / 1e9 / hbm}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
@@ -426,9 +503,10 @@ def main():
                                                    "d2h_bytes_per_step": film_bytes / E2E_SPP,
                                                    "samples_per_call": E2E_SPP, "calls": e2e_calls},
             "gpu_launches": int(args.steps * (2 + 5 * (md + 1))), "clocks": clk, "roofline": roofline,
+            "path_roofline": path_roof,
             "kernels": kernels}
     if not args.no_micro:
-        line["microbench"] = microbench(torch, GpuBVHAccel, scenes)
+        line["microbench"] = microbench(torch, GpuBVHAccel, scenes, cpu=not args.no_cpu and ws == 1)
     if not args.no_batch:
         line["batch"] = batch_bench(torch, GpuBatch, scenes)
     if not args.no_guiding:
@@ -436,7 +514,7 @@ def main():
     if not args.no_cpu and ws == 1:
         v, kind, cores, desc, build_s = cpu_sample(scene)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc,
-                                "bvh_build_s": build_s}
+                                "bvh_build_s": build_s, "cpu_model": cpu_model()}
     print(json.dumps(line), flush=True)
     return 0
 
