@@ -85,8 +85,20 @@ typedef struct {
     int32_t sample_offset;
     int32_t max_depth;   /* the reference's "maxDepth" render parameter */
     uint32_t seed;
-    int32_t reserved[4];
+    int32_t integrator;  /* SPGPU_INTEGRATOR_PATH (0) or SPGPU_INTEGRATOR_DIRECT (1) */
+    int32_t reserved[3];
 } spgpu_render_desc;
+
+/* PathIntegrator::Li (integrators/path/path.cc:42) */
+#define SPGPU_INTEGRATOR_PATH 0
+/* DirectLightingIntegrator::Li (integrators/directlighting/directlighting.cc:21): the
+ * camera ray's emission or environment radiance plus one-light NEE with both MIS
+ * strategies at its first hit.  Its specular recursion (specularReflect /
+ * specularTransmit, core/integrator.cc:112-152) samples only BxDFs whose type is
+ * Reflection|Specular or Transmission|Specular alone; none of the three materials has
+ * one, so it never recurses and max_depth has no effect.  spgpu_render and
+ * spgpu_render_host only; batches and guided renders take the path integrator. */
+#define SPGPU_INTEGRATOR_DIRECT 1
 
 typedef struct {
     int64_t paths;             /* camera paths traced */

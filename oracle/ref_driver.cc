@@ -48,6 +48,7 @@
 #include "cameras/perspective.h"
 #include "films/hdrfilm.h"
 #include "filters/box.h"
+#include "integrators/directlighting/directlighting.h"
 #include "integrators/path/path.h"
 #include "lights/area.h"
 #include "lights/envmap.h"
@@ -90,6 +91,16 @@ std::shared_ptr<SurfaceMaterial> makeSurface(const double *m) {
 class OpenPath : public PathIntegrator {
 public:
     explicit OpenPath(const std::shared_ptr<Sampler> &s) : PathIntegrator{s} {}
+    Spectrum radiance(const Scene &scene, RenderParams &params, const Ray &ray,
+                      Sampler &sampler, MemoryArena &arena) const {
+        return Li(scene, params, ray, sampler, arena, 0);
+    }
+};
+
+// DirectLightingIntegrator::Li (integrators/directlighting/directlighting.cc:21)
+class OpenDirect : public DirectLightingIntegrator {
+public:
+    explicit OpenDirect(const std::shared_ptr<Sampler> &s) : DirectLightingIntegrator{s} {}
     Spectrum radiance(const Scene &scene, RenderParams &params, const Ray &ray,
                       Sampler &sampler, MemoryArena &arena) const {
         return Li(scene, params, ray, sampler, arena, 0);
@@ -203,8 +214,13 @@ int spo_trace(spo_scene *s, int any, int64_t n, const double *org, const double 
     return 0;
 }
 
-int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h,
-               int spp, int max_depth, uint32_t seed, double *sum, double *sumsq, int nthreads) {
+}  // extern "C"
+
+namespace {
+// Film window render shared by the integrators: radiance(ray, sampler, arena) gives Li.
+template <class Integ>
+int renderWindow(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h, int spp,
+                 int max_depth, uint32_t seed, double *sum, double *sumsq, int nthreads) {
     RenderParams &params = RenderParams::getInstance();
     params.add("maxDepth", max_depth);
     auto film = std::make_shared<HDRFilm>(Point2i(W, H),
@@ -216,7 +232,7 @@ int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, 
     auto camera = std::make_shared<PerspectiveCamera>(c2w, Bounds2d(-1.0, -1.0, 1.0, 1.0), 0.0,
                                                       50.0, cam[9] * PI / 180.0, film);
     auto proto = std::make_shared<Independent>(0u);
-    OpenPath integrator(proto);
+    Integ integrator(proto);
     const int64_t npix = static_cast<int64_t>(w) * h;
     parallelRange(npix, nthreads, 1, [&](int64_t b, int64_t e) {
         MemoryArena arena;
@@ -246,6 +262,18 @@ int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, 
         }
     });
     return 0;
+}
+}  // namespace
+
+extern "C" {
+int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h,
+               int spp, int max_depth, uint32_t seed, double *sum, double *sumsq, int nthreads) {
+    return renderWindow<OpenPath>(s, cam, W, H, fx0, fy0, w, h, spp, max_depth, seed, sum, sumsq, nthreads);
+}
+
+int spo_render_direct(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h,
+                      int spp, int max_depth, uint32_t seed, double *sum, double *sumsq, int nthreads) {
+    return renderWindow<OpenDirect>(s, cam, W, H, fx0, fy0, w, h, spp, max_depth, seed, sum, sumsq, nthreads);
 }
 
 namespace {

@@ -1178,6 +1178,32 @@ struct spo_scene {
         }
         return L;
     }
+
+    // DirectLightingIntegrator::Li, integrators/directlighting/directlighting.cc:21.
+    // Its specular recursion (core/integrator.cc:112-152) samples BxDFs of type
+    // Reflection|Specular or Transmission|Specular alone (bsdf.cc:28 matching); none
+    // of the three materials has one, so it never recurses.
+    RGB LiDirect(Ray ray, Sampler &sampler, int maxDepth) const {
+        Hit h;
+        if (!intersect(ray, &h)) return hasEnv ? env.Le(ray.d) : RGB(0.0);   // sum of Light::Le(ray)
+        RGB L(0.0);
+        if (triLight[h.prim] >= 0) L = areaL(h.prim, h.n, -ray.d);        // depth 0: isect.Le(-dir)
+        const int nL = numLights();
+        if (nL > 0) {   // uniformSampleOneLight, core/mis.cc:21
+            const BSDF b = makeBSDF(&mats[SPO_MAT_STRIDE * triMat[h.prim]], h.n, h.dpdu, h.dpdv);
+            const int light = std::min(static_cast<int>(sampler.get1D() * nL), nL - 1);
+            const P2 uLight = sampler.get2D();
+            const P2 uShade = sampler.get2D();
+            if (b.numComponents(kAll & ~kSpecular) > 0) L = L + nL * directLight(h, b, uShade, light, uLight);
+        }
+        if (1 < maxDepth) {
+            // specularReflect / specularTransmit draw their 2D sample before finding no
+            // matching BxDF (core/integrator.cc:120,142)
+            (void)sampler.get2D();
+            (void)sampler.get2D();
+        }
+        return L;
+    }
 };
 
 namespace {
@@ -1270,8 +1296,13 @@ int spo_trace(spo_scene *s, int any, int64_t n, const double *org, const double 
     return 0;
 }
 
-int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h, int spp,
-               int max_depth, uint32_t seed, double *sum, double *sumsq, int nthreads) {
+}  // extern "C"
+
+namespace {
+// Film window render shared by the integrators: radiance(scene, ray, sampler) gives Li.
+template <class F>
+int renderWindow(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h, int spp,
+                 uint32_t seed, double *sum, double *sumsq, int nthreads, F radiance) {
     const Camera camera(cam, W, H);
     const int64_t npix = static_cast<int64_t>(w) * h;
     parallelRange(npix, nthreads, 1, [&](int64_t b, int64_t e) {
@@ -1286,7 +1317,7 @@ int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, 
                 (void)sampler.get2D();   // lens sample (pinhole camera ignores it)
                 V3 o, d;
                 camera.spawnRay(x, y, film, &o, &d);
-                const RGB L = s->Li(Ray(o, d), sampler, max_depth);
+                const RGB L = radiance(Ray(o, d), sampler);
                 const double c[3] = {L.r, L.g, L.b};
                 for (int j = 0; j < 3; j++) {
                     acc[j] += c[j];
@@ -1300,6 +1331,20 @@ int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, 
         }
     });
     return 0;
+}
+}  // namespace
+
+extern "C" {
+int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h, int spp,
+               int max_depth, uint32_t seed, double *sum, double *sumsq, int nthreads) {
+    return renderWindow(s, cam, W, H, fx0, fy0, w, h, spp, seed, sum, sumsq, nthreads,
+                        [&](const Ray &r, Sampler &smp) { return s->Li(r, smp, max_depth); });
+}
+
+int spo_render_direct(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w, int h, int spp,
+                      int max_depth, uint32_t seed, double *sum, double *sumsq, int nthreads) {
+    return renderWindow(s, cam, W, H, fx0, fy0, w, h, spp, seed, sum, sumsq, nthreads,
+                        [&](const Ray &r, Sampler &smp) { return s->LiDirect(r, smp, max_depth); });
 }
 
 int spo_bsdf_eval(const double *mat, int64_t n, const double *wo, const double *wi, double *f, double *pdf) {

@@ -69,6 +69,7 @@ class Oracle:
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         lib.spo_render.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.c_int, C.c_int, C.c_int, C.c_uint32, _dp, _dp, C.c_int]
+        lib.spo_render_direct.argtypes = lib.spo_render.argtypes
         lib.spo_bsdf_eval.argtypes = [_dp, C.c_int64, _dp, _dp, _dp, _dp]
         lib.spo_bsdf_sample.argtypes = [_dp, C.c_int64, _dp, _dp, _dp, _dp, _dp, _ip]
         lib.spo_name.restype = C.c_char_p
@@ -152,12 +153,14 @@ class OracleScene:
                              prim.ctypes.data, t.ctypes.data, hit.ctypes.data, nthreads)
         return prim, t
 
-    def render(self, cam, W, H, spp, max_depth, seed=0, window=None, nthreads=None):
-        """Per-pixel (sum, sumsq) over spp samples for a film window (fx0, fy0, w, h)."""
+    def render(self, cam, W, H, spp, max_depth, seed=0, window=None, nthreads=None, integrator="path"):
+        """Per-pixel (sum, sumsq) over spp samples for a film window (fx0, fy0, w, h);
+        integrator "path" (PathIntegrator) or "direct" (DirectLightingIntegrator)."""
         fx0, fy0, w, h = window or (0, 0, W, H)
         cam = np.ascontiguousarray(cam, np.float64)
         s = np.zeros((h, w, 3))
         s2 = np.zeros((h, w, 3))
         nthreads = nthreads or os.cpu_count() or 1
-        self.o.lib.spo_render(self.h, cam, W, H, fx0, fy0, w, h, spp, max_depth, seed, s, s2, nthreads)
+        fn = {"path": self.o.lib.spo_render, "direct": self.o.lib.spo_render_direct}[integrator]
+        fn(self.h, cam, W, H, fx0, fy0, w, h, spp, max_depth, seed, s, s2, nthreads)
         return s, s2

@@ -55,6 +55,11 @@ int spo_trace(spo_scene *s, int any, int64_t n, const double *org, const double 
 int spo_render(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w,
                int h, int spp, int max_depth, uint32_t seed, double *sum, double *sumsq,
                int nthreads);
+/* Same with the direct-lighting integrator
+ * (integrators/directlighting/directlighting.cc:21). */
+int spo_render_direct(spo_scene *s, const double *cam, int W, int H, int fx0, int fy0, int w,
+                      int h, int spp, int max_depth, uint32_t seed, double *sum, double *sumsq,
+                      int nthreads);
 
 /* BSDF of one material in its local frame (z = shading normal).
  * eval: f (n*3) and pdf (n) for (wo, wi) pairs (core/bsdf.cc:49,119).

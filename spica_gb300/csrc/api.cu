@@ -791,8 +791,9 @@ int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_re
         return SPGPU_ESTATE;
     }
     if (d->width <= 0 || d->height <= 0 || d->spp < 0 || d->max_depth < 0 || d->max_depth > 64 ||
+        (d->integrator != SPGPU_INTEGRATOR_PATH && d->integrator != SPGPU_INTEGRATOR_DIRECT) ||
         static_cast<int64_t>(d->width) * d->height > (int64_t(1) << 28)) {
-        setError("spgpu_render: invalid resolution, spp or max_depth");
+        setError("spgpu_render: invalid resolution, spp, max_depth or integrator");
         return SPGPU_EINVAL;
     }
     if (reinterpret_cast<uintptr_t>(film) & 15) {
@@ -804,7 +805,7 @@ int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_re
     unsigned long long st[4] = {0, 0, 0, 0};
     float ms = 0.0f;
     const int rc = renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
-                               reinterpret_cast<float4 *>(film), st, &ms, s);
+                               d->integrator, reinterpret_cast<float4 *>(film), st, &ms, s);
     if (stats) {
         stats->paths = static_cast<int64_t>(st[0]);
         stats->rays_closest = static_cast<int64_t>(st[1]);
@@ -826,8 +827,9 @@ int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
         return SPGPU_ESTATE;
     }
     if (d->width <= 0 || d->height <= 0 || d->spp < 0 || d->max_depth < 0 || d->max_depth > 64 ||
+        (d->integrator != SPGPU_INTEGRATOR_PATH && d->integrator != SPGPU_INTEGRATOR_DIRECT) ||
         (reinterpret_cast<uintptr_t>(film) & 15)) {
-        setError("spgpu_render_profile: invalid resolution, spp, max_depth or film alignment");
+        setError("spgpu_render_profile: invalid resolution, spp, max_depth, integrator or film alignment");
         return SPGPU_EINVAL;
     }
     cudaSetDevice(C.device);
@@ -836,6 +838,7 @@ int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
     long long launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     unsigned long long st[4] = {0, 0, 0, 0}, vis[4] = {0, 0, 0, 0};
     const int rc = renderProfile(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                                 d->integrator,
                                  reinterpret_cast<float4 *>(film), out->kernel_ms, launches, st, vis, s);
     for (int k = 0; k < 8; k++) out->launches[k] = launches[k];
     out->paths = static_cast<int64_t>(st[0]);
@@ -900,8 +903,8 @@ int spgpu_guiding_init(spgpu_ctx *h, const spgpu_guiding_config *cfg) {
 int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, int32_t flags,
                          spgpu_render_stats *stats, void *stream) {
     if (!h || !d || !film || d->width <= 0 || d->height <= 0 || d->spp < 0 || d->max_depth < 0 ||
-        d->max_depth > 12 || (reinterpret_cast<uintptr_t>(film) & 15)) {
-        setError("spgpu_guiding_render: invalid arguments (max_depth <= 12, aligned film)");
+        d->max_depth > 12 || d->integrator != SPGPU_INTEGRATOR_PATH || (reinterpret_cast<uintptr_t>(film) & 15)) {
+        setError("spgpu_guiding_render: invalid arguments (path integrator, max_depth <= 12, aligned film)");
         return SPGPU_EINVAL;
     }
     Ctx &C = h->c;

@@ -262,8 +262,9 @@ int batchPrepare(spgpu_ctx *self, BatchState **slot, int count, const spgpu_batc
         const spgpu_batch_item &it = items[r];
         const spgpu_render_desc &d = it.desc;
         if (it.ntri <= 0 || !it.verts || !it.tri_mat || it.nmat <= 0 || !it.materials || d.width <= 0 ||
-            d.height <= 0 || d.spp <= 0 || d.max_depth < 0 || d.max_depth > 64) {
-            setError("spgpu_batch_prepare: invalid item");
+            d.height <= 0 || d.spp <= 0 || d.max_depth < 0 || d.max_depth > 64 ||
+            d.integrator != SPGPU_INTEGRATOR_PATH) {
+            setError("spgpu_batch_prepare: invalid item (batches take the path integrator)");
             rc = SPGPU_EINVAL;
             break;
         }

@@ -146,11 +146,12 @@ CameraView makeCamera(const float *camera, int width, int height);
 
 // wavefront.cu: trace desc->spp samples per pixel into film (device, float4 per pixel)
 int renderFrame(Ctx *ctx, const float *camera, int width, int height, int spp, int sampleOffset, int maxDepth,
-                uint32_t seed, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream);
+                uint32_t seed, int integrator, float4 *film, unsigned long long *statsOut, float *msOut,
+                cudaStream_t stream);
 // the same samples launched kernel by kernel (no graph), each timed by events, then
 // again with BVH visit counters; kernelMs/launches per kernel class
 int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
-                  float4 *film, double *kernelMs, long long *launches, unsigned long long *statsOut,
+                  int integrator, float4 *film, double *kernelMs, long long *launches, unsigned long long *statsOut,
                   unsigned long long *visitOut, cudaStream_t stream);
 
 }  // namespace spgpu

@@ -58,6 +58,7 @@ struct PassArgs {
                        // [5] / [6] extend / shadow ray-fetch counters
     int *ctl;          // [0] sample index of the pass
     int ctlStride;     // sample-index step from one pass of this queue set to its next
+    int direct;        // direct lighting: no continuation rays after the first hit
     unsigned long long *stats;
     unsigned long long *visit;   // [0..1] extend nodes / triangles, [2..3] shadow nodes / triangles
     int *err;
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
                      static_cast<uint32_t>(fi), sample, fi, R);
             if (!isBlack(R.emit)) filmAdd(p.film, fi, R.emit);
         }
-        const int k = warpAppend(R.cont, nextCnt);
+        const int k = warpAppend(R.cont && !p.direct, nextCnt);
         if (k >= 0) {
             nO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pid));
             nD[k] = R.cD;
@@ -363,7 +364,7 @@ void freeRenderQueues(RenderQueues *q) {
 
 namespace {
 int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int maxDepth, uint32_t seed, float4 *film,
-              int ctlStride, PassArgs *out) {
+              int ctlStride, int integrator, PassArgs *out) {
     const int64_t npix = static_cast<int64_t>(W) * H;
     int rc = ensureQueues(q, npix, maxDepth);
     if (rc) return rc;
@@ -394,6 +395,7 @@ int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int ma
     a.visit = q.stats + 4;
     a.err = q.err;
     a.ctlStride = ctlStride;
+    a.direct = integrator == SPGPU_INTEGRATOR_DIRECT ? 1 : 0;
     return 0;
 }
 
@@ -428,8 +430,10 @@ int ensurePassGraph(Ctx &C, RenderQueues &q, const PassArgs &a, int W, int H, in
 }  // namespace
 
 int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
-                float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
+                int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
     Ctx &C = *ctx;
+    // direct lighting shades the first hit only, with light sampling whatever max_depth says
+    if (integrator == SPGPU_INTEGRATOR_DIRECT) maxDepth = 1;
     // pass lanes in use: one per pass up to the context's setting
     const int lanes = std::max(1, std::min(spp, C.passLanes));
     RenderQueues *qs[Ctx::kPassLanes];
@@ -442,7 +446,7 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
     }
     for (int k = 0; k < lanes; k++) {
         PassArgs a;
-        int rc = setupPass(C, *qs[k], camera, W, H, maxDepth, seed, film, lanes, &a);
+        int rc = setupPass(C, *qs[k], camera, W, H, maxDepth, seed, film, lanes, integrator, &a);
         if (!rc) rc = ensurePassGraph(C, *qs[k], a, W, H, maxDepth, seed, film);
         if (rc) return rc;
     }
@@ -493,12 +497,13 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
 }
 
 int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
-                  float4 *film, double *kernelMs, long long *launches, unsigned long long *statsOut,
+                  int integrator, float4 *film, double *kernelMs, long long *launches, unsigned long long *statsOut,
                   unsigned long long *visitOut, cudaStream_t stream) {
     Ctx &C = *ctx;
     RenderQueues &q = C.rq;
     PassArgs a;
-    int rc = setupPass(C, q, camera, W, H, maxDepth, seed, film, 1, &a);
+    if (integrator == SPGPU_INTEGRATOR_DIRECT) maxDepth = 1;
+    int rc = setupPass(C, q, camera, W, H, maxDepth, seed, film, 1, integrator, &a);
     if (rc) return rc;
     const Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
     const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;

@@ -43,7 +43,7 @@ class TraceCounters(C.Structure):
 class RenderDesc(C.Structure):
     _fields_ = [("camera", C.c_float * 10), ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
                 ("sample_offset", C.c_int32), ("max_depth", C.c_int32), ("seed", C.c_uint32),
-                ("reserved", C.c_int32 * 4)]
+                ("integrator", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class RenderStats(C.Structure):
@@ -315,13 +315,23 @@ class GpuPathIntegrator:
                                                   C.c_void_p(stream) if stream else None), "spgpu_render_profile")
         return pr
 
+    INTEGRATOR = 0   # SPGPU_INTEGRATOR_PATH
+
     def desc(self, camera, W, H, spp, max_depth, sample_offset=0) -> RenderDesc:
         d = RenderDesc()
         for i, v in enumerate(np.asarray(camera, np.float64).reshape(-1)[:10]):
             d.camera[i] = float(v)
         d.width, d.height, d.spp = W, H, spp
         d.sample_offset, d.max_depth, d.seed = sample_offset, max_depth, self.seed & 0xFFFFFFFF
+        d.integrator = self.INTEGRATOR
         return d
+
+
+class GpuDirectLightingIntegrator(GpuPathIntegrator):
+    """DirectLightingIntegrator on the GPU (SPGPU_INTEGRATOR_DIRECT): emission or
+    environment radiance of the camera ray plus one-light NEE at its first hit."""
+
+    INTEGRATOR = 1
 
 
 class GpuBatch:

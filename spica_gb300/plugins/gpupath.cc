@@ -1,7 +1,9 @@
 // gpupath.cc -- reference-side integrator plugin: spica's Integrator interface
 // (core/integrator.h:29-37) backed by the GB300 wavefront path integrator.
 //
-// A drop-in for integrators/path (integrator type="gpupath" in a scene file).  It
+// A drop-in for integrators/path (integrator type="gpupath" in a scene file); built a
+// second time with -DSPGPU_PLUGIN_DIRECT it is the drop-in for
+// integrators/directlighting (type="gpudirect", SPGPU_INTEGRATOR_DIRECT).  It
 // overrides render(camera, scene, params) -- the same call SceneParser makes
 // (spica/sceneparser.cc:105) -- translates the scene through the reference's public
 // interfaces, renders "sampleCount" samples of "maxDepth" bounces on the GPU and
@@ -125,6 +127,11 @@ public:
         d.spp = params.getInt("sampleCount");
         d.max_depth = params.getInt("maxDepth");
         d.seed = seed_;
+#ifdef SPGPU_PLUGIN_DIRECT
+        d.integrator = SPGPU_INTEGRATOR_DIRECT;
+#else
+        d.integrator = SPGPU_INTEGRATOR_PATH;
+#endif
         std::vector<float> pix(static_cast<size_t>(W) * H * 4, 0.0f);
         spgpu_render_stats st;
         check(spgpu_render_host(ctx, &d, pix.data(), &st));
@@ -195,5 +202,9 @@ extern "C" {
 spica::CObject *createInstance(spica::RenderParams &params) {
     return (spica::CObject *)(new spica::GpuPathIntegrator(params));
 }
+#ifdef SPGPU_PLUGIN_DIRECT
+const char *getDescription() { return "GB300 wavefront direct-lighting integrator"; }
+#else
 const char *getDescription() { return "GB300 wavefront path integrator"; }
+#endif
 }

@@ -119,7 +119,21 @@ def main():
     np.savez_compressed(os.path.join(HERE, "render_envscene.npz"), sum=S, sumsq=S2, spp=es.spp, seed=13,
                         W=es.width, H=es.height, max_depth=es.max_depth, camera=es.camera, verts=es.verts,
                         tri_mat=es.tri_mat, materials=es.materials, tri_emit=es.tri_emit, env=es.env)
+    direct_renders(ref)
     print(f"golden fixtures written in {time.time() - t0:.1f} s")
+
+
+def direct_renders(ref):
+    """6. the direct-lighting integrator on the same two scenes"""
+    sc = scenes.box_room(width=48, height=48, spp=1024)
+    S, S2 = ref.scene(sc).render(sc.camera, 48, 48, 1024, 8, seed=17, integrator="direct")
+    np.savez_compressed(os.path.join(HERE, "render_direct_boxroom.npz"), sum=S, sumsq=S2, spp=1024, seed=17, W=48,
+                        H=48, max_depth=8, camera=sc.camera)
+    es = env_scene()
+    S, S2 = ref.scene(es).render(es.camera, es.width, es.height, es.spp, es.max_depth, seed=19, integrator="direct")
+    np.savez_compressed(os.path.join(HERE, "render_direct_envscene.npz"), sum=S, sumsq=S2, spp=es.spp, seed=19,
+                        W=es.width, H=es.height, max_depth=es.max_depth, camera=es.camera, verts=es.verts,
+                        tri_mat=es.tri_mat, materials=es.materials, tri_emit=es.tri_emit, env=es.env)
 
 
 if __name__ == "__main__":

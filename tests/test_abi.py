@@ -78,7 +78,7 @@ def test_reference_side_plugins_compile_and_export():
     d = os.path.join(ROOT, "spica_gb300", "plugins")
     r = subprocess.run(["make", "-C", d, f"REF={spo.REF_TREE}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    for name in ("gpubvh", "gpupath"):
+    for name in ("gpubvh", "gpupath", "gpudirect"):
         so = os.path.join(d, "_build", name + ".so")
         syms = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
         assert " createInstance" in syms and " getDescription" in syms, name

@@ -72,19 +72,23 @@ def test_bsdf_tables_match_reference_golden(port):
         assert np.array_equal(st, g[f"stype{k}"])
 
 
-@pytest.mark.parametrize("name", ["render_boxroom", "render_envscene"])
+@pytest.mark.parametrize("name", ["render_boxroom", "render_envscene", "render_direct_boxroom",
+                                  "render_direct_envscene"])
 def test_render_matches_reference_golden(port, name):
     """Same per-pixel sampler streams => the restatement reproduces the reference's
     per-pixel sums (exactly on the host that made the fixture; libm differences in
-    the last ulp may flip rare decisions elsewhere, hence the fraction bound)."""
+    the last ulp may flip rare decisions elsewhere, hence the fraction bound), for the
+    path and the direct-lighting integrators."""
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
-    if name == "render_boxroom":
+    integrator = "direct" if "direct" in name else "path"
+    if "boxroom" in name:
         sc = scenes.box_room(width=int(g["W"]), height=int(g["H"]))
     else:
         sc = _scene_from(g)
     o = port.scene(sc)
     spp = 64   # a prefix of the fixture's samples is not comparable; render the full count
-    S, S2 = o.render(g["camera"], int(g["W"]), int(g["H"]), int(g["spp"]), int(g["max_depth"]), seed=int(g["seed"]))
+    S, S2 = o.render(g["camera"], int(g["W"]), int(g["H"]), int(g["spp"]), int(g["max_depth"]), seed=int(g["seed"]),
+                     integrator=integrator)
     rel = np.abs(S - g["sum"]) / np.maximum(np.abs(g["sum"]), 1e-12)
     assert (rel.max(axis=2) > 1e-9).mean() < 0.02
     assert abs(S.mean() - g["sum"].mean()) <= 1e-3 * g["sum"].mean()
@@ -106,6 +110,10 @@ def test_port_equals_compiled_reference(port, ref):
     Sa, _ = ref.scene(sc).render(sc.camera, 24, 16, 4, 12, seed=3)
     Sb, _ = port.scene(sc).render(sc.camera, 24, 16, 4, 12, seed=3)
     assert np.array_equal(Sa, Sb)
+    for md in (1, 8):   # direct lighting, with and without the (never taken) specular recursion
+        Sa, _ = ref.scene(sc).render(sc.camera, 24, 16, 4, md, seed=5, integrator="direct")
+        Sb, _ = port.scene(sc).render(sc.camera, 24, 16, 4, md, seed=5, integrator="direct")
+        assert np.array_equal(Sa, Sb)
 
 
 def test_port_qbvh_variant_of_reference_agrees(ref):

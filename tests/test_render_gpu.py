@@ -9,6 +9,7 @@ import pytest
 from conftest import GOLDEN
 from parity import zscores
 from spica_gb300 import GpuBVHAccel, GpuPathIntegrator, scenes
+from spica_gb300.gpu import GpuDirectLightingIntegrator
 
 pytestmark = pytest.mark.gpu
 
@@ -24,9 +25,9 @@ def _scene_from(g):
     return s
 
 
-def gpu_batches(accel, camera, W, H, max_depth, batches, spp, seed=1):
+def gpu_batches(accel, camera, W, H, max_depth, batches, spp, seed=1, integrator=GpuPathIntegrator):
     """Independent batch means -> per-pixel mean and variance of the mean."""
-    integ = GpuPathIntegrator(seed=seed)
+    integ = integrator(seed=seed)
     means = []
     for k in range(batches):
         film = integ.render(camera, accel, {"width": W, "height": H, "maxDepth": max_depth, "sampleCount": spp},
@@ -44,13 +45,16 @@ def ref_moments(g):
     return mean, var
 
 
-@pytest.mark.parametrize("name", ["render_boxroom", "render_envscene"])
+@pytest.mark.parametrize("name", ["render_boxroom", "render_envscene", "render_direct_boxroom",
+                                  "render_direct_envscene"])
 def test_matches_reference_render(gpulib, name):
+    """Path integrator and direct-lighting integrator against the reference's renders."""
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     W, H, md = int(g["W"]), int(g["H"]), int(g["max_depth"])
-    sc = scenes.box_room(width=W, height=H) if name == "render_boxroom" else _scene_from(g)
+    sc = scenes.box_room(width=W, height=H) if "boxroom" in name else _scene_from(g)
     acc = GpuBVHAccel(sc).construct()
-    mg, vg = gpu_batches(acc, g["camera"], W, H, md, batches=16, spp=512)
+    integ = GpuDirectLightingIntegrator if "direct" in name else GpuPathIntegrator
+    mg, vg = gpu_batches(acc, g["camera"], W, H, md, batches=16, spp=512, integrator=integ)
     mr, vr = ref_moments(g)
     z = zscores(mg, vg, mr, vr)
     frac = float((np.abs(z) > 3).mean())
