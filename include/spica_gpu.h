@@ -245,6 +245,31 @@ int spgpu_guiding_mlp(spgpu_ctx *ctx, const float *features, int32_t n, float *r
  * grad: 11560 floats) */
 int spgpu_guiding_grad(spgpu_ctx *ctx, const float *samples, int32_t n, float *grad, double *loss, void *stream);
 
+/* ---- film output -------------------------------------------------------------
+ * Resolve of an accumulated film (device, W*H float4 of sum of L and sample weight,
+ * film pixel order) into an output encoding, on the device:
+ *   SPGPU_FILM_RGBE         out = W*H*4 bytes: the reference's HDRPixel (R, G, B, E)
+ *                           of sum / (weight + 1e-12) -- Film::save (core/film.cc:23-30)
+ *                           then Image::saveHdr's per-pixel encoding (core/image.cc:72-88)
+ *   SPGPU_FILM_GAMMA_BYTES  out = W*H*3 bytes: GammaTmo(param = gamma) then
+ *                           Image::toByte -- LDRFilm::saveImage (films/ldrfilm.cc:25-31,
+ *                           core/tmo.cc:53, core/image.cc:476)
+ *   SPGPU_FILM_REINHARD     out = W*H*3 floats: ReinhardTmo(param = alpha)::apply of the
+ *                           resolved image (core/tmo.cc:81-124)
+ * Blocking on `stream`. */
+#define SPGPU_FILM_RGBE 0
+#define SPGPU_FILM_GAMMA_BYTES 1
+#define SPGPU_FILM_REINHARD 2
+int spgpu_film_resolve(spgpu_ctx *ctx, const float *film, int32_t width, int32_t height, int32_t format,
+                       double param, void *out, void *stream);
+/* Host-side writers.  spgpu_write_hdr writes W*H RGBE pixels in the byte layout of the
+ * reference's Image::saveHdr (core/image.cc:390-434: Radiance header, per scanline the
+ * (2, 2, width) marker and each channel as literal runs of <= 127 bytes);
+ * spgpu_write_png writes W*H 8-bit RGB pixels as a PNG (stored deflate blocks; the
+ * reference's savePng goes through an image library, core/image.cc:459). */
+int spgpu_write_hdr(const char *path, const uint8_t *rgbe, int32_t width, int32_t height);
+int spgpu_write_png(const char *path, const uint8_t *rgb, int32_t width, int32_t height);
+
 /* Profiling (no counterpart in the reference, which has only a progress printf,
  * core/integrator.cc:92-96): the same samples as spgpu_render, launched kernel by
  * kernel without the graph and timed with CUDA events on `stream`, then repeated

@@ -27,6 +27,7 @@
 #include "core/constant.h"
 #include "core/bsphere.h"
 #include "core/image.h"
+#include "core/tmo.h"
 #include "core/interaction.h"
 #include "core/bsdf.h"
 #include "core/bxdf.h"
@@ -329,4 +330,53 @@ int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double
     return 0;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------- film output
+namespace {
+// Film::save's resolve (core/film.cc:25-28) of a W x H film of float4 (sum, weight)
+Image resolveFilm(const float *film, int W, int H) {
+    Image img(W, H);
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            const float *f = film + 4 * (static_cast<size_t>(y) * W + x);
+            img.pixel(x, y) = RGBSpectrum(f[0], f[1], f[2]);
+            img.pixel(x, y) /= (static_cast<double>(f[3]) + EPS);
+        }
+    return img;
+}
+}  // namespace
+
+extern "C" {
+int spo_film_save_hdr(const float *film, int W, int H, const char *path) {
+    resolveFilm(film, W, H).save(path);   // Image::save -> saveHdr (core/image.cc:199,390)
+    return 0;
+}
+
+int spo_film_gamma(const float *film, int W, int H, double gamma, uint8_t *out) {
+    const Image g = GammaTmo(gamma).apply(resolveFilm(film, W, H));
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            const RGBSpectrum &c = g(x, y);
+            const double v[3] = {c.red(), c.green(), c.blue()};
+            for (int k = 0; k < 3; k++) {   // Image::toByte (core/image.cc:476)
+                const double d = std::max(0.0, std::min(v[k], 1.0));
+                out[3 * (static_cast<size_t>(y) * W + x) + k] = static_cast<uint8_t>(255.0 * d);
+            }
+        }
+    return 0;
+}
+
+int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out) {
+    const Image r = ReinhardTmo(alpha).apply(resolveFilm(film, W, H));
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            const RGBSpectrum &c = r(x, y);
+            double *o = out + 3 * (static_cast<size_t>(y) * W + x);
+            o[0] = c.red();
+            o[1] = c.green();
+            o[2] = c.blue();
+        }
+    return 0;
+}
 }  // extern "C"

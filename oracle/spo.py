@@ -105,6 +105,32 @@ class Oracle:
         self.lib.spo_bsdf_sample(mat, n, wo, u, wi, f, pdf, typ)
         return wi, f, pdf, typ
 
+    # ---------------------------------------------------------------- film output
+    # (compiled reference only: the restatement does not carry the image code)
+    def _film(self, film):
+        film = np.ascontiguousarray(film, np.float32)
+        H, W = film.shape[:2]
+        return film, W, H
+
+    def film_save_hdr(self, film, path):
+        film, W, H = self._film(film)
+        self.lib.spo_film_save_hdr.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_char_p]
+        self.lib.spo_film_save_hdr(film.ctypes.data, W, H, str(path).encode())
+
+    def film_gamma(self, film, gamma):
+        film, W, H = self._film(film)
+        out = np.zeros((H, W, 3), np.uint8)
+        self.lib.spo_film_gamma.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p]
+        self.lib.spo_film_gamma(film.ctypes.data, W, H, gamma, out.ctypes.data)
+        return out
+
+    def film_reinhard(self, film, alpha):
+        film, W, H = self._film(film)
+        out = np.zeros((H, W, 3), np.float64)
+        self.lib.spo_film_reinhard.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p]
+        self.lib.spo_film_reinhard(film.ctypes.data, W, H, alpha, out.ctypes.data)
+        return out
+
 
 class OracleScene:
     """A scene held by one oracle library (see spica_gb300.scenes.Scene for the layout)."""

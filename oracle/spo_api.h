@@ -71,6 +71,15 @@ int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double
 
 const char *spo_name(void);
 
+/* Film output through the reference (compiled reference only): a W x H film of float4
+ * (sum of L, weight) resolved as Film::save does (core/film.cc:25-28), then
+ *   spo_film_save_hdr  Image::save to a .hdr path (core/image.cc:390)
+ *   spo_film_gamma     GammaTmo(gamma) and Image::toByte: W*H*3 bytes (core/tmo.cc:53)
+ *   spo_film_reinhard  ReinhardTmo(alpha)::apply: W*H*3 doubles (core/tmo.cc:81) */
+int spo_film_save_hdr(const float *film, int W, int H, const char *path);
+int spo_film_gamma(const float *film, int W, int H, double gamma, uint8_t *out);
+int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out);
+
 /* per-pixel sampler seed: splitmix-style mix of (seed, pixel) folded to 32 bits */
 static inline uint32_t spo_pixel_seed(uint32_t seed, uint32_t pixel) {
     uint64_t z = ((uint64_t)seed << 32) ^ (uint64_t)pixel;

@@ -979,6 +979,36 @@ int spgpu_guiding_grad(spgpu_ctx *h, const float *samples, int32_t n, float *gra
     return guideGrad(h->c, *h->c.guide, samples, n, grad, loss, static_cast<cudaStream_t>(stream), false);
 }
 
+int spgpu_film_resolve(spgpu_ctx *h, const float *film, int32_t width, int32_t height, int32_t format,
+                       double param, void *out, void *stream) {
+    if (!h || !film || !out || width <= 0 || height <= 0 || static_cast<int64_t>(width) * height > (int64_t(1) << 28) ||
+        format < SPGPU_FILM_RGBE || format > SPGPU_FILM_REINHARD ||
+        (format != SPGPU_FILM_RGBE && !(param > 0.0)) || (reinterpret_cast<uintptr_t>(film) & 15) ||
+        (format != SPGPU_FILM_GAMMA_BYTES && (reinterpret_cast<uintptr_t>(out) & 3))) {
+        setError("spgpu_film_resolve: invalid arguments (16-byte aligned film, 4-byte aligned RGBE or float "
+                 "output, known format, param > 0)");
+        return SPGPU_EINVAL;
+    }
+    cudaSetDevice(h->c.device);
+    return filmResolve(h->c, film, width, height, format, param, out, static_cast<cudaStream_t>(stream));
+}
+
+int spgpu_write_hdr(const char *path, const uint8_t *rgbe, int32_t width, int32_t height) {
+    if (!path || !rgbe || width <= 0 || height <= 0 || width > 0x7FFF) {
+        setError("spgpu_write_hdr: invalid arguments (scanline width < 32768)");
+        return SPGPU_EINVAL;
+    }
+    return writeHdr(path, rgbe, width, height);
+}
+
+int spgpu_write_png(const char *path, const uint8_t *rgb, int32_t width, int32_t height) {
+    if (!path || !rgb || width <= 0 || height <= 0) {
+        setError("spgpu_write_png: invalid arguments");
+        return SPGPU_EINVAL;
+    }
+    return writePng(path, rgb, width, height);
+}
+
 int spgpu_render_host(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_render_stats *stats) {
     if (!h || !d || !film) {
         setError("spgpu_render_host: invalid arguments");

@@ -178,4 +178,9 @@ int guideRing(const GuideState &G, float *dst, int maxSamples, int *count);
 int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film, int flags,
                 unsigned long long *statsOut, float *msOut, cudaStream_t s);
 long long guideSamples(const GuideState &G);
+
+// film output (film.cu)
+int filmResolve(Ctx &C, const float *film, int W, int H, int format, double param, void *out, cudaStream_t s);
+int writeHdr(const char *path, const uint8_t *rgbe, int W, int H);
+int writePng(const char *path, const uint8_t *rgb, int W, int H);
 }  // namespace spgpu

@@ -76,6 +76,39 @@ class GuidingConfig(C.Structure):
 
 
 GUIDE_GUIDED, GUIDE_COLLECT = 1, 2
+FILM_RGBE, FILM_GAMMA_BYTES, FILM_REINHARD = 0, 1, 2
+
+
+def film_resolve(ctx: "Context", film_dev, fmt: int, param: float = 0.0, stream: int = 0):
+    """spgpu_film_resolve of a device film (torch (H, W, 4) float32): RGBE bytes (H, W, 4),
+    gamma-corrected bytes (H, W, 3) or a Reinhard-mapped image (H, W, 3) float32, on the
+    device."""
+    import torch
+    H, W = int(film_dev.shape[0]), int(film_dev.shape[1])
+    if fmt == FILM_RGBE:
+        out = torch.empty((H, W, 4), dtype=torch.uint8, device=film_dev.device)
+    elif fmt == FILM_GAMMA_BYTES:
+        out = torch.empty((H, W, 3), dtype=torch.uint8, device=film_dev.device)
+    else:
+        out = torch.empty((H, W, 3), dtype=torch.float32, device=film_dev.device)
+    _check(ctx.lib.spgpu_film_resolve(ctx.h, _ptr(film_dev), W, H, fmt, float(param), _ptr(out),
+                                      C.c_void_p(stream) if stream else None), "spgpu_film_resolve")
+    return out
+
+
+def write_hdr(path: str, rgbe) -> None:
+    """spgpu_write_hdr: (H, W, 4) uint8 RGBE pixels to a Radiance .hdr file laid out as
+    the reference's Image::saveHdr writes it."""
+    a = np.ascontiguousarray(rgbe, np.uint8)
+    _check(load_library().spgpu_write_hdr(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0]),
+           "spgpu_write_hdr")
+
+
+def write_png(path: str, rgb) -> None:
+    """spgpu_write_png: (H, W, 3) uint8 pixels to an 8-bit RGB PNG."""
+    a = np.ascontiguousarray(rgb, np.uint8)
+    _check(load_library().spgpu_write_png(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0]),
+           "spgpu_write_png")
 GUIDE_PARAMS = 11560
 
 
@@ -86,7 +119,7 @@ class Config(C.Structure):
 # every extern "C" symbol include/spica_gpu.h declares
 EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version", "spgpu_upload_scene",
            "spgpu_build_bvh", "spgpu_bvh_stats", "spgpu_trace", "spgpu_trace_host", "spgpu_trace_stats",
-           "spgpu_trace_host_noalloc",
+           "spgpu_trace_host_noalloc", "spgpu_film_resolve", "spgpu_write_hdr", "spgpu_write_png",
            "spgpu_render", "spgpu_render_host", "spgpu_render_profile", "spgpu_batch_prepare",
            "spgpu_batch_film_pixels", "spgpu_batch_run", "spgpu_guiding_init", "spgpu_guiding_render",
            "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_ring", "spgpu_guiding_params", "spgpu_guiding_mlp",
@@ -116,6 +149,9 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_trace.argtypes = [vp, C.c_int, vp, vp, i64, vp, vp]
     lib.spgpu_trace_host.argtypes = [vp, C.c_int, vp, vp, i64, vp]
     lib.spgpu_trace_host_noalloc.argtypes = [vp, C.c_int, vp, vp, i64, vp]
+    lib.spgpu_film_resolve.argtypes = [vp, vp, i32, i32, i32, C.c_double, vp, vp]
+    lib.spgpu_write_hdr.argtypes = [C.c_char_p, vp, i32, i32]
+    lib.spgpu_write_png.argtypes = [C.c_char_p, vp, i32, i32]
     lib.spgpu_trace_stats.argtypes = [vp, C.c_int, vp, vp, i64, vp, C.POINTER(TraceCounters)]
     lib.spgpu_render.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats), vp]
     lib.spgpu_render_host.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats)]

@@ -120,6 +120,7 @@ def main():
                         W=es.width, H=es.height, max_depth=es.max_depth, camera=es.camera, verts=es.verts,
                         tri_mat=es.tri_mat, materials=es.materials, tri_emit=es.tri_emit, env=es.env)
     direct_renders(ref)
+    film_outputs(ref)
     print(f"golden fixtures written in {time.time() - t0:.1f} s")
 
 
@@ -138,3 +139,28 @@ def direct_renders(ref):
 
 if __name__ == "__main__":
     main()
+
+
+def film_input(W=131, H=37, seed=11):
+    """A float film (sum of L, sample weight) covering the encoders' cases: zero and
+    tiny pixels, values up to 1e6, unit and fractional weights, 131 columns so that an
+    RGBE scanline needs two literal runs."""
+    rng = np.random.default_rng(seed)
+    w = rng.integers(1, 300, (H, W)).astype(np.float32)
+    L = (10.0 ** rng.uniform(-6, 3, (H, W, 3))) * w[..., None]
+    L[rng.random((H, W)) < 0.05] = 0.0
+    L[0, :5] = [[1e-35, 1e-35, 1e-35], [1e6, 1e6, 1e6], [0, 0, 1], [1, 0, 0], [0.5, 0.25, 0.125]]
+    w[0, :5] = 1.0
+    return np.concatenate([L, w[..., None]], -1).astype(np.float32)
+
+
+def film_outputs(ref):
+    """7. film output: the reference's .hdr bytes, gamma 2.2 bytes and Reinhard image"""
+    import tempfile
+    film = film_input()
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "film.hdr")
+        ref.film_save_hdr(film, path)
+        hdr = np.frombuffer(open(path, "rb").read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "film_output.npz"), film=film, hdr=hdr,
+                        gamma22=ref.film_gamma(film, 2.2), reinhard=ref.film_reinhard(film, 0.18))
