@@ -219,8 +219,15 @@ typedef struct {
     int32_t batch;         /* training samples per Adam step (0: 16384) */
     uint32_t seed;         /* weight initialisation */
     int32_t capacity;      /* training-sample ring size (0: 2^21) */
-    int32_t reserved[3];
+    int32_t fault_injection; /* tests only: SPGPU_GUIDE_FAULT_WAIT makes spgpu_guiding_mlp's
+                              * tensor-core completion wait run out (no MMA is issued, so
+                              * the barrier is never signalled; the wait is cut to 1024
+                              * polls); the call then returns SPGPU_EKERNEL and the context
+                              * stays usable.  0 otherwise. */
+    int32_t reserved[2];
 } spgpu_guiding_config;
+
+#define SPGPU_GUIDE_FAULT_WAIT 1
 
 #define SPGPU_GUIDE_GUIDED 1   /* sample with the network mixture */
 #define SPGPU_GUIDE_COLLECT 2  /* record training samples */

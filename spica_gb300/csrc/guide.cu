@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
 __global__ void __launch_bounds__(kGTile, 1) k_guide_forward(const uint8_t *__restrict__ packFwd,
                                                              const float *__restrict__ biasPad,
                                                              const float *__restrict__ feat, int n, float *out,
-                                                             int *err) {
+                                                             int *err, int faultWait) {
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t *wf = sm;
     float *bias = reinterpret_cast<float *>(sm + kPackFwdBytes);
@@ -305,7 +305,10 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_forward(const uint8_t *__re
         for (int i = 0; i < 16; i++) xf[i] = (s < n && i < kGIn) ? feat[9 * static_cast<int64_t>(s) + i] : 0.0f;
         storeRow8(x, t, 0, kGK0, xf);
         storeRow8(x, t, 8, kGK0, xf + 8);
-        ok = mlpForwardTile(tmem, wf, bias, x, h, h, h, o, 41, bar, phase);
+        if (faultWait)   // fault injection: nothing arrives on the barrier, the short wait runs out
+            ok = tileMma(tmem, x, wf, kGK0, kGHid, bar, phase, true, 1024u);
+        else
+            ok = mlpForwardTile(tmem, wf, bias, x, h, h, h, o, 41, bar, phase);
         if (ok && s < n)
             for (int j = 0; j < kGOut; j++) out[kGOut * static_cast<int64_t>(s) + j] = o[t * 41 + j];
         __syncthreads();
@@ -925,7 +928,8 @@ int guideForward(Ctx &C, GuideState &G, const float *feat, int n, float *out, cu
     const int tiles = (n + kGTile - 1) / kGTile;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
-    k_guide_forward<<<std::min(tiles, sms), kGTile, kForwardSmem, s>>>(G.packFwd, G.biasPad, feat, n, out, G.ctl + 1);
+    k_guide_forward<<<std::min(tiles, sms), kGTile, kForwardSmem, s>>>(G.packFwd, G.biasPad, feat, n, out, G.ctl + 1,
+                                                                       G.cfg.fault_injection == SPGPU_GUIDE_FAULT_WAIT);
     int err = 0;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&err, G.ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s);

@@ -132,12 +132,15 @@ __device__ __forceinline__ float loadBf16(const uint8_t *tile, uint32_t r, uint3
 // D = A x B over K (multiple of 16), issued by thread 0; returns once the tensor core
 // is done (all threads wait on the barrier).  Returns false on a timed-out wait (the
 // CTA-wide result is uniform).
+// withhold = true (fault injection in tests) issues nothing, so the barrier is never
+// signalled and the bounded wait of maxTries polls runs out.
 __device__ __forceinline__ bool tileMma(uint32_t tmem, const uint8_t *a, const uint8_t *b, uint32_t K, uint32_t N,
-                                        uint64_t *bar, uint32_t &phase) {
+                                        uint64_t *bar, uint32_t &phase, bool withhold = false,
+                                        uint32_t maxTries = kMmaWaitTries) {
     tc::fenceBeforeSync();
     tc::fenceAsyncShared();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !withhold) {
         tc::fenceAfterSync();
         const uint32_t sbo = (K / 8) * 128;
         const uint32_t idesc = tc::instrDescBf16(128, N);
@@ -147,7 +150,7 @@ __device__ __forceinline__ bool tileMma(uint32_t tmem, const uint8_t *a, const u
                         j > 0 ? 1u : 0u);
         tc::mmaCommit(bar);
     }
-    const bool ok = tc::mbarWait(bar, phase, kMmaWaitTries);
+    const bool ok = tc::mbarWait(bar, phase, maxTries);
     phase ^= 1u;
     const bool allOk = __syncthreads_and(ok) != 0;
     tc::fenceAfterSync();
