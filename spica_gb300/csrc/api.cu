@@ -519,6 +519,7 @@ void spgpu_destroy(spgpu_ctx *h) {
 
 int spgpu_upload_scene(spgpu_ctx *h, int32_t ntri, const float *verts, const int32_t *tri_mat, int32_t nmat,
                        const float *materials, const float *tri_emit, int32_t env_w, int32_t env_h, const float *env) {
+    NvtxRange nvtxRange("spgpu_upload_scene");
     if (!h || ntri <= 0 || !verts || !tri_mat || nmat <= 0 || !materials || (env && (env_w <= 0 || env_h <= 0))) {
         setError("spgpu_upload_scene: invalid arguments");
         return SPGPU_EINVAL;
@@ -614,6 +615,7 @@ int spgpu_upload_scene(spgpu_ctx *h, int32_t ntri, const float *verts, const int
 }
 
 int spgpu_build_bvh(spgpu_ctx *h) {
+    NvtxRange nvtxRange("spgpu_build_bvh");
     if (!h) return SPGPU_EINVAL;
     Ctx &C = h->c;
     if (!C.sceneReady) {
@@ -665,6 +667,7 @@ int spgpu_bvh_stats(spgpu_ctx *h, spgpu_bvh_info *out) {
 
 int spgpu_trace(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out,
                 void *stream) {
+    NvtxRange nvtxRange("spgpu_trace");
     if (!h) return SPGPU_EINVAL;
     Ctx &C = h->c;
     cudaSetDevice(C.device);
@@ -673,6 +676,7 @@ int spgpu_trace(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *d
 
 int spgpu_trace_stats(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out,
                       spgpu_trace_counters *counters) {
+    NvtxRange nvtxRange("spgpu_trace_stats");
     if (!h || !counters) return SPGPU_EINVAL;
     Ctx &C = h->c;
     cudaSetDevice(C.device);
@@ -691,6 +695,7 @@ int spgpu_trace_stats(spgpu_ctx *h, int any_hit, const float *org_tmin, const fl
 }
 
 int spgpu_trace_host(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out) {
+    NvtxRange nvtxRange("spgpu_trace_host");
     if (!h) return SPGPU_EINVAL;
     Ctx &C = h->c;
     if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
@@ -724,6 +729,7 @@ int spgpu_trace_host(spgpu_ctx *h, int any_hit, const float *org_tmin, const flo
 
 int spgpu_trace_host_noalloc(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
                              void *out) {
+    NvtxRange nvtxRange("spgpu_trace_host_noalloc");
     if (!h) return SPGPU_EINVAL;
     Ctx &C = h->c;
     if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
@@ -781,6 +787,7 @@ int spgpu_trace_host_noalloc(spgpu_ctx *h, int any_hit, const float *org_tmin, c
 }
 
 int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_render_stats *stats, void *stream) {
+    NvtxRange nvtxRange("spgpu_render");
     if (!h || !d || !film) {
         setError("spgpu_render: invalid arguments");
         return SPGPU_EINVAL;
@@ -817,6 +824,7 @@ int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_re
 
 int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_kernel_profile *out,
                          void *stream) {
+    NvtxRange nvtxRange("spgpu_render_profile");
     if (!h || !d || !film || !out) {
         setError("spgpu_render_profile: invalid arguments");
         return SPGPU_EINVAL;
@@ -853,6 +861,7 @@ int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
 
 int spgpu_batch_prepare(spgpu_ctx *h, int32_t count, const spgpu_batch_item *items, int32_t autotune,
                         spgpu_batch_tuning *tuning) {
+    NvtxRange nvtxRange("spgpu_batch_prepare");
     if (!h || count <= 0 || !items) {
         setError("spgpu_batch_prepare: invalid arguments");
         return SPGPU_EINVAL;
@@ -864,6 +873,7 @@ int spgpu_batch_prepare(spgpu_ctx *h, int32_t count, const spgpu_batch_item *ite
 int64_t spgpu_batch_film_pixels(spgpu_ctx *h) { return h && h->c.batch ? batchPixels(*h->c.batch) : -1; }
 
 int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_stats *stats, void *stream) {
+    NvtxRange nvtxRange("spgpu_batch_run");
     if (!h || !films || !render_ms) {
         setError("spgpu_batch_run: invalid arguments");
         return SPGPU_EINVAL;
@@ -892,6 +902,7 @@ int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_
 }
 
 int spgpu_guiding_init(spgpu_ctx *h, const spgpu_guiding_config *cfg) {
+    NvtxRange nvtxRange("spgpu_guiding_init");
     if (!h || !cfg) {
         setError("spgpu_guiding_init: invalid arguments");
         return SPGPU_EINVAL;
@@ -902,6 +913,7 @@ int spgpu_guiding_init(spgpu_ctx *h, const spgpu_guiding_config *cfg) {
 
 int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, int32_t flags,
                          spgpu_render_stats *stats, void *stream) {
+    NvtxRange nvtxRange("spgpu_guiding_render");
     if (!h || !d || !film || d->width <= 0 || d->height <= 0 || d->spp < 0 || d->max_depth < 0 ||
         d->max_depth > 12 || d->integrator != SPGPU_INTEGRATOR_PATH || (reinterpret_cast<uintptr_t>(film) & 15)) {
         setError("spgpu_guiding_render: invalid arguments (path integrator, max_depth <= 12, aligned film)");
@@ -931,6 +943,7 @@ int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
 }
 
 int spgpu_guiding_train(spgpu_ctx *h, int32_t steps, double *mean_loss) {
+    NvtxRange nvtxRange("spgpu_guiding_train");
     if (!h || steps < 0) return SPGPU_EINVAL;
     if (!h->c.guide) {
         setError("spgpu_guiding_train: call spgpu_guiding_init first");
@@ -961,6 +974,7 @@ int spgpu_guiding_params(spgpu_ctx *h, float *params, int32_t set) {
 }
 
 int spgpu_guiding_mlp(spgpu_ctx *h, const float *features, int32_t n, float *raw, void *stream) {
+    NvtxRange nvtxRange("spgpu_guiding_mlp");
     if (!h || !h->c.guide || n < 0 || (n > 0 && (!features || !raw))) {
         setError("spgpu_guiding_mlp: invalid arguments or no guiding state");
         return SPGPU_EINVAL;
@@ -971,6 +985,7 @@ int spgpu_guiding_mlp(spgpu_ctx *h, const float *features, int32_t n, float *raw
 }
 
 int spgpu_guiding_grad(spgpu_ctx *h, const float *samples, int32_t n, float *grad, double *loss, void *stream) {
+    NvtxRange nvtxRange("spgpu_guiding_grad");
     if (!h || !h->c.guide || n <= 0 || !samples || !grad) {
         setError("spgpu_guiding_grad: invalid arguments or no guiding state");
         return SPGPU_EINVAL;
@@ -981,6 +996,7 @@ int spgpu_guiding_grad(spgpu_ctx *h, const float *samples, int32_t n, float *gra
 
 int spgpu_film_resolve(spgpu_ctx *h, const float *film, int32_t width, int32_t height, int32_t format,
                        double param, void *out, void *stream) {
+    NvtxRange nvtxRange("spgpu_film_resolve");
     if (!h || !film || !out || width <= 0 || height <= 0 || static_cast<int64_t>(width) * height > (int64_t(1) << 28) ||
         format < SPGPU_FILM_RGBE || format > SPGPU_FILM_REINHARD ||
         (format != SPGPU_FILM_RGBE && !(param > 0.0)) || (reinterpret_cast<uintptr_t>(film) & 15) ||
@@ -1010,6 +1026,7 @@ int spgpu_write_png(const char *path, const uint8_t *rgb, int32_t width, int32_t
 }
 
 int spgpu_render_host(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_render_stats *stats) {
+    NvtxRange nvtxRange("spgpu_render_host");
     if (!h || !d || !film) {
         setError("spgpu_render_host: invalid arguments");
         return SPGPU_EINVAL;

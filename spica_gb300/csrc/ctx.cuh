@@ -4,6 +4,8 @@
 
 #include <cstdint>
 #include <string>
+
+#include <nvtx3/nvToolsExt.h>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -130,6 +132,15 @@ struct Ctx {
         v.env = env;
         return v;
     }
+};
+
+// NVTX range over a host API call (visible in Nsight Systems timelines; a no-op
+// without a profiler attached)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
 };
 
 void setError(const std::string &msg);
