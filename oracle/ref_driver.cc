@@ -44,6 +44,8 @@
 
 #include "accelerators/bvh.h"
 #include "bsdfs/dielectric.h"
+#include "bsdfs/plastic.h"
+#include "bsdfs/roughdielectric.h"
 #include "bsdfs/diffuse.h"
 #include "bsdfs/roughconductor.h"
 #include "cameras/perspective.h"
@@ -84,6 +86,16 @@ std::shared_ptr<SurfaceMaterial> makeSurface(const double *m) {
                                                 constTex(Spectrum(m[5], m[6], m[7])),
                                                 alpha, alpha, "ggx", nullptr, false);
     }
+    if (type == SPO_MAT_ROUGH_DIELECTRIC) {
+        auto alpha = constTex(Spectrum(m[1]));
+        return std::make_shared<RoughDielectric>(constTex(Spectrum(1.0)), constTex(Spectrum(1.0)), alpha, alpha,
+                                                 constTex(Spectrum(m[2])), m[3] != 0.0 ? "ggx" : "beckmann",
+                                                 nullptr, false);
+    }
+    if (type == SPO_MAT_PLASTIC) {
+        return std::make_shared<Plastic>(constTex(Spectrum(m[1], m[2], m[3])), constTex(Spectrum(m[4], m[5], m[6])),
+                                         constTex(Spectrum(m[7])), nullptr);
+    }
     return std::make_shared<Dielectric>(constTex(Spectrum(1.0)), constTex(Spectrum(1.0)),
                                         constTex(Spectrum(m[1])), nullptr);
 }
@@ -111,7 +123,13 @@ public:
 template <class F>
 void parallelRange(int64_t n, int nthreads, int64_t chunk, F &&body) {
     if (nthreads <= 1) {
-        for (int64_t i = 0; i < n; i += chunk) body(i, std::min(n, i + chunk));
+        // one fresh thread: the BxDFs' hidden thread_local generators (core/bxdf.cc:18,
+        // bsdfs/plastic.cc:18) start from their seed, so single-threaded results are
+        // reproducible
+        std::thread th([&]() {
+            for (int64_t i = 0; i < n; i += chunk) body(i, std::min(n, i + chunk));
+        });
+        th.join();
         return;
     }
     std::atomic<int64_t> next{0};
@@ -311,22 +329,26 @@ int spo_bsdf_eval(const double *mat, int64_t n, const double *wo, const double *
 int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double *u, double *wi,
                     double *f, double *pdf, int32_t *type) {
     LocalBSDF b(mat);
-    for (int64_t i = 0; i < n; i++) {
-        const Vector3d o(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
-        Vector3d d(0, 0, 0);
-        double p = 0.0;
-        BxDFType st = BxDFType::None;
-        const Spectrum v = b.isect.bsdf()->sample(o, &d, Point2d(u[2 * i], u[2 * i + 1]), &p,
-                                                  BxDFType::All, &st);
-        wi[3 * i] = d.x();
-        wi[3 * i + 1] = d.y();
-        wi[3 * i + 2] = d.z();
-        f[3 * i] = v.red();
-        f[3 * i + 1] = v.green();
-        f[3 * i + 2] = v.blue();
-        pdf[i] = p;
-        type[i] = static_cast<int32_t>(st);
-    }
+    // in a fresh thread, so that the hidden generators of the BxDFs start from their seed
+    std::thread th([&]() {
+        for (int64_t i = 0; i < n; i++) {
+            const Vector3d o(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+            Vector3d d(0, 0, 0);
+            double p = 0.0;
+            BxDFType st = BxDFType::None;
+            const Spectrum v = b.isect.bsdf()->sample(o, &d, Point2d(u[2 * i], u[2 * i + 1]), &p,
+                                                      BxDFType::All, &st);
+            wi[3 * i] = d.x();
+            wi[3 * i + 1] = d.y();
+            wi[3 * i + 2] = d.z();
+            f[3 * i] = v.red();
+            f[3 * i + 1] = v.green();
+            f[3 * i + 2] = v.blue();
+            pdf[i] = p;
+            type[i] = static_cast<int32_t>(st);
+        }
+    });
+    th.join();
     return 0;
 }
 

@@ -851,19 +851,205 @@ struct GGX {   // TrowbridgeReitzDistribution, visible-normal sampling on
     }
 };
 
-// One material instantiated at a hit: the single BxDF each of the three plugins adds.
+// The reference's own erf / erfinv (core/math.h:14-67): Giles' single-precision
+// polynomial for erfinv and Abramowitz & Stegun 7.1.26 for erf, with their float-rounded
+// coefficients promoted to double as in the reference.
+inline double refErfinv(double x) {
+    double w, p;
+    x = clampd(x, -0.99999, 0.99999);
+    w = -std::log((1 - x) * (1 + x));
+    if (w < 5) {
+        w = w - 2.5f;
+        p = 2.81022636e-08f;
+        p = 3.43273939e-07f + p * w;
+        p = -3.5233877e-06f + p * w;
+        p = -4.39150654e-06f + p * w;
+        p = 0.00021858087f + p * w;
+        p = -0.00125372503f + p * w;
+        p = -0.00417768164f + p * w;
+        p = 0.246640727f + p * w;
+        p = 1.50140941f + p * w;
+    } else {
+        w = std::sqrt(w) - 3;
+        p = -0.000200214257f;
+        p = 0.000100950558f + p * w;
+        p = 0.00134934322f + p * w;
+        p = -0.00367342844f + p * w;
+        p = 0.00573950773f + p * w;
+        p = -0.0076224613f + p * w;
+        p = 0.00943887047f + p * w;
+        p = 1.00167406f + p * w;
+        p = 2.83297682f + p * w;
+    }
+    return p * x;
+}
+inline double refErf(double x) {
+    const double a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f, a4 = -1.453152027f,
+                 a5 = 1.061405429f, pp = 0.3275911f;
+    int sign = 1;
+    if (x < 0) sign = -1;
+    x = std::abs(x);
+    const double t = 1 / (1 + pp * x);
+    const double y = 1 - (((((a5 * t + a4) * t) + a3) * t + a2) * t + a1) * t * std::exp(-x * x);
+    return sign * y;
+}
+
+// BeckmannDistribution with visible-normal sampling (microfacet.cc:79-150, 273-356):
+// Jakob's bisection / Newton inversion of the slope CDF.
+struct Beckmann {
+    double ax, ay;
+    double D(const V3 &wh) const {
+        const double t2 = tan2T(wh);
+        if (std::isinf(t2)) return 0.0;
+        const double c4 = cos2T(wh) * cos2T(wh);
+        const double ab2 = cos2P(wh) / (ax * ax) + sin2P(wh) / (ay * ay);
+        return std::exp(-t2 * ab2) / (kPi * ax * ay * c4);
+    }
+    double lambda(const V3 &w) const {
+        const double at = std::abs(tanT(w));
+        if (std::isinf(at)) return 0.0;
+        const double alpha = std::sqrt(cos2P(w) * ax * ax + sin2P(w) * ay * ay);
+        const double a = 1.0 / (alpha * at);
+        if (a >= 1.6) return 0.0;
+        return (1.0 - 1.259 * a + 0.396 * a * a) / (3.535 * a + 2.181 * a * a);
+    }
+    double G1(const V3 &w, const V3 &wh) const {
+        if (w.z * dot(w, wh) <= 0.0) return 0.0;
+        return 1.0 / (1.0 + lambda(w));
+    }
+    double G(const V3 &wo, const V3 &wi, const V3 &wh) const {
+        if (wi.z * dot(wi, wh) <= 0.0) return 0.0;
+        if (wo.z * dot(wo, wh) <= 0.0) return 0.0;
+        return 1.0 / (1.0 + lambda(wo) + lambda(wi));
+    }
+    double pdf(const V3 &wo, const V3 &wh) const {
+        return D(wh) * G1(wo, wh) * absDot(wo, wh) / std::abs(cosT(wo));
+    }
+    static void sample11(double cosThetaI, double U1, double U2, double *sx, double *sy) {
+        if (cosThetaI > 0.9999) {
+            const double r = std::sqrt(-std::log(1.0 - U1));
+            const double sinPhi = std::sin(2.0 * kPi * U2);
+            const double cosPhi = std::cos(2.0 * kPi * U2);
+            *sx = r * cosPhi;
+            *sy = r * sinPhi;
+            return;
+        }
+        const double sinThetaI = std::sqrt(std::max(0.0, 1.0 - cosThetaI * cosThetaI));
+        const double tanThetaI = sinThetaI / cosThetaI;
+        const double cotThetaI = 1.0 / tanThetaI;
+        double a = -1.0;
+        double c = refErf(cotThetaI);
+        const double samplex = std::max(U1, 1.0e-6);
+        const double thetaI = std::acos(cosThetaI);
+        const double fit = 1.0 + thetaI * (-0.876 + thetaI * (0.4265 - 0.0594 * thetaI));
+        double b = c - (1.0 + c) * std::pow(1.0 - samplex, fit);
+        static const double SQRT_PI_INV = 1.0 / std::sqrt(kPi);
+        const double normalization = 1.0 / (1.0 + c + SQRT_PI_INV * tanThetaI * std::exp(-cotThetaI * cotThetaI));
+        for (int it = 0; it < 16; it++) {
+            if (b < a || c < b) b = 0.5 * (a + c);
+            const double xm = refErfinv(b);
+            const double value = normalization * (1.0 + b + SQRT_PI_INV * tanThetaI * std::exp(-xm * xm)) - samplex;
+            const double derivative = normalization * (1.0 - xm * tanThetaI);
+            if (std::abs(value) < 1.0e-6) break;
+            if (value > 0.0) c = b;
+            else a = b;
+            b -= value / derivative;
+        }
+        *sx = refErfinv(b);
+        *sy = refErfinv(2.0 * std::max(U2, 1.0e-6) - 1.0);
+    }
+    V3 sample(const V3 &wo, P2 u) const {
+        const bool flip = wo.z < 0.0;
+        const V3 wi = flip ? -wo : wo;
+        const V3 ws = normalizeDiv(V3(ax * wi.x, ay * wi.y, wi.z));
+        double sx, sy;
+        sample11(cosT(ws), u.u0, u.u1, &sx, &sy);
+        const double tmp = cosP(ws) * sx - sinP(ws) * sy;
+        sy = sinP(ws) * sx + cosP(ws) * sy;
+        sx = tmp;
+        sx *= ax;
+        sy *= ay;
+        V3 wh = normalizeDiv(V3(-sx, -sy, 1.0));
+        if (flip) wh = -wh;
+        return wh;
+    }
+};
+
+// The BxDFs' hidden generators: `static thread_local Random random` in core/bxdf.cc:18
+// (MicrofacetTransmission) and bsdfs/plastic.cc:18 (PlasticBRDF), default seed 0.
+inline Sampler &hiddenBxdfRandom() {
+    static thread_local Sampler r(0u);
+    return r;
+}
+inline Sampler &hiddenPlasticRandom() {
+    static thread_local Sampler r(0u);
+    return r;
+}
+
+inline double frDiffuseReflectance(double eta) {   // fresnel.cc:87
+    if (eta >= 1.0) return -1.4399 / (eta * eta) + 0.7099 / eta + 0.6681 + 0.0636 * eta;
+    return -0.4399f + 0.7099 / eta - 0.3319 / (eta * eta) + 0.0636 / (eta * eta * eta);
+}
+
+// One material instantiated at a hit: the single BxDF each of the plugins adds.
 struct BSDF {
     int kind = -1;        // SPO_MAT_*, -1 = no component (black Lambert)
     RGB R;                // Lambert reflectance
     GGX ggx{1, 1};
     RGB eta, k;           // conductor
-    double ior = 1.0;     // dielectric
+    double ior = 1.0;     // dielectric, rough dielectric, plastic
+    bool beckmann = true; // rough dielectric distribution
+    Beckmann bk{1, 1};
+    RGB Kd, Ks;           // plastic
+    double specWeight = 0.0;
     V3 nrm, tan, bin;     // shading frame, bsdf.cc:14-19
+
+    double mD(const V3 &wh) const { return beckmann ? bk.D(wh) : ggx.D(wh); }
+    double mG(const V3 &wo, const V3 &wi, const V3 &wh) const { return beckmann ? bk.G(wo, wi, wh) : ggx.G(wo, wi, wh); }
+    double mPdf(const V3 &wo, const V3 &wh) const { return beckmann ? bk.pdf(wo, wh) : ggx.pdf(wo, wh); }
+    V3 mSample(const V3 &wo, P2 u) const { return beckmann ? bk.sample(wo, u) : ggx.sample(wo, u); }
+
+    // MicrofacetTransmission::f / pdf with a given half vector (bxdf.cc:333, 408)
+    RGB mtF(const V3 &wo, const V3 &wi, const V3 &wh) const {
+        const double cO = cosT(wo), cI = cosT(wi);
+        if (cO == 0.0 || cI == 0.0) return RGB(0.0);
+        if (wo.z * dot(wo, wh) <= 0.0) return RGB(0.0);
+        if (wi.z * dot(wi, wh) <= 0.0) return RGB(0.0);
+        const double F = frDielectric(dot(wo, wh), 1.0, ior);
+        if (sameHemi(wo, wi)) return RGB(1.0) * F * mD(wh) * mG(wo, wi, wh) / (4.0 * cO * cI);
+        const double eta = dot(wo, wh) > 0.0 ? (ior / 1.0) : (1.0 / ior);
+        const double factor = 1.0 / eta;
+        const double sd = dot(wo, wh) + eta * dot(wi, wh);
+        return RGB(1.0) * (1.0 - F) * std::abs(mD(wh) * mG(wo, wi, wh) * eta * eta * absDot(wi, wh) *
+                                            absDot(wo, wh) * factor * factor / (cI * cO * sd * sd));
+    }
+    double mtPdf(const V3 &wo, const V3 &wi, const V3 &wh) const {
+        if (wo.z * dot(wo, wh) <= 0.0) return 0.0;
+        if (wi.z * dot(wi, wh) <= 0.0) return 0.0;
+        const double F = frDielectric(dot(wo, wh), 1.0, ior);
+        if (sameHemi(wo, wi)) return F * mPdf(wo, wh) / (4.0 * absDot(wo, wh));
+        const double eta = dot(wo, wh) > 0.0 ? (ior / 1.0) : (1.0 / ior);
+        const double sd = dot(wo, wh) + eta * dot(wi, wh);
+        const double dwhdwi = std::abs((eta * eta * dot(wi, wh)) / (sd * sd));
+        return (1.0 - F) * mPdf(wo, wh) * dwhdwi;
+    }
+    V3 mtHalf(const V3 &wo, const V3 &wi) const {   // bxdf.cc:321-330 / 396-405
+        V3 wh;
+        if (sameHemi(wo, wi)) {
+            wh = normalizeDiv(wo + wi);
+        } else {
+            const double eta = cosT(wo) > 0.0 ? (ior / 1.0) : (1.0 / ior);
+            wh = normalizeDiv(wo + wi * eta);
+        }
+        return wh.z >= 0.0 ? wh : -wh;
+    }
 
     int type() const {
         if (kind == SPO_MAT_LAMBERT) return kReflection | kDiffuse;
         if (kind == SPO_MAT_CONDUCTOR) return kReflection | kGlossy;
         if (kind == SPO_MAT_DIELECTRIC) return kReflection | kTransmission | kSpecular;
+        if (kind == SPO_MAT_ROUGH_DIELECTRIC) return kReflection | kTransmission | kGlossy;
+        if (kind == SPO_MAT_PLASTIC) return kReflection | kSpecular | kDiffuse;
         return 0;
     }
     int numComponents(int t) const { return (kind >= 0 && (type() & t) == type()) ? 1 : 0; }
@@ -894,7 +1080,23 @@ struct BSDF {
             }
             return RGB(0.0);
         }
+        if (kind == SPO_MAT_ROUGH_DIELECTRIC) {   // MicrofacetTransmission::f, bxdf.cc:315
+            if (cosT(wo) == 0.0 || cosT(wi) == 0.0) return RGB(0.0);
+            return mtF(wo, wi, mtHalf(wo, wi));
+        }
+        if (kind == SPO_MAT_PLASTIC) {   // PlasticBRDF::f, plastic.cc:31
+            const double Fo = frDielectric(cosT(wo), 1.0, ior);
+            if (dot(wi, V3(-wi.x, -wi.y, wi.z)) > 1.0 - kEps) return Fo * Ks / std::abs(cosT(wi));
+            const double eta = ior / 1.0, invEta = 1.0 / eta;
+            const double Fi = frDielectric(cosT(wi), 1.0, ior);
+            const double Fdr = frDiffuseReflectance(eta);
+            return (1.0 - Fo) * (1.0 - Fi) * invEta * invEta * Kd * kInvPi / (1.0 - Fdr);
+        }
         return RGB(0.0);
+    }
+    double plasticProbSpecular(const V3 &wo) const {   // plastic.cc:48-50
+        const double Fo = frDielectric(cosT(wo), 1.0, ior);
+        return (Fo * specWeight) / (Fo * specWeight + (1.0 - Fo) * (1.0 - specWeight));
     }
     double pdfLocal(const V3 &wo, const V3 &wi) const {
         if (kind == SPO_MAT_LAMBERT) return wo.z * wi.z > 0.0 ? std::abs(wi.z) * kInvPi : 0.0;
@@ -914,6 +1116,12 @@ struct BSDF {
                 if (!refractV(wo, faceForward(V3(0, 0, 1), wo), eI / eT, &wt)) return 0.0;
                 if (dot(wi, wt) > 1.0 - 1.0e-4) return 1.0 - F;
             }
+        }
+        if (kind == SPO_MAT_ROUGH_DIELECTRIC) return mtPdf(wo, wi, mtHalf(wo, wi));   // bxdf.cc:394
+        if (kind == SPO_MAT_PLASTIC) {   // PlasticBRDF::pdf, plastic.cc:71
+            const double ps = plasticProbSpecular(wo);
+            if (dot(wi, V3(-wi.x, -wi.y, wi.z)) > 1.0 - kEps) return ps;
+            return (1.0 - ps) * std::abs(cosT(wi)) * kInvPi;
         }
         return 0.0;
     }
@@ -963,6 +1171,42 @@ struct BSDF {
                 *pdf = ggx.pdf(wo, wh) / (4.0 * dot(wo, wh));
                 ret = fLocal(wo, wi);
             }
+        } else if (kind == SPO_MAT_ROUGH_DIELECTRIC) {   // MicrofacetTransmission::sample, bxdf.cc:356
+            const V3 wh = mSample(wo, ur);
+            const double cO = dot(wo, wh.z > 0.0 ? wh : -wh);
+            const double F = frDielectric(cO, 1.0, ior);
+            bool ok = true;
+            if (hiddenBxdfRandom().get1D() < F) {
+                wi = reflectV(wo, wh);
+                if (!sameHemi(wo, wi)) ok = false;
+                else st = kReflection | kGlossy;
+            } else {
+                const double eta = cO > 0.0 ? (1.0 / ior) : (ior / 1.0);
+                if (!refractV(wo, wh, eta, &wi) || sameHemi(wo, wi)) ok = false;
+                else st = kTransmission | kGlossy;
+            }
+            if (ok) {
+                const V3 whp = wh.z >= 0.0 ? wh : -wh;
+                *pdf = mtPdf(wo, wi, whp);
+                ret = mtF(wo, wi, whp);
+            } else {
+                ret = RGB(0.0);
+            }
+        } else if (kind == SPO_MAT_PLASTIC) {   // PlasticBRDF::sample, plastic.cc:44
+            const double Fo = frDielectric(cosT(wo), 1.0, ior);
+            const double ps = plasticProbSpecular(wo);
+            if (hiddenPlasticRandom().get1D() < ps) {
+                wi = V3(-wo.x, -wo.y, wo.z);
+                *pdf = ps;
+                ret = Ks * Fo / std::abs(cosT(wi));
+            } else {
+                wi = cosineHemisphere(ur);
+                const double eta = ior / 1.0, invEta = 1.0 / eta;
+                const double Fi = frDielectric(cosT(wi), 1.0, ior);
+                const double Fdr = frDiffuseReflectance(eta);
+                *pdf = (1.0 - ps) * std::abs(cosT(wi)) * kInvPi;
+                ret = (1.0 - Fo) * (1.0 - Fi) * invEta * invEta * Kd * kInvPi / (1.0 - Fdr);
+            }
         } else {   // FresnelSpecular::sample, bxdf.cc:198
             const double F = frDielectric(cosT(wo), 1.0, ior);
             if (ur.u0 < F) {
@@ -1009,6 +1253,23 @@ inline BSDF makeBSDF(const double *m, const V3 &ns, const V3 &ts, const V3 &bs) 
         b.ggx = GGX{a, a};
         b.eta = RGB(m[2], m[3], m[4]);
         b.k = RGB(m[5], m[6], m[7]);
+    } else if (type == SPO_MAT_ROUGH_DIELECTRIC) {   // RoughDielectric::setScatterFuncs, roughdielectric.cc:41
+        const double a = RGB(m[1]).gray();
+        b.ior = RGB(m[2]).gray();
+        if (a == 0.0) {
+            b.kind = SPO_MAT_DIELECTRIC;   // FresnelSpecular when both roughnesses are 0
+        } else {
+            b.kind = SPO_MAT_ROUGH_DIELECTRIC;
+            b.beckmann = m[3] == 0.0;
+            b.bk = Beckmann{a, a};
+            b.ggx = GGX{a, a};
+        }
+    } else if (type == SPO_MAT_PLASTIC) {   // Plastic::setScatterFuncs, plastic.cc:112
+        b.kind = SPO_MAT_PLASTIC;
+        b.Kd = RGB(m[1], m[2], m[3]);
+        b.Ks = RGB(m[4], m[5], m[6]);
+        b.ior = RGB(m[7]).gray();
+        b.specWeight = b.Ks.gray() / (b.Kd.gray() + b.Ks.gray());
     } else {   // Dielectric::setScatterFuncs, dielectric.cc:30
         b.kind = SPO_MAT_DIELECTRIC;
         b.ior = RGB(m[1]).gray();
@@ -1194,7 +1455,9 @@ struct spo_scene {
             const int light = std::min(static_cast<int>(sampler.get1D() * nL), nL - 1);
             const P2 uLight = sampler.get2D();
             const P2 uShade = sampler.get2D();
-            if (b.numComponents(kAll & ~kSpecular) > 0) L = L + nL * directLight(h, b, uShade, light, uLight);
+            // unconditional, unlike the path integrator's guard (path.cc:77): BSDF::f matches
+            // a BxDF sharing any type bit, so plastic's diffuse lobe is light-sampled here
+            if (b.kind >= 0) L = L + nL * directLight(h, b, uShade, light, uLight);
         }
         if (1 < maxDepth) {
             // specularReflect / specularTransmit draw their 2D sample before finding no
@@ -1210,7 +1473,12 @@ namespace {
 template <class F>
 void parallelRange(int64_t n, int nthreads, int64_t chunk, F &&body) {
     if (nthreads <= 1) {
-        for (int64_t i = 0; i < n; i += chunk) body(i, std::min(n, i + chunk));
+        // one fresh thread, whose hidden BxDF generators start from their seed (as a
+        // fresh reference thread's do)
+        std::thread th([&]() {
+            for (int64_t i = 0; i < n; i += chunk) body(i, std::min(n, i + chunk));
+        });
+        th.join();
         return;
     }
     std::atomic<int64_t> next{0};
@@ -1365,21 +1633,25 @@ int spo_bsdf_eval(const double *mat, int64_t n, const double *wo, const double *
 int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double *u, double *wi, double *f,
                     double *pdf, int32_t *type) {
     const BSDF b = makeBSDF(mat, normalizeDiv(cross(V3(1, 0, 0), V3(0, 1, 0))), V3(1, 0, 0), V3(0, 1, 0));
-    for (int64_t i = 0; i < n; i++) {
-        const V3 o(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
-        V3 d(0, 0, 0);
-        double p = 0.0;
-        int st = 0;
-        const RGB v = b.sample(o, &d, P2{u[2 * i], u[2 * i + 1]}, &p, kAll, &st);
-        wi[3 * i] = d.x;
-        wi[3 * i + 1] = d.y;
-        wi[3 * i + 2] = d.z;
-        f[3 * i] = v.r;
-        f[3 * i + 1] = v.g;
-        f[3 * i + 2] = v.b;
-        pdf[i] = p;
-        type[i] = st;
-    }
+    // in a fresh thread: the hidden BxDF generators start from their seed
+    std::thread th([&]() {
+        for (int64_t i = 0; i < n; i++) {
+            const V3 o(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+            V3 d(0, 0, 0);
+            double p = 0.0;
+            int st = 0;
+            const RGB v = b.sample(o, &d, P2{u[2 * i], u[2 * i + 1]}, &p, kAll, &st);
+            wi[3 * i] = d.x;
+            wi[3 * i + 1] = d.y;
+            wi[3 * i + 2] = d.z;
+            f[3 * i] = v.r;
+            f[3 * i + 1] = v.g;
+            f[3 * i + 2] = v.b;
+            pdf[i] = p;
+            type[i] = st;
+        }
+    });
+    th.join();
     return 0;
 }
 

@@ -27,6 +27,9 @@ extern "C" {
 #define SPO_MAT_LAMBERT    0 /* [1..3] reflectance RGB                       (bsdfs/diffuse.cc)        */
 #define SPO_MAT_CONDUCTOR  1 /* [1] GGX alpha, [2..4] eta RGB, [5..7] k RGB  (bsdfs/roughconductor.cc) */
 #define SPO_MAT_DIELECTRIC 2 /* [1] interior IOR (exterior 1.0), white Kr/Kt (bsdfs/dielectric.cc)    */
+#define SPO_MAT_ROUGH_DIELECTRIC 3 /* [1] alpha, [2] interior IOR, [3] 0 Beckmann / 1 GGX, white Kr/Kt
+                                     (bsdfs/roughdielectric.cc)                                  */
+#define SPO_MAT_PLASTIC    4 /* [1..3] Kd RGB, [4..6] Ks RGB, [7] IOR     (bsdfs/plastic.cc)          */
 #define SPO_MAT_STRIDE     8
 
 typedef struct spo_scene spo_scene;

@@ -28,7 +28,7 @@ from typing import Optional
 
 import numpy as np
 
-MAT_LAMBERT, MAT_CONDUCTOR, MAT_DIELECTRIC = 0, 1, 2
+MAT_LAMBERT, MAT_CONDUCTOR, MAT_DIELECTRIC, MAT_ROUGH_DIELECTRIC, MAT_PLASTIC = 0, 1, 2, 3, 4
 
 
 @dataclasses.dataclass
@@ -67,6 +67,16 @@ def conductor_f0(alpha, f0):
 
 def dielectric(ior):
     return [MAT_DIELECTRIC, ior, 0, 0, 0, 0, 0, 0]
+
+
+def rough_dielectric(alpha, ior, distribution="beckmann"):
+    """bsdfs/roughdielectric.cc with white Kr/Kt; distribution "beckmann" (its default) or "ggx"."""
+    return [MAT_ROUGH_DIELECTRIC, alpha, ior, 0.0 if distribution == "beckmann" else 1.0, 0, 0, 0, 0]
+
+
+def plastic(kd, ks, ior=1.5):
+    """bsdfs/plastic.cc: diffuse substrate Kd under a smooth coat with specular Ks."""
+    return [MAT_PLASTIC, *kd, *ks, ior]
 
 
 # ----------------------------------------------------------------------------- helpers
@@ -214,6 +224,20 @@ def box_room(albedo_grey=0.75, albedo_red=(0.63, 0.06, 0.05), albedo_green=(0.14
     cam = np.array([0.0, 1.0, 3.9, 0.0, 1.0, 0.0, 0.0, 1.0, 0.0, 40.0])
     return Scene(verts, np.array(mat, np.int32), np.array(mats, np.float64), emit, None, cam,
                  width, height, spp, max_depth, name)
+
+
+def material_room(width=64, height=64, spp=64, max_depth=8, distribution="beckmann") -> Scene:
+    """The box room with its tall box a rough dielectric (alpha 0.25, IOR 1.5) and its short
+    box plastic (Kd (0.6, 0.3, 0.2), Ks 0.4, IOR 1.5): the remaining reference materials."""
+    sc = box_room(width=width, height=height, spp=spp, max_depth=max_depth, name="material_room")
+    mats = [list(m) for m in sc.materials] + [rough_dielectric(0.25, 1.5, distribution),
+                                              plastic((0.6, 0.3, 0.2), (0.4, 0.4, 0.4), 1.5)]
+    tri_mat = sc.tri_mat.copy()
+    tri_mat[10:22] = 3   # tall box
+    tri_mat[22:34] = 4   # short box
+    sc.materials = np.array(mats, np.float64)
+    sc.tri_mat = tri_mat
+    return sc
 
 
 # ----------------------------------------------------------------------------- ray microbench
