@@ -39,6 +39,9 @@ typedef struct spgpu_ctx spgpu_ctx;
 #define SPGPU_MAT_LAMBERT 0    /* [1..3] reflectance */
 #define SPGPU_MAT_CONDUCTOR 1  /* [1] alpha, [2..4] eta, [5..7] k */
 #define SPGPU_MAT_DIELECTRIC 2 /* [1] interior IOR */
+#define SPGPU_MAT_ROUGH_DIELECTRIC 3 /* [1] alpha, [2] interior IOR, [3] 0 Beckmann / 1 GGX
+                                        (bsdfs/roughdielectric.cc, white Kr / Kt) */
+#define SPGPU_MAT_PLASTIC 4    /* [1..3] Kd, [4..6] Ks, [7] IOR (bsdfs/plastic.cc) */
 
 typedef struct {
     int device;          /* CUDA device ordinal */

@@ -553,6 +553,29 @@ int spgpu_upload_scene(spgpu_ctx *h, int32_t ntri, const float *verts, const int
             }
         } else if (M.type == kMatDielectric) {
             M.a = make_float4(0.0f, 0.0f, 0.0f, static_cast<float>(gray1(r[1])));
+        } else if (M.type == kMatRoughDielectric) {
+            // roughdielectric.cc:41-84: zero roughness is the smooth dielectric's FresnelSpecular
+            const float alpha = static_cast<float>(gray1(r[1])), ior = static_cast<float>(gray1(r[2]));
+            if (alpha == 0.0f) {
+                M.type = kMatDielectric;
+                M.a = make_float4(0.0f, 0.0f, 0.0f, ior);
+            } else if (!(alpha > 0.0f) || !(ior > 0.0f) || (r[3] != 0.0f && r[3] != 1.0f)) {
+                setError("spgpu_upload_scene: rough dielectric needs alpha >= 0, ior > 0, distribution 0 or 1");
+                return SPGPU_EINVAL;
+            } else {
+                M.a = make_float4(alpha, ior, r[3], 0.0f);
+            }
+        } else if (M.type == kMatPlastic) {
+            // plastic.cc:112-122 and PlasticBRDF's specular sampling weight (plastic.cc:26)
+            const double kd = 0.2126 * r[1] + 0.7152 * r[2] + 0.0722 * r[3];
+            const double ks = 0.2126 * r[4] + 0.7152 * r[5] + 0.0722 * r[6];
+            const float ior = static_cast<float>(gray1(r[7]));
+            if (!(ior > 0.0f) || !(kd + ks > 0.0)) {
+                setError("spgpu_upload_scene: plastic needs ior > 0 and a non-black Kd + Ks");
+                return SPGPU_EINVAL;
+            }
+            M.a = make_float4(r[1], r[2], r[3], ior);
+            M.b = make_float4(r[4], r[5], r[6], static_cast<float>(ks / (kd + ks)));
         } else {
             setError("spgpu_upload_scene: unknown material type");
             return SPGPU_EINVAL;

@@ -180,12 +180,14 @@ __device__ __forceinline__ float3 offsetOrigin(float3 p, float3 n, float3 w) {
 // core/bxdf.cc, core/microfacet.cc and core/fresnel.cc in single precision.
 // ---------------------------------------------------------------------------
 enum : int { kReflection = 1, kTransmission = 2, kDiffuse = 4, kGlossy = 8, kSpecular = 16, kAll = 31 };
-enum : int { kMatLambert = 0, kMatConductor = 1, kMatDielectric = 2 };
+enum : int { kMatLambert = 0, kMatConductor = 1, kMatDielectric = 2, kMatRoughDielectric = 3, kMatPlastic = 4 };
 
 // material record on the device: 2 x float4
-//   Lambert:    a = (R.rgb, 0),          b = 0
-//   conductor:  a = (eta.rgb, alpha),    b = (k.rgb, 0)
-//   dielectric: a = (0, 0, 0, ior)
+//   Lambert:          a = (R.rgb, 0),                       b = 0
+//   conductor:        a = (eta.rgb, alpha),                 b = (k.rgb, 0)
+//   dielectric:       a = (0, 0, 0, ior)
+//   rough dielectric: a = (alpha, ior, 0 Beckmann / 1 GGX, 0)
+//   plastic:          a = (Kd.rgb, ior),                    b = (Ks.rgb, specular sampling weight)
 struct alignas(16) MaterialRecord {
     float4 a;
     float4 b;
@@ -334,6 +336,133 @@ __device__ __forceinline__ float3 ggxSampleWh(float3 wo, float a, float u0, floa
     return flip ? -wh : wh;
 }
 
+// The reference's own erfinv and erf (core/math.h:14-67): Giles' single-precision
+// polynomial and Abramowitz & Stegun 7.1.26, used by its Beckmann sampler; the same
+// approximations here, so that the sampled distribution is the reference's.
+__device__ __forceinline__ float refErfinvf(float x) {
+    x = clampf(x, -0.99999f, 0.99999f);
+    float w = -logf((1.0f - x) * (1.0f + x)), p;
+    if (w < 5.0f) {
+        w = w - 2.5f;
+        p = 2.81022636e-08f;
+        p = 3.43273939e-07f + p * w;
+        p = -3.5233877e-06f + p * w;
+        p = -4.39150654e-06f + p * w;
+        p = 0.00021858087f + p * w;
+        p = -0.00125372503f + p * w;
+        p = -0.00417768164f + p * w;
+        p = 0.246640727f + p * w;
+        p = 1.50140941f + p * w;
+    } else {
+        w = sqrtf(w) - 3.0f;
+        p = -0.000200214257f;
+        p = 0.000100950558f + p * w;
+        p = 0.00134934322f + p * w;
+        p = -0.00367342844f + p * w;
+        p = 0.00573950773f + p * w;
+        p = -0.0076224613f + p * w;
+        p = 0.00943887047f + p * w;
+        p = 1.00167406f + p * w;
+        p = 2.83297682f + p * w;
+    }
+    return p * x;
+}
+__device__ __forceinline__ float refErff(float x) {
+    const float a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f, a4 = -1.453152027f, a5 = 1.061405429f,
+                p = 0.3275911f;
+    const float sgn = x < 0.0f ? -1.0f : 1.0f;
+    x = fabsf(x);
+    const float t = 1.0f / (1.0f + p * x);
+    const float y = 1.0f - (((((a5 * t + a4) * t) + a3) * t + a2) * t + a1) * t * expf(-x * x);
+    return sgn * y;
+}
+
+// Beckmann, isotropic alpha, visible-normal sampling (microfacet.cc:79-150, 273-356)
+__device__ __forceinline__ float beckD(float3 wh, float a) {
+    const float t2 = tan2T(wh);
+    if (isinf(t2)) return 0.0f;
+    const float c4 = cos2T(wh) * cos2T(wh);
+    return expf(-t2 / (a * a)) / (kPi * a * a * c4);
+}
+__device__ __forceinline__ float beckLambda(float3 w, float a) {
+    const float at = fabsf(sqrtf(sin2T(w)) / (w.z + kEpsT));
+    if (isinf(at)) return 0.0f;
+    const float x = 1.0f / (a * at);
+    if (x >= 1.6f) return 0.0f;
+    return (1.0f - 1.259f * x + 0.396f * x * x) / (3.535f * x + 2.181f * x * x);
+}
+// slopes of the unit-roughness distribution seen from cosThetaI: Jakob's inversion of
+// the slope CDF by bisection / Newton steps (at most 16)
+__device__ __forceinline__ void beckSample11(float cosThetaI, float U1, float U2, float *sx, float *sy) {
+    if (cosThetaI > 0.9999f) {
+        const float r = sqrtf(-logf(1.0f - U1));
+        float s, c;
+        sincosf(2.0f * kPi * U2, &s, &c);
+        *sx = r * c;
+        *sy = r * s;
+        return;
+    }
+    const float sinThetaI = sqrtf(fmaxf(0.0f, 1.0f - cosThetaI * cosThetaI));
+    const float tanThetaI = sinThetaI / cosThetaI;
+    const float cotThetaI = 1.0f / tanThetaI;
+    float a = -1.0f, c = refErff(cotThetaI);
+    const float samplex = fmaxf(U1, 1.0e-6f);
+    const float thetaI = acosf(cosThetaI);
+    const float fit = 1.0f + thetaI * (-0.876f + thetaI * (0.4265f - 0.0594f * thetaI));
+    float b = c - (1.0f + c) * powf(1.0f - samplex, fit);
+    const float sqrtPiInv = 0.5641895835f;   // 1 / sqrt(pi)
+    const float norm = 1.0f / (1.0f + c + sqrtPiInv * tanThetaI * expf(-cotThetaI * cotThetaI));
+    for (int it = 0; it < 16; it++) {
+        if (b < a || c < b) b = 0.5f * (a + c);
+        const float xm = refErfinvf(b);
+        const float value = norm * (1.0f + b + sqrtPiInv * tanThetaI * expf(-xm * xm)) - samplex;
+        const float deriv = norm * (1.0f - xm * tanThetaI);
+        if (fabsf(value) < 1.0e-6f) break;
+        if (value > 0.0f) c = b;
+        else a = b;
+        b -= value / deriv;
+    }
+    *sx = refErfinvf(b);
+    *sy = refErfinvf(2.0f * fmaxf(U2, 1.0e-6f) - 1.0f);
+}
+// stretch, sample the slopes, rotate, unstretch (shared by both distributions)
+template <bool BECKMANN>
+__device__ __forceinline__ float3 visibleNormal(float3 wo, float a, float u0, float u1) {
+    const bool flip = wo.z < 0.0f;
+    const float3 w = flip ? -wo : wo;
+    const float3 ws = normalize(mk(a * w.x, a * w.y, w.z));
+    float sx, sy;
+    if (BECKMANN) beckSample11(ws.z, u0, u1, &sx, &sy);
+    else ggxSample11(ws.z, u0, u1, &sx, &sy);
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - ws.z * ws.z));
+    const float cp = st == 0.0f ? 1.0f : clampf(ws.x / st, -1.0f, 1.0f);
+    const float sp = st == 0.0f ? 0.0f : clampf(ws.y / st, -1.0f, 1.0f);
+    const float tmp = cp * sx - sp * sy;
+    sy = sp * sx + cp * sy;
+    sx = tmp * a;
+    sy = sy * a;
+    const float3 wh = normalize(mk(-sx, -sy, 1.0f));
+    return flip ? -wh : wh;
+}
+
+// microfacet distribution of a rough dielectric (a.x alpha, a.z 0 Beckmann / 1 GGX)
+__device__ __forceinline__ float mfD(const MaterialRecord &m, float3 wh) {
+    return m.a.z == 0.0f ? beckD(wh, m.a.x) : ggxD(wh, m.a.x);
+}
+__device__ __forceinline__ float mfLambda(const MaterialRecord &m, float3 w) {
+    return m.a.z == 0.0f ? beckLambda(w, m.a.x) : ggxLambda(w, m.a.x);
+}
+__device__ __forceinline__ float mfG(const MaterialRecord &m, float3 wo, float3 wi, float3 wh) {
+    if (wi.z * dot(wi, wh) <= 0.0f) return 0.0f;
+    if (wo.z * dot(wo, wh) <= 0.0f) return 0.0f;
+    return 1.0f / (1.0f + mfLambda(m, wo) + mfLambda(m, wi));
+}
+__device__ __forceinline__ float mfPdf(const MaterialRecord &m, float3 wo, float3 wh) {
+    if (wo.z * dot(wo, wh) <= 0.0f) return 0.0f;
+    const float g1 = 1.0f / (1.0f + mfLambda(m, wo));
+    return mfD(m, wh) * g1 * fabsf(dot(wo, wh)) / fabsf(wo.z);
+}
+
 __device__ __forceinline__ bool refract(float3 wi, float3 n, float eta, float3 *wt) {
     const float cI = dot(n, wi);
     const float s2I = fmaxf(0.0f, 1.0f - cI * cI);
@@ -344,7 +473,72 @@ __device__ __forceinline__ bool refract(float3 wi, float3 n, float eta, float3 *
     return true;
 }
 
-// f(wo, wi) for the non-specular materials (BSDF::f restricted to one lobe)
+// MicrofacetTransmission (bxdf.cc:304-427) with etaA = 1, etaB = ior, white Kr / Kt
+__device__ __forceinline__ float3 mtHalf(const MaterialRecord &m, float3 wo, float3 wi) {
+    float3 wh;
+    if (wo.z * wi.z > 0.0f) {
+        wh = normalize(wo + wi);
+    } else {
+        const float eta = wo.z > 0.0f ? m.a.y : 1.0f / m.a.y;
+        wh = normalize(wo + wi * eta);
+    }
+    return wh.z >= 0.0f ? wh : -wh;
+}
+__device__ __forceinline__ float mtF(const MaterialRecord &m, float3 wo, float3 wi, float3 wh) {
+    const float cO = wo.z, cI = wi.z;
+    if (cO == 0.0f || cI == 0.0f) return 0.0f;
+    if (wo.z * dot(wo, wh) <= 0.0f) return 0.0f;
+    if (wi.z * dot(wi, wh) <= 0.0f) return 0.0f;
+    const float F = frDielectric(dot(wo, wh), 1.0f, m.a.y);
+    if (wo.z * wi.z > 0.0f) return F * mfD(m, wh) * mfG(m, wo, wi, wh) / (4.0f * cO * cI);
+    const float eta = dot(wo, wh) > 0.0f ? m.a.y : 1.0f / m.a.y;
+    const float factor = 1.0f / eta;
+    const float sd = dot(wo, wh) + eta * dot(wi, wh);
+    return (1.0f - F) * fabsf(mfD(m, wh) * mfG(m, wo, wi, wh) * eta * eta * fabsf(dot(wi, wh)) *
+                              fabsf(dot(wo, wh)) * factor * factor / (cI * cO * sd * sd));
+}
+__device__ __forceinline__ float mtPdf(const MaterialRecord &m, float3 wo, float3 wi, float3 wh) {
+    if (wo.z * dot(wo, wh) <= 0.0f) return 0.0f;
+    if (wi.z * dot(wi, wh) <= 0.0f) return 0.0f;
+    const float F = frDielectric(dot(wo, wh), 1.0f, m.a.y);
+    if (wo.z * wi.z > 0.0f) return F * mfPdf(m, wo, wh) / (4.0f * fabsf(dot(wo, wh)));
+    const float eta = dot(wo, wh) > 0.0f ? m.a.y : 1.0f / m.a.y;
+    const float sd = dot(wo, wh) + eta * dot(wi, wh);
+    return (1.0f - F) * mfPdf(m, wo, wh) * fabsf((eta * eta * dot(wi, wh)) / (sd * sd));
+}
+
+// PlasticBRDF (bsdfs/plastic.cc:18-95) with etaA = 1, etaB = ior
+__device__ __forceinline__ float frDiffuseReflectance(float eta) {   // fresnel.cc:87
+    if (eta >= 1.0f) return -1.4399f / (eta * eta) + 0.7099f / eta + 0.6681f + 0.0636f * eta;
+    return -0.4399f + 0.7099f / eta - 0.3319f / (eta * eta) + 0.0636f / (eta * eta * eta);
+}
+__device__ __forceinline__ float plasticProbSpecular(const MaterialRecord &m, float3 wo) {
+    const float Fo = frDielectric(wo.z, 1.0f, m.a.w), s = m.b.w;
+    return (Fo * s) / (Fo * s + (1.0f - Fo) * (1.0f - s));
+}
+// PlasticBRDF::f and pdf test wi against its own mirror image (plastic.cc:33,76):
+// true only for wi along the normal
+__device__ __forceinline__ bool plasticMirror(float3 wi) { return wi.z * wi.z - wi.x * wi.x - wi.y * wi.y > 1.0f - 1.0e-12f; }
+__device__ __forceinline__ float3 plasticDiffuse(const MaterialRecord &m, float3 wo, float3 wi) {
+    const float Fo = frDielectric(wo.z, 1.0f, m.a.w), Fi = frDielectric(wi.z, 1.0f, m.a.w);
+    const float invEta = 1.0f / m.a.w;
+    return xyz(m.a) * ((1.0f - Fo) * (1.0f - Fi) * invEta * invEta * kInvPi / (1.0f - frDiffuseReflectance(m.a.w)));
+}
+
+// FresnelSpecular's f and pdf treat wi within 1e-4 (in cosine) of the mirror or the
+// refracted direction as the delta direction: F (reflection) or 1 - F (transmission)
+// there, 0 elsewhere (bxdf.cc:171-196, 236-247)
+__device__ __forceinline__ float dielectricCone(const MaterialRecord &m, float3 wo, float3 wi) {
+    const float F = frDielectric(wo.z, 1.0f, m.a.w);
+    if (wo.z * wi.z > 0.0f) return dot(mk(-wo.x, -wo.y, wo.z), wi) > 1.0f - 1.0e-4f ? F : 0.0f;
+    const bool entering = wo.z > 0.0f;
+    const float eI = entering ? 1.0f : m.a.w, eT = entering ? m.a.w : 1.0f;
+    float3 wt;
+    if (!refract(wo, mk(0.0f, 0.0f, entering ? 1.0f : -1.0f), eI / eT, &wt)) return 0.0f;
+    return dot(wi, wt) > 1.0f - 1.0e-4f ? 1.0f - F : 0.0f;
+}
+
+// f(wo, wi) of the material's BxDF (BSDF::f)
 __device__ __forceinline__ float3 bsdfF(const MaterialRecord &m, float3 wo, float3 wi) {
     if (m.type == kMatLambert) {
         if (wo.z * wi.z <= 0.0f) return mk(0, 0, 0);
@@ -361,20 +555,45 @@ __device__ __forceinline__ float3 bsdfF(const MaterialRecord &m, float3 wo, floa
         const float3 F = frConductor(fabsf(dot(wi, wh)), xyz(m.a), xyz(m.b));
         return F * (ggxD(wh, a) * ggxG(wo, wi, wh, a) / (4.0f * cI * cO));
     }
-    return mk(0, 0, 0);   // specular: zero for any finite pair
+    if (m.type == kMatRoughDielectric) {
+        if (wo.z == 0.0f || wi.z == 0.0f) return mk(0, 0, 0);
+        const float v = mtF(m, wo, wi, mtHalf(m, wo, wi));
+        return mk(v, v, v);
+    }
+    if (m.type == kMatPlastic) {
+        if (wo.z * wi.z <= 0.0f) return mk(0, 0, 0);   // reflection only (BSDF::f, bsdf.cc:57)
+        if (plasticMirror(wi)) return xyz(m.b) * (frDielectric(wo.z, 1.0f, m.a.w) / fabsf(wi.z));
+        return plasticDiffuse(m, wo, wi);
+    }
+    if (m.type == kMatDielectric) {   // FresnelSpecular::f (bxdf.cc:171): a 1e-4 cone about the deltas
+        const float v = dielectricCone(m, wo, wi);
+        return mk(v, v, v) / fabsf(wi.z);
+    }
+    return mk(0, 0, 0);
 }
 __device__ __forceinline__ float bsdfPdf(const MaterialRecord &m, float3 wo, float3 wi) {
+    if (m.type == kMatRoughDielectric) return mtPdf(m, wo, wi, mtHalf(m, wo, wi));
     if (wo.z * wi.z <= 0.0f) return 0.0f;
     if (m.type == kMatLambert) return fabsf(wi.z) * kInvPi;
     if (m.type == kMatConductor) {
         const float3 wh = normalize(wo + wi);
         return ggxPdf(wo, wh, m.a.w) / (4.0f * dot(wo, wh));
     }
+    if (m.type == kMatPlastic) {
+        const float ps = plasticProbSpecular(m, wo);
+        return plasticMirror(wi) ? ps : (1.0f - ps) * fabsf(wi.z) * kInvPi;
+    }
     return 0.0f;
 }
-// BSDF::sample for one lobe; returns f, sets wi, pdf and the sampled type bits
-__device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo, float u0, float u1, float3 *wi,
-                                             float *pdf, int *type) {
+__device__ __forceinline__ float bsdfPdfDielectricCone(const MaterialRecord &m, float3 wo, float3 wi) {
+    return dielectricCone(m, wo, wi);   // FresnelSpecular::pdf (bxdf.cc:236): F or 1 - F inside the cones
+}
+// BSDF::sample for the material's BxDF; returns f, sets wi, pdf and the sampled type
+// bits.  uc is the draw the reference takes from its BxDFs' hidden generator
+// (core/bxdf.cc:18, bsdfs/plastic.cc:18): the rough dielectric's reflect / refract and
+// the plastic's specular / diffuse choice.
+__device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo, float u0, float u1, float uc,
+                                             float3 *wi, float *pdf, int *type) {
     *pdf = 0.0f;
     *type = 0;
     if (wo.z == 0.0f) return mk(0, 0, 0);
@@ -396,6 +615,42 @@ __device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo,
         *type = kReflection | kGlossy;
         return bsdfF(m, wo, w);
     }
+    if (m.type == kMatRoughDielectric) {   // MicrofacetTransmission::sample, bxdf.cc:356
+        const float3 wh = m.a.z == 0.0f ? visibleNormal<true>(wo, m.a.x, ur0, u1)
+                                        : visibleNormal<false>(wo, m.a.x, ur0, u1);
+        const float cO = dot(wo, wh.z > 0.0f ? wh : -wh);
+        const float F = frDielectric(cO, 1.0f, m.a.y);
+        float3 w;
+        int t;
+        if (uc < F) {
+            w = -wo + wh * (2.0f * dot(wh, wo));
+            if (wo.z * w.z <= 0.0f) return mk(0, 0, 0);
+            t = kReflection | kGlossy;
+        } else {
+            const float eta = cO > 0.0f ? 1.0f / m.a.y : m.a.y;
+            if (!refract(wo, wh, eta, &w) || wo.z * w.z > 0.0f) return mk(0, 0, 0);
+            t = kTransmission | kGlossy;
+        }
+        const float3 whp = wh.z >= 0.0f ? wh : -wh;
+        *wi = w;
+        *pdf = mtPdf(m, wo, w, whp);
+        *type = t;
+        const float v = mtF(m, wo, w, whp);
+        return mk(v, v, v);
+    }
+    if (m.type == kMatPlastic) {   // PlasticBRDF::sample, plastic.cc:44; the BxDF's own type is reported
+        const float ps = plasticProbSpecular(m, wo);
+        *type = kReflection | kSpecular | kDiffuse;
+        if (uc < ps) {
+            *wi = mk(-wo.x, -wo.y, wo.z);
+            *pdf = ps;
+            return xyz(m.b) * (frDielectric(wo.z, 1.0f, m.a.w) / fabsf(wo.z));
+        }
+        const float3 w = cosineHemisphere(ur0, u1);
+        *wi = w;
+        *pdf = (1.0f - ps) * fabsf(w.z) * kInvPi;
+        return plasticDiffuse(m, wo, w);
+    }
     // smooth dielectric (FresnelSpecular::sample, bxdf.cc:198)
     const float ior = m.a.w;
     const float F = frDielectric(wo.z, 1.0f, ior);
@@ -414,6 +669,12 @@ __device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo,
     *type = kSpecular | kTransmission;
     const float ft = (1.0f - F) * ((eI * eI) / (eT * eT));
     return mk(ft, ft, ft) / fabsf(w.z);
+}
+
+// wavefront shading class (sort key of the material-sorted queues): 0 diffuse, 1 glossy,
+// 2 specular-typed
+__device__ __forceinline__ int shadeClass(int type) {
+    return type == kMatLambert ? 0 : (type == kMatConductor || type == kMatRoughDielectric) ? 1 : 2;
 }
 
 __device__ __forceinline__ float powerHeuristic(float f, float g) { return (f * f) / (f * f + g * g); }

@@ -420,7 +420,7 @@ struct MixProposal {
         if (!M || uSel < alpha) {
             float pb;
             int type;
-            const float3 fb = bsdfSample(m, woL, u1, u2, &wiL, &pb, &type);
+            const float3 fb = bsdfSample(m, woL, u1, u2, 0.0f, &wiL, &pb, &type);   // Lambert only
             if (isBlack(fb) || pb <= 0.0f) return false;
             *wiW = normalize(tg * wiL.x + bg * wiL.y + n * wiL.z);
         } else {

@@ -121,9 +121,13 @@ struct ShadeResult {
 // Shade the hit h of ray (o, d) for a path with throughput beta at bounce b.
 // pixelKey / sample select the counter-based random streams; filmIdx is stored in the
 // shadow entries.  S.lights[S.lightBase + k] are the area lights of this scene.
+// direct = true is DirectLightingIntegrator's estimator (no continuation is used):
+// light sampling at every material, since its BSDF::f matches any BxDF sharing a type
+// bit with the non-specular set (bsdf.cc:49-60); the path integrator light-samples only
+// materials with a non-specular BxDF (path.cc:77).
 __device__ __forceinline__ void shadeHit(const SceneView &S, const HitRecord &h, float3 o, float3 d, float3 beta,
                                          bool spec, int b, int maxDepth, uint32_t seed, uint32_t pixelKey,
-                                         uint32_t sample, int filmIdx, ShadeResult &R) {
+                                         uint32_t sample, int filmIdx, ShadeResult &R, bool direct = false) {
     R.emit = mk(0, 0, 0);
     R.cont = false;
     R.sh0 = R.sh1 = false;
@@ -146,7 +150,12 @@ __device__ __forceinline__ void shadeHit(const SceneView &S, const HitRecord &h,
                                static_cast<uint32_t>(b), 0u);
         const Rand4 r1 = rand4(seed, pixelKey, sample,
                                static_cast<uint32_t>(b), 1u);
-        if (m.type != kMatDielectric && S.nLights > 0) {
+        // the draws the reference takes from its BxDFs' hidden generator
+        const bool hidden = m.type == kMatRoughDielectric || m.type == kMatPlastic;
+        const Rand4 r3 = hidden ? rand4(seed, pixelKey, sample, static_cast<uint32_t>(b), 3u) : Rand4{0, 0, 0, 0};
+        // materials with a non-specular BxDF (numComponents(All & ~Specular) > 0)
+        const bool nonSpecular = m.type == kMatLambert || m.type == kMatConductor || m.type == kMatRoughDielectric;
+        if ((nonSpecular || direct) && S.nLights > 0) {
             // ---- uniformSampleOneLight + estimateDirectLight (mis.cc:21-136)
             const int nL = S.nLights;
             const int li = min(static_cast<int>(r0.a * nL), nL - 1);
@@ -191,7 +200,8 @@ __device__ __forceinline__ void shadeHit(const SceneView &S, const HitRecord &h,
                 const float3 wiL = mk(dot(wi, tg), dot(wi, bg), dot(wi, n));
                 const float3 f = bsdfF(m, woL, wiL) * fabsf(dot(wi, n));
                 if (!isBlack(f)) {
-                    const float bp = bsdfPdf(m, woL, wiL);
+                    const float bp = m.type == kMatDielectric ? bsdfPdfDielectricCone(m, woL, wiL)
+                                                              : bsdfPdf(m, woL, wiL);
                     const float w = powerHeuristic(lightPdf, bp);
                     const float3 c = scale * f * Li * (w / lightPdf);
                     // VisibilityTester::unoccluded via spawnRayTo (interaction.cc:88)
@@ -209,11 +219,12 @@ __device__ __forceinline__ void shadeHit(const SceneView &S, const HitRecord &h,
                     }
                 }
             }
-            // BSDF sampling with MIS
+            // BSDF sampling with MIS (only BxDFs of the non-specular set can be sampled)
             float3 wiL2;
-            float pdf2;
+            float pdf2 = 0.0f;
             int type2;
-            float3 f2 = bsdfSample(m, woL, r0.d, r1.a, &wiL2, &pdf2, &type2);
+            float3 f2 = mk(0, 0, 0);
+            if (nonSpecular) f2 = bsdfSample(m, woL, r0.d, r1.a, r3.a, &wiL2, &pdf2, &type2);
             if (!isBlack(f2) && pdf2 > 0.0f) {
                 const float3 wi2 = normalize(tg * wiL2.x + bg * wiL2.y + n * wiL2.z);
                 f2 = f2 * fabsf(dot(wi2, n));
@@ -242,7 +253,7 @@ __device__ __forceinline__ void shadeHit(const SceneView &S, const HitRecord &h,
         float3 wiL;
         float pdf;
         int type;
-        const float3 f = bsdfSample(m, woL, r1.b, r1.c, &wiL, &pdf, &type);
+        const float3 f = bsdfSample(m, woL, r1.b, r1.c, r3.b, &wiL, &pdf, &type);
         if (!isBlack(f) && pdf > 0.0f) {
             const float3 wi = normalize(tg * wiL.x + bg * wiL.y + n * wiL.z);
             beta = beta * f * (fabsf(dot(wi, n)) / pdf);

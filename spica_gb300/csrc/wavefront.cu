@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_extend(PassArgs p, int b) {
                 h.u = L.hu;
                 h.v = L.hv;
                 p.hits[i] = h;
-                cls = __ldg(&p.sv.mats[__ldg(&p.sv.slotShade[L.hitSlot]).x].type);
+                cls = shadeClass(__ldg(&p.sv.mats[__ldg(&p.sv.slotShade[L.hitSlot]).x].type));
             } else if (p.sv.hasEnv) {
                 // escaped: the environment at the first hit or after a specular bounce
                 const int pid = __float_as_int(rO[i].w);
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
             const float4 bt = p.beta[pid];
             const int fi = filmIndex(p, pid);
             shadeHit(p.sv, p.hits[i], xyz(o4), xyz(d4), xyz(bt), bt.w != 0.0f, b, p.maxDepth, p.seed,
-                     static_cast<uint32_t>(fi), sample, fi, R);
+                     static_cast<uint32_t>(fi), sample, fi, R, p.direct != 0);
             if (!isBlack(R.emit)) filmAdd(p.film, fi, R.emit);
         }
         const int k = warpAppend(R.cont && !p.direct, nextCnt);

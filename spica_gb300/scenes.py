@@ -228,8 +228,14 @@ def box_room(albedo_grey=0.75, albedo_red=(0.63, 0.06, 0.05), albedo_green=(0.14
 
 def material_room(width=64, height=64, spp=64, max_depth=8, distribution="beckmann") -> Scene:
     """The box room with its tall box a rough dielectric (alpha 0.25, IOR 1.5) and its short
-    box plastic (Kd (0.6, 0.3, 0.2), Ks 0.4, IOR 1.5): the remaining reference materials."""
+    box plastic (Kd (0.6, 0.3, 0.2), Ks 0.4, IOR 1.5): the remaining reference materials.
+    The dielectric box floats 1 cm above the floor: resting on it, its bottom face would be
+    coplanar with the floor, and every ray leaving the box downwards would tie between the
+    two, a tie that the reference's BVH and the 8-wide one break differently."""
     sc = box_room(width=width, height=height, spp=spp, max_depth=max_depth, name="material_room")
+    V = sc.verts.reshape(-1, 3, 3).copy()
+    V[10:22, :, 1] += 0.01
+    sc.verts = V.reshape(-1, 9).astype(np.float32)
     mats = [list(m) for m in sc.materials] + [rough_dielectric(0.25, 1.5, distribution),
                                               plastic((0.6, 0.3, 0.2), (0.4, 0.4, 0.4), 1.5)]
     tri_mat = sc.tri_mat.copy()

@@ -121,6 +121,7 @@ def main():
                         tri_mat=es.tri_mat, materials=es.materials, tri_emit=es.tri_emit, env=es.env)
     direct_renders(ref)
     film_outputs(ref)
+    more_materials(ref)
     print(f"golden fixtures written in {time.time() - t0:.1f} s")
 
 
@@ -135,10 +136,6 @@ def direct_renders(ref):
     np.savez_compressed(os.path.join(HERE, "render_direct_envscene.npz"), sum=S, sumsq=S2, spp=es.spp, seed=19,
                         W=es.width, H=es.height, max_depth=es.max_depth, camera=es.camera, verts=es.verts,
                         tri_mat=es.tri_mat, materials=es.materials, tri_emit=es.tri_emit, env=es.env)
-
-
-if __name__ == "__main__":
-    main()
 
 
 def film_input(W=131, H=37, seed=11):
@@ -164,3 +161,58 @@ def film_outputs(ref):
         hdr = np.frombuffer(open(path, "rb").read(), np.uint8)
     np.savez_compressed(os.path.join(HERE, "film_output.npz"), film=film, hdr=hdr,
                         gamma22=ref.film_gamma(film, 2.2), reinhard=ref.film_reinhard(film, 0.18))
+
+
+def more_materials(ref):
+    """8. rough dielectric (Beckmann, GGX) and plastic: BSDF tables, and path / direct renders
+    of the material room.  One thread (a fresh one), so that the reference's hidden BxDF
+    generators start from their seed and the fixtures are reproducible."""
+    rng = np.random.default_rng(21)
+    n = 2000
+    wo = rng.normal(size=(n, 3))
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    wi = rng.normal(size=(n, 3))
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    u = rng.random((n, 2))
+    mats = np.array([scenes.rough_dielectric(0.3, 1.5, "beckmann"), scenes.rough_dielectric(0.15, 1.33, "ggx"),
+                     scenes.plastic((0.6, 0.3, 0.2), (0.4, 0.4, 0.4), 1.5),
+                     scenes.plastic((0.1, 0.8, 0.5), (0.05, 0.02, 0.03), 1.3)], np.float64)
+    out = {"mats": mats, "wo": wo, "wi": wi, "u": u}
+    for k, m in enumerate(mats):
+        f, pdf = ref.bsdf_eval(m, wo, wi)
+        swi, sf, spdf, st = ref.bsdf_sample(m, wo, u)
+        out.update({f"f{k}": f, f"pdf{k}": pdf, f"swi{k}": swi, f"sf{k}": sf, f"spdf{k}": spdf, f"stype{k}": st})
+    np.savez_compressed(os.path.join(HERE, "bsdf_tables_more.npz"), **out)
+    sc = scenes.material_room(width=48, height=48)
+    for integ, name in (("path", "render_material_room.npz"), ("direct", "render_direct_material_room.npz")):
+        S, S2 = ref.scene(sc).render(sc.camera, 48, 48, 1024, 8, seed=29, nthreads=1, integrator=integ)
+        bmean, bvar = batch_moments(integ, MATERIAL_BATCHES, 1024, seed0=1000)
+        np.savez_compressed(os.path.join(HERE, name), sum=S, sumsq=S2, spp=1024, seed=29, W=48, H=48, max_depth=8,
+                            camera=sc.camera, verts=sc.verts, tri_mat=sc.tri_mat, materials=sc.materials,
+                            tri_emit=sc.tri_emit, env=np.zeros((0,), np.float32), bmean=bmean, bvar=bvar,
+                            batches=MATERIAL_BATCHES, batch_spp=1024)
+
+
+MATERIAL_BATCHES = 32
+
+
+def _material_batch(args):
+    integ, spp, seed = args
+    sc = scenes.material_room(width=48, height=48)
+    S, _ = spo.Oracle("ref").scene(sc).render(sc.camera, 48, 48, spp, 8, seed=seed, nthreads=1, integrator=integ)
+    return S / spp
+
+
+def batch_moments(integ, batches, spp, seed0):
+    """Per-pixel mean and variance of the mean over independent batches (seeds seed0..).
+    Light refracted through the glass box reaches the walls along rare bright paths; the
+    per-sample variance of a 1024-sample render under-reads that tail, so the 3-sigma
+    comparison uses the spread of batch means instead."""
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(min(batches, os.cpu_count() or 1)) as pool:
+        m = np.stack(pool.map(_material_batch, [(integ, spp, seed0 + k) for k in range(batches)]))
+    return m.mean(0), m.var(0, ddof=1) / batches
+
+
+if __name__ == "__main__":
+    main()

@@ -72,8 +72,26 @@ def test_bsdf_tables_match_reference_golden(port):
         assert np.array_equal(st, g[f"stype{k}"])
 
 
+def test_more_bsdf_tables_match_reference_golden(port):
+    """Rough dielectric (Beckmann, GGX) and plastic, including the draws the reference
+    takes from its BxDFs' hidden generators (sampling runs in a fresh thread on both
+    sides, where those generators start from their seed)."""
+    g = np.load(os.path.join(GOLDEN, "bsdf_tables_more.npz"))
+    for k, m in enumerate(g["mats"]):
+        f, pdf = port.bsdf_eval(m, g["wo"], g["wi"])
+        np.testing.assert_allclose(f, g[f"f{k}"], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(pdf, g[f"pdf{k}"], rtol=1e-12, atol=1e-14)
+        wi, sf, spdf, st = port.bsdf_sample(m, g["wo"], g["u"])
+        np.testing.assert_allclose(wi, g[f"swi{k}"], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(sf, g[f"sf{k}"], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(spdf, g[f"spdf{k}"], rtol=1e-12, atol=1e-14)
+        assert np.array_equal(st, g[f"stype{k}"])
+        assert (np.abs(f).sum(1) > 0).mean() > 0.2
+
+
 @pytest.mark.parametrize("name", ["render_boxroom", "render_envscene", "render_direct_boxroom",
-                                  "render_direct_envscene"])
+                                  "render_direct_envscene", "render_material_room",
+                                  "render_direct_material_room"])
 def test_render_matches_reference_golden(port, name):
     """Same per-pixel sampler streams => the restatement reproduces the reference's
     per-pixel sums (exactly on the host that made the fixture; libm differences in
@@ -81,14 +99,18 @@ def test_render_matches_reference_golden(port, name):
     path and the direct-lighting integrators."""
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     integrator = "direct" if "direct" in name else "path"
-    if "boxroom" in name:
+    # the material room's BxDFs draw from hidden per-thread generators: one thread
+    nthreads = 1 if "material" in name else None
+    if "material_room" in name:
+        sc = scenes.material_room(width=int(g["W"]), height=int(g["H"]))
+    elif "boxroom" in name:
         sc = scenes.box_room(width=int(g["W"]), height=int(g["H"]))
     else:
         sc = _scene_from(g)
     o = port.scene(sc)
     spp = 64   # a prefix of the fixture's samples is not comparable; render the full count
     S, S2 = o.render(g["camera"], int(g["W"]), int(g["H"]), int(g["spp"]), int(g["max_depth"]), seed=int(g["seed"]),
-                     integrator=integrator)
+                     integrator=integrator, nthreads=nthreads)
     rel = np.abs(S - g["sum"]) / np.maximum(np.abs(g["sum"]), 1e-12)
     assert (rel.max(axis=2) > 1e-9).mean() < 0.02
     assert abs(S.mean() - g["sum"].mean()) <= 1e-3 * g["sum"].mean()

@@ -39,6 +39,10 @@ def gpu_batches(accel, camera, W, H, max_depth, batches, spp, seed=1, integrator
 
 
 def ref_moments(g):
+    """Per-pixel mean and variance of the mean of a reference render: from independent
+    batch means where the fixture holds them, else from the per-sample sums."""
+    if "bmean" in g:
+        return g["bmean"], g["bvar"]
     n = float(g["spp"])
     mean = g["sum"] / n
     var = np.maximum(g["sumsq"] / n - mean ** 2, 0.0) * n / (n - 1) / n
@@ -46,15 +50,22 @@ def ref_moments(g):
 
 
 @pytest.mark.parametrize("name", ["render_boxroom", "render_envscene", "render_direct_boxroom",
-                                  "render_direct_envscene"])
+                                  "render_direct_envscene", "render_material_room",
+                                  "render_direct_material_room"])
 def test_matches_reference_render(gpulib, name):
     """Path integrator and direct-lighting integrator against the reference's renders."""
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     W, H, md = int(g["W"]), int(g["H"]), int(g["max_depth"])
-    sc = scenes.box_room(width=W, height=H) if "boxroom" in name else _scene_from(g)
+    if "material_room" in name:   # rough dielectric and plastic boxes
+        sc = scenes.material_room(width=W, height=H)
+    else:
+        sc = scenes.box_room(width=W, height=H) if "boxroom" in name else _scene_from(g)
     acc = GpuBVHAccel(sc).construct()
     integ = GpuDirectLightingIntegrator if "direct" in name else GpuPathIntegrator
-    mg, vg = gpu_batches(acc, g["camera"], W, H, md, batches=16, spp=512, integrator=integ)
+    # match the fixture's sample count where it holds batch moments: both sides then see
+    # the same share of the rare bright paths through the glass box
+    batches, spp = (int(g["batches"]), int(g["batch_spp"])) if "bmean" in g else (16, 512)
+    mg, vg = gpu_batches(acc, g["camera"], W, H, md, batches=batches, spp=spp, integrator=integ)
     mr, vr = ref_moments(g)
     z = zscores(mg, vg, mr, vr)
     frac = float((np.abs(z) > 3).mean())
@@ -122,3 +133,21 @@ def test_pass_lanes_render_the_same_samples(gpulib):
         for a, b in zip(films[1], films[lanes]):
             np.testing.assert_array_equal(a[..., 3], b[..., 3])
             np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=1e-5, atol=1e-6)
+
+
+def test_checkpoint_resume_continues_the_sample_index(gpulib, tmp_path):
+    """Checkpoint / resume: the film (sum of L, sample count) saved after k samples and
+    rendered on from sample_offset = k holds exactly the samples of one uninterrupted
+    render (the sampler is counter-based: a sample's numbers depend only on its
+    pixel, index, bounce and stream)."""
+    sc = scenes.box_room(width=80, height=60)
+    params = {"width": 80, "height": 60, "maxDepth": 8}
+    acc = GpuBVHAccel(sc).construct()
+    integ = GpuPathIntegrator(seed=5)
+    whole = integ.render(sc.camera, acc, dict(params, sampleCount=12))
+    part = integ.render(sc.camera, acc, dict(params, sampleCount=5))
+    np.save(tmp_path / "film.npy", part)                       # checkpoint
+    film = np.load(tmp_path / "film.npy")                      # resume
+    integ.render(sc.camera, acc, dict(params, sampleCount=7), film=film, sample_offset=5)
+    np.testing.assert_array_equal(film[..., 3], whole[..., 3])
+    np.testing.assert_allclose(film[..., :3], whole[..., :3], rtol=1e-5, atol=1e-6)
