@@ -59,10 +59,13 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdio>
 #include <memory>
+#include <string>
 #include <thread>
 #include <vector>
 
+#include "material_probe.h"   // the drop-in plugin's material translation, under test
 #include "spo_api.h"
 
 using namespace spica;
@@ -324,6 +327,14 @@ int spo_bsdf_eval(const double *mat, int64_t n, const double *wo, const double *
         pdf[i] = b.isect.bsdf()->pdf(o, d);
     }
     return 0;
+}
+
+int spo_probe_material(const double *mat, float *rec, char *why, int why_len) {
+    LocalBSDF b(mat);
+    std::string reason;
+    const int rc = spgpu_probe::probeMaterial(b.isect.bsdf(), rec, &reason);
+    if (why && why_len > 0) std::snprintf(why, why_len, "%s", reason.c_str());
+    return rc;
 }
 
 int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double *u, double *wi,

@@ -105,6 +105,16 @@ class Oracle:
         self.lib.spo_bsdf_sample(mat, n, wo, u, wi, f, pdf, typ)
         return wi, f, pdf, typ
 
+    def probe_material(self, mat):
+        """The drop-in plugin's material translation on the reference's BSDF for a
+        material record (compiled reference only): (record, None) or (None, reason)."""
+        mat = np.ascontiguousarray(mat, np.float64)
+        rec = np.zeros(8, np.float32)
+        why = C.create_string_buffer(256)
+        self.lib.spo_probe_material.argtypes = [_dp, C.c_void_p, C.c_char_p, C.c_int]
+        rc = self.lib.spo_probe_material(mat, rec.ctypes.data, why, 256)
+        return (rec, None) if rc == 0 else (None, why.value.decode())
+
     # ---------------------------------------------------------------- film output
     # (compiled reference only: the restatement does not carry the image code)
     def _film(self, film):

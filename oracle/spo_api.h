@@ -83,6 +83,11 @@ int spo_film_save_hdr(const float *film, int W, int H, const char *path);
 int spo_film_gamma(const float *film, int W, int H, double gamma, uint8_t *out);
 int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out);
 
+/* The drop-in integrator plugin's material translation (spica_gb300/plugins/
+ * material_probe.h) run on the reference's own BSDF for a material record (compiled
+ * reference only): 0 and the spgpu record in rec[0..7], or -1 and the refusal in why. */
+int spo_probe_material(const double *mat, float *rec, char *why, int why_len);
+
 /* per-pixel sampler seed: splitmix-style mix of (seed, pixel) folded to 32 bits */
 static inline uint32_t spo_pixel_seed(uint32_t seed, uint32_t pixel) {
     uint64_t z = ((uint64_t)seed << 32) ^ (uint64_t)pixel;

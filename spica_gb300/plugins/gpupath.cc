@@ -12,12 +12,9 @@
 // Translation uses only public API:
 //   geometry   Primitive::triangulate (core/primitive.h:26)
 //   materials  Primitive::setScatterFuncs on a unit-frame SurfaceInteraction, then the
-//              BSDF's public f / pdf / sample / eta (core/bsdf.h:20-54):
-//                Lambert       R = pi f(z, z)
-//                GGX conductor alpha from pdf(z, z) = 1 / (4 pi alpha^2), F0 = 4 pi alpha^2 f(z, z),
-//                              stored as eta = 1, k = 2 sqrt(F0 / (1 - F0)) (exact for F0-authored
-//                              conductors; others are matched at normal incidence)
-//                dielectric    IOR = BSDF::eta() (bsdfs/dielectric.cc:38)
+//              BSDF's public f / pdf / hasType / eta (core/bsdf.h:20-54), read as one of
+//              the GPU's materials by material_probe.h (Lambert, GGX conductor,
+//              dielectric, rough dielectric, plastic); any other material is a FatalError
 //   lights     Primitive::light() + Light::L for area lights; Light::Le sampled at texel
 //              centres (envmapWidth x envmapWidth/2, default 1024) for the environment
 //   camera     Camera::cameraToWorld / cameraToScreen (core/camera.h:43-44): eye, view
@@ -29,6 +26,7 @@
 #include <cmath>
 #include <map>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "core/bsdf.h"
@@ -49,6 +47,7 @@
 #include "core/transform.h"
 #include "core/triangle.h"
 
+#include "material_probe.h"
 #include "spica_gpu.h"
 
 namespace spica {
@@ -161,30 +160,9 @@ private:
         SurfaceInteraction si(Point3d(0, 0, 0), Point2d(0, 0), Vector3d(0, 0, 1), Vector3d(1, 0, 0),
                               Vector3d(0, 1, 0), Normal3d(), Normal3d(), nullptr);
         prim.setScatterFuncs(&si, arena);
-        float rec[8] = {SPGPU_MAT_LAMBERT, 0, 0, 0, 0, 0, 0, 0};
-        const BSDF *b = si.bsdf();
-        const Vector3d z(0, 0, 1);
-        if (b && b->hasType(BxDFType::Transmission)) {
-            rec[0] = SPGPU_MAT_DIELECTRIC;
-            rec[1] = (float)b->eta();
-        } else if (b && b->hasType(BxDFType::Glossy)) {
-            const double pdf = b->pdf(z, z);
-            const double alpha = std::sqrt(1.0 / (4.0 * PI * pdf));
-            const Spectrum f = b->f(z, z);
-            const double f0[3] = {f.red(), f.green(), f.blue()};
-            rec[0] = SPGPU_MAT_CONDUCTOR;
-            rec[1] = (float)alpha;
-            for (int c = 0; c < 3; c++) {
-                const double F0 = std::min(0.999, 4.0 * PI * alpha * alpha * f0[c]);
-                rec[2 + c] = 1.0f;
-                rec[5 + c] = (float)(2.0 * std::sqrt(F0 / (1.0 - F0)));
-            }
-        } else if (b && b->numComponents() > 0) {
-            const Spectrum f = b->f(z, z);
-            rec[1] = (float)(PI * f.red());
-            rec[2] = (float)(PI * f.green());
-            rec[3] = (float)(PI * f.blue());
-        }
+        float rec[8];
+        std::string why;
+        if (spgpu_probe::probeMaterial(si.bsdf(), rec, &why) != 0) FatalError("gpupath: %s", why.c_str());
         const int m = static_cast<int>(mats->size() / 8);
         mats->insert(mats->end(), rec, rec + 8);
         (*index)[key] = m;
