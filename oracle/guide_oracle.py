@@ -116,9 +116,11 @@ def grad(p, x, wdir, c, emulate_bf16=True):
     for li in range(3, -1, -1):
         W, b = L[li]
         h_in = acts[li]
-        grads.append((dy.T @ h_in, dy.sum(0)))
+        # the device feeds dY to the tensor core as bf16 (weight gradient and dX); the
+        # bias gradient sums the fp32 dY
+        grads.append((q(dy).T @ h_in, dy.sum(0)))
         if li > 0:
-            dx = dy @ q(W)
+            dx = q(dy) @ q(W)
             dy = dx * (acts[li] > 0)
     grads = grads[::-1]
     out = []

@@ -127,27 +127,58 @@ struct TrainLayout {
     static constexpr int h3 = h2 + kGTile * kGHid * 2;
     static constexpr int dyb = h3 + kGTile * kGHid * 2;
     static constexpr int dy = dyb + kGTile * kGHid * 2;
-    static constexpr int gw = dy + kGTile * kTrainStride * 4;
-    static constexpr int bar = gw + kGParams * 4;
+    static constexpr int gb = dy + kGTile * kTrainStride * 4;
+    static constexpr int bar = gb + kBiasPad * 4;
     static constexpr int tmem = bar + 8;
     static constexpr int total = tmem + 8;
 };
 static_assert(TrainLayout::x % 16 == 0 && TrainLayout::h1 % 16 == 0 && TrainLayout::dyb % 16 == 0, "alignment");
 static_assert(TrainLayout::bar % 8 == 0, "alignment");
+// one training CTA per SM: its 512-column TMEM allocation (all of the SM's tensor
+// memory) then never waits for another CTA's
+static_assert(2 * TrainLayout::total > 228 * 1024, "training CTA must fill more than half of an SM's shared memory");
 
-// dW[o][i] += sum_r dy[r][o] * h[r][i] for this tile; bias[o] += sum_r dy[r][o]
-__device__ __forceinline__ void accumLayer(float *gw, int offW, int offB, int nOut, int nIn, const float *dy,
-                                           const uint8_t *h, int Kh) {
-    for (int e = threadIdx.x; e < nOut * nIn; e += kGTile) {
-        const int o = e / nIn, i = e % nIn;
-        float s = 0.0f;
-        for (int r = 0; r < kGTile; r++) s += dy[r * kTrainStride + o] * loadBf16(h, r, i, Kh);
-        gw[offW + e] += s;
-    }
+// Weight-gradient accumulators in tensor memory (columns after the layer accumulator
+// at 0-63), M = 64 (a layer's outputs), N = its inputs, accumulated over all tiles of
+// the CTA: dW4 (40 x 64), dW3, dW2 (64 x 64), dW1 (64 x 16, inputs padded)
+constexpr uint32_t kTrainTmemCols = 512;
+constexpr uint32_t kColDW4 = 64, kColDW3 = 128, kColDW2 = 192, kColDW1 = 256;
+
+// dW (+)= dY^T H over the tile's 128 rows, on the tensor core: dY and H are the tile's
+// K-major bf16 tiles ([128][kDy] and [128][kH]) read transposed (MN-major), so the
+// tile's rows are the MMA's K; the first 64 columns of dY are the MMA's M rows (rows
+// past the layer's outputs are never read back).  Called by the issuing thread.
+__device__ __forceinline__ void issueWeightGrad(uint32_t dTmem, const uint8_t *dyTile, uint32_t kDy,
+                                                const uint8_t *hTile, uint32_t kH, bool accumulate) {
+    const uint32_t aLbo = (kDy / 8) * 128, bLbo = (kH / 8) * 128;
+    const uint32_t idesc = tc::instrDescBf16(64, kH) | tc::kTransposeA | tc::kTransposeB;
+    const uint32_t aAddr = tc::smemAddr(dyTile), bAddr = tc::smemAddr(hTile);
+    for (uint32_t j = 0; j < kGTile / 16; j++)
+        tc::mmaBf16(dTmem, tc::smemDesc(aAddr + 2 * aLbo * j, aLbo, 128), tc::smemDesc(bAddr + 2 * bLbo * j, bLbo, 128),
+                    idesc, (accumulate || j > 0) ? 1u : 0u);
+}
+
+// bias[o] += sum_r dy[r][o] for this tile (fp32 dy)
+__device__ __forceinline__ void accumBias(float *gb, int nOut, const float *dy) {
     for (int o = threadIdx.x; o < nOut; o += kGTile) {
         float s = 0.0f;
         for (int r = 0; r < kGTile; r++) s += dy[r * kTrainStride + o];
-        gw[offB + o] += s;
+        gb[o] += s;
+    }
+}
+
+// one M = 64 weight-gradient accumulator -> grad[offW + o * nIn + i] (atomic); every
+// thread takes part (tcgen05.ld is warp-wide), lanes 0-15 of each warp hold its rows
+__device__ __forceinline__ void flushWeightGrad(uint32_t dTmem, uint32_t nCols, int offW, int nOut, int nIn,
+                                                float *grad) {
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int o = static_cast<int>(16 * warp + lane);
+    for (uint32_t c = 0; c < nCols; c += 16) {
+        float v[16];
+        tc::tmemLoad16(dTmem + ((warp * 32u) << 16) + c, v);
+        if (lane < 16 && o < nOut)
+            for (int i = 0; i < 16; i++)
+                if (static_cast<int>(c) + i < nIn) atomicAdd(&grad[offW + o * nIn + c + i], v[i]);
     }
 }
 
@@ -178,7 +209,7 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
     uint8_t *x = sm + TrainLayout::x, *h1 = sm + TrainLayout::h1, *h2 = sm + TrainLayout::h2,
             *h3 = sm + TrainLayout::h3, *dyb = sm + TrainLayout::dyb;
     float *dy = reinterpret_cast<float *>(sm + TrainLayout::dy);
-    float *gw = reinterpret_cast<float *>(sm + TrainLayout::gw);
+    float *gb = reinterpret_cast<float *>(sm + TrainLayout::gb);   // bias gradients B1 | B2 | B3 | B4
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + TrainLayout::bar);
     uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + TrainLayout::tmem);
     const int t = threadIdx.x;
@@ -192,10 +223,10 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
     for (int i = t; i < kPackBwdBytes / 16; i += kGTile)
         reinterpret_cast<uint4 *>(wb)[i] = reinterpret_cast<const uint4 *>(packBwd)[i];
     for (int i = t; i < kBiasPad; i += kGTile) bias[i] = biasPad[i];
-    for (int i = t; i < kGParams; i += kGTile) gw[i] = 0.0f;
+    for (int i = t; i < kBiasPad; i += kGTile) gb[i] = 0.0f;
     if (t == 0) tc::mbarInit(bar, 1);
     if (t < 32) {
-        tc::tmemAlloc(tmemSlot, 64);
+        tc::tmemAlloc(tmemSlot, kTrainTmemCols);
         tc::tmemRelinquish();
     }
     tc::fenceBeforeSync();
@@ -205,6 +236,7 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
     uint32_t phase = 0;
     bool ok = true;
     float lossSum = 0.0f, wSum = 0.0f;
+    bool acc = false;   // weight-gradient accumulators hold this CTA's earlier tiles
     const uint8_t *w2b = wb, *w3b = wb + kW2fBytes, *w4b = wb + 2 * kW2fBytes;
     for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
         const int s = tile * kGTile + t;
@@ -235,32 +267,63 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
             for (int j = 0; j < kGN4; j += 8) storeRow8(dyb, t, j, kGN4, g + j);
         }
         __syncthreads();
-        accumLayer(gw, kOffW4, kOffB4, kGOut, kGHid, dy, h3, kGHid);
-        ok = tileMma(tmem, dyb, w4b, kGN4, kGHid, bar, phase);   // dX3 = dY4 W4
+        // each layer: its bias gradient on the CUDA cores, then one commit for the
+        // backward MMA (dX = dY W) and the weight-gradient MMA (dW += dY^T H), which
+        // read the same dY tile
+        accumBias(gb + 3 * kGHid, kGOut, dy);
+        ok = mmaRun(bar, phase, [&] {
+            issueTileMma(tmem, dyb, w4b, kGN4, kGHid);                    // dX3 = dY4 W4
+            issueWeightGrad(tmem + kColDW4, dyb, kGN4, h3, kGHid, acc);   // dW4 += dY4^T H3
+        });
         if (!ok) break;
         backEpilogue(tmem, h3, dy, dyb);
         __syncthreads();
-        accumLayer(gw, kOffW3, kOffB3, kGHid, kGHid, dy, h2, kGHid);
-        ok = tileMma(tmem, dyb, w3b, kGHid, kGHid, bar, phase);   // dX2 = dY3 W3
+        accumBias(gb + 2 * kGHid, kGHid, dy);
+        ok = mmaRun(bar, phase, [&] {
+            issueTileMma(tmem, dyb, w3b, kGHid, kGHid);                   // dX2 = dY3 W3
+            issueWeightGrad(tmem + kColDW3, dyb, kGHid, h2, kGHid, acc);  // dW3 += dY3^T H2
+        });
         if (!ok) break;
         backEpilogue(tmem, h2, dy, dyb);
         __syncthreads();
-        accumLayer(gw, kOffW2, kOffB2, kGHid, kGHid, dy, h1, kGHid);
-        ok = tileMma(tmem, dyb, w2b, kGHid, kGHid, bar, phase);   // dX1 = dY2 W2
+        accumBias(gb + kGHid, kGHid, dy);
+        ok = mmaRun(bar, phase, [&] {
+            issueTileMma(tmem, dyb, w2b, kGHid, kGHid);                   // dX1 = dY2 W2
+            issueWeightGrad(tmem + kColDW2, dyb, kGHid, h1, kGHid, acc);  // dW2 += dY2^T H1
+        });
         if (!ok) break;
         backEpilogue(tmem, h1, dy, dyb);
         __syncthreads();
-        accumLayer(gw, kOffW1, kOffB1, kGHid, kGIn, dy, x, kGK0);
-        __syncthreads();
+        accumBias(gb, kGHid, dy);
+        ok = mmaRun(bar, phase, [&] {
+            issueWeightGrad(tmem + kColDW1, dyb, kGHid, x, kGK0, acc);    // dW1 += dY1^T X
+        });
+        acc = true;
     }
-    tc::fenceBeforeSync();
-    __syncthreads();
-    if (t < 32) tc::tmemDealloc(tmem, 64);
     if (!ok) {
+        // a wait gave up: wait (bounded) for the MMAs still in flight before freeing TMEM
+        tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);
+        tc::fenceBeforeSync();
+        __syncthreads();
+        if (t < 32) tc::tmemDealloc(tmem, kTrainTmemCols);
         if (t == 0) atomicOr(err, 1);
         return;
     }
-    for (int i = t; i < kGParams; i += kGTile) atomicAdd(&grad[i], gw[i]);
+    if (acc) {
+        flushWeightGrad(tmem + kColDW4, kGHid, kOffW4, kGOut, kGHid, grad);
+        flushWeightGrad(tmem + kColDW3, kGHid, kOffW3, kGHid, kGHid, grad);
+        flushWeightGrad(tmem + kColDW2, kGHid, kOffW2, kGHid, kGHid, grad);
+        flushWeightGrad(tmem + kColDW1, kGK0, kOffW1, kGHid, kGIn, grad);
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (t < 32) tc::tmemDealloc(tmem, kTrainTmemCols);
+    for (int o = t; o < kGHid; o += kGTile) {
+        atomicAdd(&grad[kOffB1 + o], gb[o]);
+        atomicAdd(&grad[kOffB2 + o], gb[kGHid + o]);
+        atomicAdd(&grad[kOffB3 + o], gb[2 * kGHid + o]);
+        if (o < kGOut) atomicAdd(&grad[kOffB4 + o], gb[3 * kGHid + o]);
+    }
     for (int off = 16; off > 0; off >>= 1) {
         lossSum += __shfl_xor_sync(0xffffffffu, lossSum, off);
         wSum += __shfl_xor_sync(0xffffffffu, wSum, off);

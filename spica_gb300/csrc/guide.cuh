@@ -129,25 +129,32 @@ __device__ __forceinline__ float loadBf16(const uint8_t *tile, uint32_t r, uint3
     return __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(tile + tc::kmajorOffset(r, k, K)));
 }
 
-// D = A x B over K (multiple of 16), issued by thread 0; returns once the tensor core
-// is done (all threads wait on the barrier).  Returns false on a timed-out wait (the
-// CTA-wide result is uniform).
+// D = A x B over K (multiple of 16) for a 128-row tile: A [128][K], B [N][K], both
+// K-major canonical tiles; called by the issuing thread only
+__device__ __forceinline__ void issueTileMma(uint32_t tmem, const uint8_t *a, const uint8_t *b, uint32_t K,
+                                             uint32_t N) {
+    const uint32_t sbo = (K / 8) * 128;
+    const uint32_t idesc = tc::instrDescBf16(128, N);
+    const uint32_t aAddr = tc::smemAddr(a), bAddr = tc::smemAddr(b);
+    for (uint32_t j = 0; j < K / 16; j++)
+        tc::mmaBf16(tmem, tc::smemDesc(aAddr + 256 * j, 128, sbo), tc::smemDesc(bAddr + 256 * j, 128, sbo), idesc,
+                    j > 0 ? 1u : 0u);
+}
+
+// Runs issue() on thread 0 after making the CTA's shared-memory writes visible to the
+// tensor core, commits, and waits (all threads) until every MMA it issued is done.
+// Returns false on a timed-out wait (the CTA-wide result is uniform).
 // withhold = true (fault injection in tests) issues nothing, so the barrier is never
 // signalled and the bounded wait of maxTries polls runs out.
-__device__ __forceinline__ bool tileMma(uint32_t tmem, const uint8_t *a, const uint8_t *b, uint32_t K, uint32_t N,
-                                        uint64_t *bar, uint32_t &phase, bool withhold = false,
-                                        uint32_t maxTries = kMmaWaitTries) {
+template <class Issue>
+__device__ __forceinline__ bool mmaRun(uint64_t *bar, uint32_t &phase, Issue &&issue, bool withhold = false,
+                                       uint32_t maxTries = kMmaWaitTries) {
     tc::fenceBeforeSync();
     tc::fenceAsyncShared();
     __syncthreads();
     if (threadIdx.x == 0 && !withhold) {
         tc::fenceAfterSync();
-        const uint32_t sbo = (K / 8) * 128;
-        const uint32_t idesc = tc::instrDescBf16(128, N);
-        const uint32_t aAddr = tc::smemAddr(a), bAddr = tc::smemAddr(b);
-        for (uint32_t j = 0; j < K / 16; j++)
-            tc::mmaBf16(tmem, tc::smemDesc(aAddr + 256 * j, 128, sbo), tc::smemDesc(bAddr + 256 * j, 128, sbo), idesc,
-                        j > 0 ? 1u : 0u);
+        issue();
         tc::mmaCommit(bar);
     }
     const bool ok = tc::mbarWait(bar, phase, maxTries);
@@ -155,6 +162,13 @@ __device__ __forceinline__ bool tileMma(uint32_t tmem, const uint8_t *a, const u
     const bool allOk = __syncthreads_and(ok) != 0;
     tc::fenceAfterSync();
     return allOk;
+}
+
+// D = A x B (issueTileMma), returning once the tensor core is done
+__device__ __forceinline__ bool tileMma(uint32_t tmem, const uint8_t *a, const uint8_t *b, uint32_t K, uint32_t N,
+                                        uint64_t *bar, uint32_t &phase, bool withhold = false,
+                                        uint32_t maxTries = kMmaWaitTries) {
+    return mmaRun(bar, phase, [&] { issueTileMma(tmem, a, b, K, N); }, withhold, maxTries);
 }
 
 // this thread's row (its TMEM lane) of the accumulator, columns [c0, c0 + 16)

@@ -9,6 +9,16 @@
 // so core matrices adjacent along K are 128 bytes apart (leading byte offset) and those
 // adjacent along rows are K/8 * 128 bytes apart (stride byte offset).  One
 // tcgen05.mma of kind::f16 consumes K = 16, i.e. two core matrices along K.
+//
+// The same tile read as the transpose (an MN-major operand, instruction-descriptor
+// transpose bits): its rows become the MMA's K and its columns the MMA's M (or N).  For
+// MN-major operands without swizzling the stride byte offset is the distance between
+// core matrices along M (N) -- 128 bytes here -- and the leading byte offset the
+// distance between core matrices along K -- cols/8 * 128 bytes here.
+//
+// Accumulator placement in tensor memory (cta_group::1): for M = 128, row r is lane r;
+// for M = 64, rows 16w .. 16w + 15 are lanes 32w .. 32w + 15 (lanes 0-15 of each warp's
+// quarter), columns 0 .. N-1 in both cases.
 #pragma once
 
 #include <cstdint>
@@ -79,6 +89,10 @@ __device__ __forceinline__ uint64_t smemDesc(uint32_t addr, uint32_t lbo, uint32
 __host__ __device__ constexpr uint32_t instrDescBf16(uint32_t M, uint32_t N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
+
+// instruction-descriptor bits: A (B) is read MN-major, i.e. transposed
+constexpr uint32_t kTransposeA = 1u << 15;
+constexpr uint32_t kTransposeB = 1u << 16;
 
 // D[tmem] (+)= A * B, issued by a single thread
 __device__ __forceinline__ void mmaBf16(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc,

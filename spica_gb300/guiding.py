@@ -24,17 +24,41 @@ def _mean(film):
     return f[..., :3] / np.maximum(f[..., 3:4], 1)
 
 
-def render_reference(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, spp, seed=777, chunk=256):
-    """Plain high-sample reference (same estimator, plain BSDF sampling)."""
+def reference_noise(ref, ref_var):
+    """The reference's own share of relmse(img, ref): E[(I - R)^2] = E[(I - mu)^2] +
+    Var(R) for an image I independent of the reference R, so subtracting this term
+    from relmse gives the error against the converged image."""
+    return float(np.mean(ref_var / (ref ** 2 + 1e-2)))
+
+
+def render_reference(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, spp, seed=777, chunk=256,
+                     with_variance=False):
+    """Plain high-sample reference (same estimator, plain BSDF sampling); with
+    with_variance, also the per-pixel variance of its mean, from the spread of the
+    chunk means (spp // chunk independent chunks)."""
     film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
-    done = 0
+    s1 = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+    s2 = torch.zeros_like(s1)
+    prev = film[..., :3].double().clone()
+    done, chunks = 0, 0
     while done < spp:
         n = min(chunk, spp - done)
         guide.render(scene.camera, {"width": W, "height": H, "sampleCount": n, "maxDepth": scene.max_depth}, film, 0,
                      seed=seed, sample_offset=done)
         done += n
+        if with_variance:
+            cur = film[..., :3].double()
+            m = (cur - prev) / n
+            s1 += m
+            s2 += m * m
+            prev = cur.clone()
+            chunks += 1
     torch.cuda.synchronize()
-    return _mean(film)
+    if not with_variance:
+        return _mean(film)
+    mean_c = s1 / chunks
+    var = ((s2 / chunks - mean_c * mean_c) * chunks / max(chunks - 1, 1) / chunks).clamp_min(0.0)
+    return _mean(film), var.cpu().numpy()
 
 
 def render_equal_time(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, budget_ms, guided: bool,
