@@ -234,11 +234,18 @@ typedef struct {
 
 #define SPGPU_GUIDE_GUIDED 1   /* sample with the network mixture */
 #define SPGPU_GUIDE_COLLECT 2  /* record training samples */
+#define SPGPU_GUIDE_MEGAKERNEL 4 /* trace with the persistent megakernel, which runs the
+                                  * network for a whole CTA at every bounce; collection
+                                  * passes always do.  Otherwise the wavefront of
+                                  * spgpu_render traces, and at each bounce a tensor-core
+                                  * kernel runs the network over the compacted queue of
+                                  * diffuse hits before they are shaded. */
 #define SPGPU_GUIDE_PARAMS 11560
 
 int spgpu_guiding_init(spgpu_ctx *ctx, const spgpu_guiding_config *cfg);
-/* one persistent launch tracing desc->spp samples per pixel (flags 0: plain BSDF
- * sampling, the same estimator as spgpu_render); film as for spgpu_render (device) */
+/* desc->spp samples per pixel (flags 0: plain BSDF sampling, the same estimator as
+ * spgpu_render; guided rendering needs desc->integrator SPGPU_INTEGRATOR_PATH); film as
+ * for spgpu_render (device) */
 int spgpu_guiding_render(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, int32_t flags,
                          spgpu_render_stats *stats, void *stream);
 int spgpu_guiding_train(spgpu_ctx *ctx, int32_t steps, double *mean_loss);

@@ -938,8 +938,9 @@ int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
                          spgpu_render_stats *stats, void *stream) {
     NvtxRange nvtxRange("spgpu_guiding_render");
     if (!h || !d || !film || d->width <= 0 || d->height <= 0 || d->spp < 0 || d->max_depth < 0 ||
-        d->max_depth > 12 || d->integrator != SPGPU_INTEGRATOR_PATH || (reinterpret_cast<uintptr_t>(film) & 15)) {
-        setError("spgpu_guiding_render: invalid arguments (path integrator, max_depth <= 12, aligned film)");
+        d->max_depth > 12 || d->integrator != SPGPU_INTEGRATOR_PATH || (reinterpret_cast<uintptr_t>(film) & 15) ||
+        (flags & ~(SPGPU_GUIDE_GUIDED | SPGPU_GUIDE_COLLECT | SPGPU_GUIDE_MEGAKERNEL))) {
+        setError("spgpu_guiding_render: invalid arguments (path integrator, max_depth <= 12, aligned film, flags)");
         return SPGPU_EINVAL;
     }
     Ctx &C = h->c;

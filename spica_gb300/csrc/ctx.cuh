@@ -63,6 +63,7 @@ struct RenderQueues {
     float4 *rayO[2] = {nullptr, nullptr};   // [cap] origin, w = path id bits
     float4 *rayD[2] = {nullptr, nullptr};   // [cap] direction, w = tmax
     HitRecord *hits = nullptr;    // [cap]
+    float *mix = nullptr;         // [cap * 40] guided passes: mixture per diffuse hit (lazy)
     int *classQ = nullptr;        // [3*cap] ray indices per material class
     float4 *shO = nullptr;        // [2*cap] origin, w = film pixel bits
     float4 *shD = nullptr;        // [2*cap] direction, w = tmax
@@ -155,10 +156,35 @@ struct CameraView {
 };
 CameraView makeCamera(const float *camera, int width, int height);
 
-// wavefront.cu: trace desc->spp samples per pixel into film (device, float4 per pixel)
+// learned-guiding state that a guided wavefront pass reads (guide.cu fills it)
+struct GuideView {
+    const uint8_t *packFwd;   // packed bf16 forward weights
+    const float *biasPad;     // biases
+    float alpha;              // BSDF share of the one-sample proposal
+};
+
+// guide.cu: the network over one bounce's diffuse-hit queue of a wavefront pass, one
+// mixture per queue entry (kMixFloats floats at mix + 40 * entry)
+struct GuideInferArgs {
+    const int *count;           // queue length (device)
+    const int *queue;           // ray index of each entry
+    const float4 *rayO, *rayD;  // the bounce's rays
+    const HitRecord *hits;      // their closest hits
+    const TriRecord *tris;
+    const uint8_t *packFwd;
+    const float *biasPad;
+    float3 lo, invExt;          // scene box of the network's position input
+    float *mix;
+    int *err;                   // bit 1: a tensor-core wait timed out
+};
+int guideInferGrid(int device);   // call before stream capture
+void launchGuideInfer(const GuideInferArgs &a, int grid, cudaStream_t s);
+
+// wavefront.cu: trace desc->spp samples per pixel into film (device, float4 per pixel);
+// with gv, diffuse hits sample the learned guiding proposal (path integrator only)
 int renderFrame(Ctx *ctx, const float *camera, int width, int height, int spp, int sampleOffset, int maxDepth,
                 uint32_t seed, int integrator, float4 *film, unsigned long long *statsOut, float *msOut,
-                cudaStream_t stream);
+                cudaStream_t stream, const GuideView *gv = nullptr);
 // the same samples launched kernel by kernel (no graph), each timed by events, then
 // again with BVH visit counters; kernelMs/launches per kernel class
 int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,

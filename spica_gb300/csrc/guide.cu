@@ -16,6 +16,7 @@
 #include "../../include/spica_gpu.h"
 #include "ctx.cuh"
 #include "guide.cuh"
+#include "guided_shade.cuh"
 #include "shade.cuh"
 
 namespace spgpu {
@@ -384,6 +385,67 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_forward(const uint8_t *__re
 constexpr int kForwardSmem = kPackFwdBytes + kBiasPad * 4 + kGTile * kGK0 * 2 + kGTile * kGHid * 2 + kGTile * 41 * 4 + 16;
 
 // ------------------------------------------------------------------ Adam
+// Network inference over a wavefront pass's diffuse-hit queue: persistent CTAs walk
+// 128-entry tiles; each thread forms its entry's inputs from the ray and its hit (the
+// same hit point and normal the megakernel uses), the tile runs through the four
+// tensor-core layers, and each row's mixture is written for the shade kernel.
+// shared memory: packed forward weights | biases (padded to 1 KB) | input/hidden tile
+// (bf16 [128][64]) | mbarrier, TMEM slot
+constexpr int kInferSmOffBias = kPackFwdBytes;
+constexpr int kInferSmOffXH = kInferSmOffBias + 1024;
+constexpr int kInferSmOffBar = kInferSmOffXH + kGTile * kGHid * 2;
+constexpr int kInferSmem = kInferSmOffBar + 16;
+__global__ void __launch_bounds__(kGTile) k_guide_infer(GuideInferArgs a) {
+    const int n = *a.count;
+    if (static_cast<int>(blockIdx.x) * kGTile >= n) return;   // no tile for this CTA
+    extern __shared__ __align__(128) uint8_t sm[];
+    uint8_t *wf = sm;
+    float *bias = reinterpret_cast<float *>(sm + kInferSmOffBias);
+    uint8_t *xh = sm + kInferSmOffXH;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kInferSmOffBar);
+    uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int t = threadIdx.x;
+    for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
+        reinterpret_cast<uint4 *>(wf)[i] = reinterpret_cast<const uint4 *>(a.packFwd)[i];
+    for (int i = t; i < kBiasPad; i += kGTile) bias[i] = a.biasPad[i];
+    if (t == 0) tc::mbarInit(bar, 1);
+    if (t < 32) {
+        tc::tmemAlloc(tmemSlot, 64);
+        tc::tmemRelinquish();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tmem = *tmemSlot;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
+        const int j = tile * kGTile + t;
+        float xf[16];
+        for (int i = 0; i < 16; i++) xf[i] = 0.0f;
+        if (j < n) {
+            const int i = a.queue[j];
+            const float3 d = xyz(a.rayD[i]);
+            const HitRecord h = a.hits[i];
+            guideFeatures(hitPoint(xyz(a.rayO[i]), d, h.t), triNormal(a.tris[h.prim]), -d, a.lo, a.invExt, xf);
+        }
+        storeRow8(xh, t, 0, kGK0, xf);
+        storeRow8(xh, t, 8, kGK0, xf + 8);
+        float raw[kGOut];
+        ok = mlpForwardRow(tmem, wf, bias, xh, bar, phase, raw);
+        if (ok && j < n) {
+            Mixture M;
+            mixtureFromRaw(raw, M);
+            storeMixture(a.mix + static_cast<int64_t>(j) * kMixFloats, M);
+        }
+    }
+    if (!ok) tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);   // MMAs still in flight
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (t < 32) tc::tmemDealloc(tmem, 64);
+    if (!ok && t == 0) atomicOr(a.err, 2);
+}
+
 __global__ void k_adam(float *P, float *G, float *M, float *V, int n, float lr, float b1, float b2, float eps,
                        float c1, float c2) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -469,32 +531,6 @@ constexpr int kMaxRec = 13;
 __device__ __forceinline__ float lum(float3 c) { return gray(c); }
 
 // one-sample MIS mixture of cosine-weighted Lambert sampling and the vMF mixture
-struct MixProposal {
-    const Mixture *M;
-    float alpha;
-    __device__ float pdf(const MaterialRecord &m, float3 woL, float3 wiL, float3 wiW) const {
-        const float pb = bsdfPdf(m, woL, wiL);
-        return M ? alpha * pb + (1.0f - alpha) * mixturePdf(*M, wiW) : pb;
-    }
-    // returns f (times nothing), world direction, pdf; false if the sample is invalid
-    __device__ bool sample(const MaterialRecord &m, float3 woL, float3 tg, float3 bg, float3 n, float uSel,
-                           float uLobe, float u1, float u2, float3 *wiW, float3 *f, float *pdf) const {
-        float3 wiL;
-        if (!M || uSel < alpha) {
-            float pb;
-            int type;
-            const float3 fb = bsdfSample(m, woL, u1, u2, 0.0f, &wiL, &pb, &type);   // Lambert only
-            if (isBlack(fb) || pb <= 0.0f) return false;
-            *wiW = normalize(tg * wiL.x + bg * wiL.y + n * wiL.z);
-        } else {
-            *wiW = mixtureSample(*M, uLobe, u1, u2);
-            wiL = mk(dot(*wiW, tg), dot(*wiW, bg), dot(*wiW, n));
-        }
-        *f = bsdfF(m, woL, wiL);
-        *pdf = this->pdf(m, woL, wiL, *wiW);
-        return *pdf > 0.0f;
-    }
-};
 
 template <bool GUIDED, bool COLLECT>
 __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
@@ -598,11 +634,11 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
                 ends = true;
             } else {
                 const TriRecord tr = S.tris[hr.prim];
-                n = normalize(cross(xyz(tr.v1) - xyz(tr.v0), xyz(tr.v2) - xyz(tr.v0)));
+                n = triNormal(tr);
                 const int2 sh = __ldg(&S.slotShade[hr.prim]);
                 m = S.mats[sh.x];
                 lightOf = sh.y;
-                ps = o + d * hr.t;
+                ps = hitPoint(o, d, hr.t);
                 if (COLLECT && recLast && lightOf >= 0 && dot(n, -d) > 0.0f) {
                     const LightRecord &Lr = S.lights[lightOf];
                     const float lp = hr.t * hr.t / (dot(n, -d) * Lr.p0.w);
@@ -636,134 +672,21 @@ __global__ void __launch_bounds__(kGTile) k_guided(GuidedArgs a) {
                 shadeHit(S, hr, o, d, beta, spec, b, a.maxDepth, a.seed, static_cast<uint32_t>(fi), sample, fi, R);
                 recLast = false;
             } else {
-                // the wavefront's shadeHit for a Lambert hit, with the BSDF strategy replaced
-                // by the mixture proposal (NEE weights use its pdf too)
-                R.emit = mk(0, 0, 0);
-                R.cont = R.sh0 = R.sh1 = false;
-                if ((b == 0 || spec) && lightOf >= 0 && dot(n, -d) > 0.0f) R.emit = beta * xyz(S.lights[lightOf].L);
-                MixProposal P{&mix, a.alpha};
-                float3 tg, bg;
-                onb(n, &tg, &bg);
-                const float3 wo = -d;
-                const float3 woL = mk(dot(wo, tg), dot(wo, bg), dot(wo, n));
-                const Rand4 r0 = rand4(a.seed, static_cast<uint32_t>(fi), sample, static_cast<uint32_t>(b), 0u);
-                const Rand4 r1 = rand4(a.seed, static_cast<uint32_t>(fi), sample, static_cast<uint32_t>(b), 1u);
-                const Rand4 r2 = rand4(a.seed, static_cast<uint32_t>(fi), sample, static_cast<uint32_t>(b), 2u);
-                if (S.nLights > 0) {
-                    const int nL = S.nLights;
-                    const int li = min(static_cast<int>(r0.a * nL), nL - 1);
-                    const bool isEnv = li >= S.nArea;
-                    const float3 scale = beta * static_cast<float>(nL);
-                    float3 wi = mk(0, 0, 0), Li = mk(0, 0, 0), target = mk(0, 0, 0), tn = mk(0, 0, 0);
-                    float lightPdf = 0.0f;
-                    if (!isEnv) {
-                        const LightRecord Lr = S.lights[S.lightBase + li];
-                        float u0 = r0.b, u1 = r0.c;
-                        if (u0 + u1 >= 1.0f) {
-                            u0 = 1.0f - u0;
-                            u1 = 1.0f - u1;
-                        }
-                        target = xyz(Lr.p0) + xyz(Lr.e1) * u0 + xyz(Lr.e2) * u1;
-                        tn = xyz(Lr.n);
-                        wi = normalize(target - ps);
-                        float tl;
-                        lightPdf = lightTriPdf(Lr, ps, n, wi, &tl);
-                        if (dot(tn, -wi) > 0.0f) Li = xyz(Lr.L);
-                    } else {
-                        const DeviceEnv &E = S.env;
-                        float pv, pu;
-                        int vOff, uOff;
-                        const float vv = sample1D(E.margCdf, E.margFunc, E.h, E.margIntegral, r0.c, &pv, &vOff);
-                        const float uu = sample1D(E.condCdf + static_cast<int64_t>(vOff) * (E.w + 1),
-                                                  E.condFunc + static_cast<int64_t>(vOff) * E.w, E.w,
-                                                  __ldg(&E.margFunc[vOff]), r0.b, &pu, &uOff);
-                        const float mapPdf = pu * pv;
-                        if (mapPdf > 0.0f) {
-                            float st, ct, sp, cp;
-                            sincosf(vv * kPi, &st, &ct);
-                            sincosf(uu * 2.0f * kPi, &sp, &cp);
-                            wi = mk(st * cp, st * sp, ct);
-                            lightPdf = st == 0.0f ? 0.0f : mapPdf / (2.0f * kPi * kPi * st);
-                            Li = envLookup(E, uu, vv);
-                            target = ps + wi * (2.0f * E.radius);
-                        }
-                    }
-                    if (lightPdf > 0.0f && !isBlack(Li)) {
-                        const float3 wiL = mk(dot(wi, tg), dot(wi, bg), dot(wi, n));
-                        const float3 f = bsdfF(m, woL, wiL) * fabsf(dot(wi, n));
-                        if (!isBlack(f)) {
-                            const float w = powerHeuristic(lightPdf, P.pdf(m, woL, wiL, wi));
-                            const float3 c = scale * f * Li * (w / lightPdf);
-                            const float3 oo = offsetOrigin(ps, n, target - ps);
-                            const float3 t2 = isEnv ? mk(nextafterf(target.x, -INFINITY),
-                                                         nextafterf(target.y, -INFINITY),
-                                                         nextafterf(target.z, -INFINITY))
-                                                    : offsetOrigin(target, tn, oo - target);
-                            const float3 dd = t2 - oo;
-                            const float len = length(dd);
-                            if (len > 0.0f) {
-                                R.sh0 = true;
-                                R.s0O = make_float4(oo.x, oo.y, oo.z, 0.0f);
-                                R.s0D = make_float4(dd.x / len, dd.y / len, dd.z / len, len);
-                                R.s0L = make_float4(c.x, c.y, c.z, 0.0f);
-                            }
-                        }
-                    }
-                    // the mixture strategy of MIS
-                    float3 wi2, f2;
-                    float pdf2;
-                    if (P.sample(m, woL, tg, bg, n, r2.a, r2.b, r0.d, r1.a, &wi2, &f2, &pdf2) && !isBlack(f2)) {
-                        f2 = f2 * fabsf(dot(wi2, n));
-                        float lp = 0.0f, tl = 0.0f;
-                        float3 L2 = mk(0, 0, 0);
-                        if (!isEnv) {
-                            const LightRecord Lr = S.lights[S.lightBase + li];
-                            lp = lightTriPdf(Lr, ps, n, wi2, &tl);
-                            if (lp > 0.0f && dot(xyz(Lr.n), -wi2) > 0.0f) L2 = xyz(Lr.L);
-                        } else {
-                            lp = envPdf(S.env, wi2);
-                            if (lp > 0.0f) L2 = envLe(S.env, wi2);
-                        }
-                        if (lp > 0.0f && !isBlack(L2)) {
-                            const float w = powerHeuristic(pdf2, lp);
-                            const float3 c = scale * f2 * L2 * (w / pdf2);
-                            const float3 oo = offsetOrigin(ps, n, wi2);
-                            R.sh1 = true;
-                            R.s1O = make_float4(oo.x, oo.y, oo.z, 0.0f);
-                            R.s1D = make_float4(wi2.x, wi2.y, wi2.z, isEnv ? kInfT : tl * (1.0f - 1.0e-5f));
-                            R.s1L = make_float4(c.x, c.y, c.z, 0.0f);
-                        }
-                    }
-                }
-                // continuation from the mixture, Russian roulette
-                float3 wi, f;
+                float3 fc;
                 float pdf;
-                R.beta = beta;
-                R.spec = false;
-                if (COLLECT) recLast = false;
-                if (P.sample(m, woL, tg, bg, n, r2.c, r2.d, r1.b, r1.c, &wi, &f, &pdf) && !isBlack(f)) {
-                    const float3 fc = f * fabsf(dot(wi, n));
-                    R.beta = beta * fc * (1.0f / pdf);
-                    R.cont = true;
-                    if (b > 3) {
-                        const float q = fminf(0.95f, gray(R.beta));
-                        if (r1.d > q) R.cont = false;
-                        else R.beta = R.beta / q;
-                    }
-                    if (R.cont) {
-                        const float3 oo = offsetOrigin(ps, n, wi);
-                        R.cO = make_float4(oo.x, oo.y, oo.z, 0.0f);
-                        R.cD = make_float4(wi.x, wi.y, wi.z, kInfT);
-                        if (COLLECT && nrec < kMaxRec) {
-                            TrainRec &T = rec[nrec++];
-                            guideFeatures(ps, n, wo, a.lo, a.invExt, T.x);
-                            T.w = wi;
-                            T.q = pdf;
-                            T.fcos = fc;
-                            T.beta = R.beta;
-                            T.E = mk(0, 0, 0);
-                            recLast = true;
-                        }
+                shadeGuidedLambert(S, ps, n, m, lightOf, d, beta, spec, b, mix, a.alpha, a.seed,
+                                   static_cast<uint32_t>(fi), sample, R, &fc, &pdf);
+                if (COLLECT) {
+                    recLast = false;
+                    if (R.cont && nrec < kMaxRec) {
+                        TrainRec &T = rec[nrec++];
+                        guideFeatures(ps, n, -d, a.lo, a.invExt, T.x);
+                        T.w = xyz(R.cD);
+                        T.q = pdf;
+                        T.fcos = fc;
+                        T.beta = R.beta;
+                        T.E = mk(0, 0, 0);
+                        recLast = true;
                     }
                 }
             }
@@ -852,6 +775,8 @@ void setGuideKernelAttributes() {
                              cudaSharedmemCarveoutMaxShared);
         cudaFuncSetAttribute(k_guided<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
         cudaGetLastError();
     });
 }
@@ -861,7 +786,7 @@ void setGuideKernelAttributes() {
 // register count and the device's limits.  (The occupancy API reports a single CTA
 // per SM for kernels that allocate tensor memory; co-resident CTAs are fine as long as
 // their allocations fit the SM's 512 TMEM columns, which the last term ensures.)
-int tmemKernelResidentCtas(const void *kernel, int device) {
+int tmemKernelResidentCtas(const void *kernel, int device, int dynSmem = kGuidedSmem) {
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
         cudaGetLastError();
@@ -876,7 +801,7 @@ int tmemKernelResidentCtas(const void *kernel, int device) {
     const int warps = kGTile / 32;
     const int regsPerWarp = ((fa.numRegs * 32 + 255) / 256) * 256;
     const int byRegs = regsPerWarp > 0 ? regsSM / (regsPerWarp * warps) : 1;
-    const int bySmem = smemSM / (kGuidedSmem + static_cast<int>(fa.sharedSizeBytes) + smemReserved);
+    const int bySmem = smemSM / (dynSmem + static_cast<int>(fa.sharedSizeBytes) + smemReserved);
     const int byThreads = thrSM / kGTile;
     constexpr int byTmem = 512 / 64;
     return std::max(1, std::min(std::min(byRegs, bySmem), std::min(std::min(byThreads, blkSM), byTmem)));
@@ -895,6 +820,17 @@ int packWeights(GuideState &G, cudaStream_t s) {
 }
 
 }  // namespace
+
+int guideInferGrid(int device) {
+    setGuideKernelAttributes();
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    return sms * tmemKernelResidentCtas(reinterpret_cast<const void *>(k_guide_infer), device, kInferSmem);
+}
+
+void launchGuideInfer(const GuideInferArgs &a, int grid, cudaStream_t s) {
+    k_guide_infer<<<grid, kGTile, kInferSmem, s>>>(a);
+}
 
 void freeGuide(GuideState *G) {
     if (!G) return;
@@ -1105,6 +1041,17 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
                 unsigned long long *statsOut, float *msOut, cudaStream_t s) {
     const bool guided = (flags & 1) && G;
     const bool collect = (flags & 2) && G;
+    if (!collect && !(flags & 4)) {
+        // the wavefront, with per-bounce network inference over the diffuse hits
+        if (guided && d->integrator != SPGPU_INTEGRATOR_PATH) {
+            setError("spgpu_guiding_render: guided rendering needs the path integrator");
+            return SPGPU_EINVAL;
+        }
+        GuideView gv{guided ? G->packFwd : nullptr, guided ? G->biasPad : nullptr,
+                     guided ? G->cfg.bsdf_fraction : 1.0f};
+        return renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                           d->integrator, film, statsOut, msOut, s, guided ? &gv : nullptr);
+    }
     GuidedArgs a;
     std::memset(&a, 0, sizeof(a));
     a.sv = C.view();

@@ -10,6 +10,8 @@
 // layer's operand back to shared memory.
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "tc.cuh"
 
@@ -77,6 +79,41 @@ __device__ __forceinline__ void mixtureFromRaw(const float *raw, Mixture &M) {
     }
     for (int k = 0; k < kGLobes; k++) M.w[k] /= s;
 }
+// a mixture in global memory: lobe axes (x, y, z per lobe) | concentrations | weights,
+// 40 floats (160 bytes, 16-byte aligned)
+constexpr int kMixFloats = 5 * kGLobes;
+__device__ __forceinline__ void storeMixture(float *dst, const Mixture &M) {
+    float v[kMixFloats];
+#pragma unroll
+    for (int k = 0; k < kGLobes; k++) {
+        v[3 * k] = M.mu[k].x;
+        v[3 * k + 1] = M.mu[k].y;
+        v[3 * k + 2] = M.mu[k].z;
+        v[3 * kGLobes + k] = M.kappa[k];
+        v[4 * kGLobes + k] = M.w[k];
+    }
+#pragma unroll
+    for (int i = 0; i < kMixFloats / 4; i++)
+        reinterpret_cast<float4 *>(dst)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+__device__ __forceinline__ void loadMixture(const float *src, Mixture &M) {
+    float v[kMixFloats];
+#pragma unroll
+    for (int i = 0; i < kMixFloats / 4; i++) {
+        const float4 q = __ldg(reinterpret_cast<const float4 *>(src) + i);
+        v[4 * i] = q.x;
+        v[4 * i + 1] = q.y;
+        v[4 * i + 2] = q.z;
+        v[4 * i + 3] = q.w;
+    }
+#pragma unroll
+    for (int k = 0; k < kGLobes; k++) {
+        M.mu[k] = mk(v[3 * k], v[3 * k + 1], v[3 * k + 2]);
+        M.kappa[k] = v[3 * kGLobes + k];
+        M.w[k] = v[4 * kGLobes + k];
+    }
+}
+
 __device__ __forceinline__ float mixturePdf(const Mixture &M, float3 w) {
     float p = 0.0f;
     for (int k = 0; k < kGLobes; k++) p += M.w[k] * vmfPdf(w, M.mu[k], M.kappa[k]);

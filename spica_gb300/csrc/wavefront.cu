@@ -32,6 +32,7 @@
 
 #include "../../include/spica_gpu.h"
 #include "ctx.cuh"
+#include "guided_shade.cuh"
 #include "shade.cuh"
 
 namespace spgpu {
@@ -59,6 +60,13 @@ struct PassArgs {
     int *ctl;          // [0] sample index of the pass
     int ctlStride;     // sample-index step from one pass of this queue set to its next
     int direct;        // direct lighting: no continuation rays after the first hit
+    // learned guiding (packFwd == nullptr: plain pass): network weights, scene box of its
+    // position input, BSDF share of the proposal, mixture per diffuse-queue entry
+    const uint8_t *packFwd;
+    const float *biasPad;
+    float3 guideLo, guideInvExt;
+    float guideAlpha;
+    float *mix;
     unsigned long long *stats;
     unsigned long long *visit;   // [0..1] extend nodes / triangles, [2..3] shadow nodes / triangles
     int *err;
@@ -154,7 +162,9 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_extend(PassArgs p, int b) {
     }
 }
 
-template <int CLS>
+// GUIDED (diffuse class, bounces before the last): the hit samples the learned proposal
+// whose mixture k_guide_infer wrote for its queue entry
+template <int CLS, bool GUIDED = false>
 __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
     const int *cnt = p.counters + b * kCountersPerBounce;
     const int n = cnt[1 + CLS];
@@ -178,8 +188,20 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
             pid = __float_as_int(o4.w);
             const float4 bt = p.beta[pid];
             const int fi = filmIndex(p, pid);
-            shadeHit(p.sv, p.hits[i], xyz(o4), xyz(d4), xyz(bt), bt.w != 0.0f, b, p.maxDepth, p.seed,
-                     static_cast<uint32_t>(fi), sample, fi, R, p.direct != 0);
+            if (GUIDED) {
+                const HitRecord h = p.hits[i];
+                const int2 sh = __ldg(&p.sv.slotShade[h.prim]);
+                Mixture M;
+                loadMixture(p.mix + static_cast<int64_t>(j) * kMixFloats, M);
+                float3 fc;
+                float pdf;
+                shadeGuidedLambert(p.sv, hitPoint(xyz(o4), xyz(d4), h.t), triNormal(p.sv.tris[h.prim]),
+                                   p.sv.mats[sh.x], sh.y, xyz(d4), xyz(bt), bt.w != 0.0f, b, M, p.guideAlpha, p.seed,
+                                   static_cast<uint32_t>(fi), sample, R, &fc, &pdf);
+            } else {
+                shadeHit(p.sv, p.hits[i], xyz(o4), xyz(d4), xyz(bt), bt.w != 0.0f, b, p.maxDepth, p.seed,
+                         static_cast<uint32_t>(fi), sample, fi, R, p.direct != 0);
+            }
             if (!isBlack(R.emit)) filmAdd(p.film, fi, R.emit);
         }
         const int k = warpAppend(R.cont && !p.direct, nextCnt);
@@ -278,7 +300,7 @@ int ensureQueues(RenderQueues &q, int64_t npix, int maxDepth) {
 }
 
 struct Grids {
-    int trace, shade, raygen;
+    int trace, shade, raygen, infer;
 };
 
 Grids passGrids(int device, int64_t npix) {
@@ -291,6 +313,7 @@ Grids passGrids(int device, int64_t npix) {
     g.trace = sms * std::max(occT, 1);
     g.shade = sms * std::max(occS, 1);
     g.raygen = static_cast<int>(std::min<int64_t>((npix + 255) / 256, static_cast<int64_t>(sms) * 8));
+    g.infer = 0;
     return g;
 }
 
@@ -319,7 +342,25 @@ void launchPass(const PassArgs &a, const Grids &g, cudaStream_t cs, size_t ctrBy
         k_extend<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
         done();
         mark(kShadeL);
-        k_shade<kMatLambert><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
+        if (a.packFwd && b < a.maxDepth) {
+            GuideInferArgs ia;
+            ia.count = a.counters + b * kCountersPerBounce + 1 + kMatLambert;
+            ia.queue = a.classQ + kMatLambert * a.cap;
+            ia.rayO = (b & 1) ? a.rayO1 : a.rayO0;
+            ia.rayD = (b & 1) ? a.rayD1 : a.rayD0;
+            ia.hits = a.hits;
+            ia.tris = a.sv.tris;
+            ia.packFwd = a.packFwd;
+            ia.biasPad = a.biasPad;
+            ia.lo = a.guideLo;
+            ia.invExt = a.guideInvExt;
+            ia.mix = a.mix;
+            ia.err = a.err;
+            launchGuideInfer(ia, g.infer, cs);
+            k_shade<kMatLambert, true><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
+        } else {
+            k_shade<kMatLambert><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
+        }
         done();
         mark(kShadeC);
         k_shade<kMatConductor><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
@@ -352,6 +393,7 @@ void freeRenderQueues(RenderQueues *q) {
         cudaFree(q->rayD[k]);
     }
     cudaFree(q->hits);
+    cudaFree(q->mix);
     cudaFree(q->classQ);
     cudaFree(q->shO);
     cudaFree(q->shD);
@@ -364,10 +406,15 @@ void freeRenderQueues(RenderQueues *q) {
 
 namespace {
 int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int maxDepth, uint32_t seed, float4 *film,
-              int ctlStride, int integrator, PassArgs *out) {
+              int ctlStride, int integrator, const GuideView *gv, PassArgs *out) {
     const int64_t npix = static_cast<int64_t>(W) * H;
     int rc = ensureQueues(q, npix, maxDepth);
     if (rc) return rc;
+    if (gv && !q.mix && cudaMalloc(&q.mix, sizeof(float) * kMixFloats * q.capacity) != cudaSuccess) {
+        q.mix = nullptr;
+        setError("spgpu_render: device allocation of the guiding mixtures failed");
+        return SPGPU_ENOMEM;
+    }
     PassArgs &a = *out;
     std::memset(&a, 0, sizeof(a));
     a.sv = C.view();
@@ -396,6 +443,16 @@ int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int ma
     a.err = q.err;
     a.ctlStride = ctlStride;
     a.direct = integrator == SPGPU_INTEGRATOR_DIRECT ? 1 : 0;
+    if (gv) {
+        a.packFwd = gv->packFwd;
+        a.biasPad = gv->biasPad;
+        a.guideAlpha = gv->alpha;
+        a.mix = q.mix;
+        const float3 ext = C.bvh.hi - C.bvh.lo;
+        a.guideLo = C.bvh.lo;
+        a.guideInvExt = mk(ext.x > 0 ? 1.0f / ext.x : 0.0f, ext.y > 0 ? 1.0f / ext.y : 0.0f,
+                           ext.z > 0 ? 1.0f / ext.z : 0.0f);
+    }
     return 0;
 }
 
@@ -412,7 +469,8 @@ int ensurePassGraph(Ctx &C, RenderQueues &q, const PassArgs &a, int W, int H, in
         cudaGraphExecDestroy(q.graph);
         q.graph = nullptr;
     }
-    const Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
+    Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
+    if (a.packFwd) gr.infer = guideInferGrid(C.device);   // attributes and grid before capture
     const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;
     cudaStream_t cs = C.stream;
     cudaGraph_t g = nullptr;
@@ -430,7 +488,8 @@ int ensurePassGraph(Ctx &C, RenderQueues &q, const PassArgs &a, int W, int H, in
 }  // namespace
 
 int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
-                int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
+                int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream,
+                const GuideView *gv) {
     Ctx &C = *ctx;
     // direct lighting shades the first hit only, with light sampling whatever max_depth says
     if (integrator == SPGPU_INTEGRATOR_DIRECT) maxDepth = 1;
@@ -446,7 +505,7 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
     }
     for (int k = 0; k < lanes; k++) {
         PassArgs a;
-        int rc = setupPass(C, *qs[k], camera, W, H, maxDepth, seed, film, lanes, integrator, &a);
+        int rc = setupPass(C, *qs[k], camera, W, H, maxDepth, seed, film, lanes, integrator, gv, &a);
         if (!rc) rc = ensurePassGraph(C, *qs[k], a, W, H, maxDepth, seed, film);
         if (rc) return rc;
     }
@@ -490,7 +549,8 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
     }
     *msOut = ms;
     if (anyErr) {
-        setError("spgpu_render: traversal stack overflow");
+        setError((anyErr & 2) ? "spgpu_render: guiding network tensor-core wait timed out"
+                              : "spgpu_render: traversal stack overflow");
         return SPGPU_EKERNEL;
     }
     return 0;
@@ -503,7 +563,7 @@ int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int samp
     RenderQueues &q = C.rq;
     PassArgs a;
     if (integrator == SPGPU_INTEGRATOR_DIRECT) maxDepth = 1;
-    int rc = setupPass(C, q, camera, W, H, maxDepth, seed, film, 1, integrator, &a);
+    int rc = setupPass(C, q, camera, W, H, maxDepth, seed, film, 1, integrator, nullptr, &a);
     if (rc) return rc;
     const Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
     const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;

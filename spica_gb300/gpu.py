@@ -76,7 +76,7 @@ class GuidingConfig(C.Structure):
                 ("reserved", C.c_int32 * 2)]
 
 
-GUIDE_GUIDED, GUIDE_COLLECT = 1, 2
+GUIDE_GUIDED, GUIDE_COLLECT, GUIDE_MEGAKERNEL = 1, 2, 4
 FILM_RGBE, FILM_GAMMA_BYTES, FILM_REINHARD = 0, 1, 2
 
 

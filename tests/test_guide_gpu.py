@@ -7,7 +7,7 @@ import pytest
 from oracle import guide_oracle as go
 from parity import zscores
 from spica_gb300 import GpuBVHAccel, GpuGuide, scenes
-from spica_gb300.gpu import GUIDE_COLLECT, GUIDE_GUIDED
+from spica_gb300.gpu import GUIDE_COLLECT, GUIDE_GUIDED, GUIDE_MEGAKERNEL
 
 pytestmark = pytest.mark.gpu
 
@@ -100,7 +100,8 @@ def test_training_reduces_loss_and_guided_render_is_unbiased(gpulib):
 
 
 def test_plain_megakernel_matches_wavefront(gpulib):
-    """flags 0 is the same estimator as spgpu_render: same film from the same streams."""
+    """The plain megakernel is the same estimator as spgpu_render: same film from the
+    same streams."""
     import torch
     from spica_gb300 import GpuPathIntegrator
     sc = _room(20)
@@ -108,12 +109,41 @@ def test_plain_megakernel_matches_wavefront(gpulib):
     acc = GpuBVHAccel(sc).construct()
     g = GpuGuide(acc, seed=1)
     f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
-    g.render(sc.camera, {"width": W, "height": H, "sampleCount": 16, "maxDepth": sc.max_depth}, f, 0, seed=4)
+    g.render(sc.camera, {"width": W, "height": H, "sampleCount": 16, "maxDepth": sc.max_depth}, f, GUIDE_MEGAKERNEL,
+             seed=4)
     ref = GpuPathIntegrator(seed=4).render(sc.camera, acc, {"width": W, "height": H, "sampleCount": 16,
                                                             "maxDepth": sc.max_depth})
     got = f.cpu().numpy()
     assert np.array_equal(got[..., 3], ref[..., 3])
     np.testing.assert_allclose(got[..., :3], ref[..., :3], rtol=2e-3, atol=2e-3)
+
+
+def test_guided_wavefront_matches_guided_megakernel(gpulib):
+    """Guided rendering in the wavefront (network run per bounce over the queue of diffuse
+    hits) and in the megakernel (network run per CTA at each bounce) are the same
+    estimator: the same inputs reach the network, a row's outputs do not depend on the
+    other rows of its tile, and both shade with the same code and sampler streams, so
+    the films agree up to the order of the film's atomic additions."""
+    import torch
+    sc = _room(40)
+    W, H = 64, 40
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=5)
+    p = {"width": W, "height": H, "maxDepth": sc.max_depth}
+    scratch = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    for k in range(6):
+        g.render(sc.camera, dict(p, sampleCount=4), scratch, GUIDE_GUIDED | GUIDE_COLLECT, seed=70, sample_offset=4 * k)
+        g.train(16)
+    films = []
+    for flags in (GUIDE_GUIDED, GUIDE_GUIDED | GUIDE_MEGAKERNEL):
+        f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        st = g.render(sc.camera, dict(p, sampleCount=16), f, flags, seed=8, sample_offset=0)
+        assert st.paths == W * H * 16
+        films.append(f.cpu().numpy())
+    a, b = films
+    assert np.array_equal(a[..., 3], b[..., 3])
+    assert a[..., :3].sum() > 0
+    np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=2e-3, atol=2e-3)
 
 
 def test_trained_guide_lowers_error_per_sample(gpulib):
