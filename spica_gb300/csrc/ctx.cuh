@@ -63,7 +63,11 @@ struct RenderQueues {
     float4 *rayO[2] = {nullptr, nullptr};   // [cap] origin, w = path id bits
     float4 *rayD[2] = {nullptr, nullptr};   // [cap] direction, w = tmax
     HitRecord *hits = nullptr;    // [cap]
-    float *mix = nullptr;         // [cap * 40] guided passes: mixture per diffuse hit (lazy)
+    // training-sample collection (lazy): radiance gathered per path, record count and
+    // records per path (kCollectRecs x 7 float4 per path, wavefront.cu)
+    float4 *pathL = nullptr;
+    int *recCount = nullptr;
+    float4 *recs = nullptr;
     int *classQ = nullptr;        // [3*cap] ray indices per material class
     float4 *shO = nullptr;        // [2*cap] origin, w = film pixel bits
     float4 *shD = nullptr;        // [2*cap] direction, w = tmax
@@ -71,8 +75,10 @@ struct RenderQueues {
     int *counters = nullptr;      // [(maxDepth+2) * 8]
     unsigned long long *stats = nullptr;   // [4] paths, closest rays, shadow rays, spare
     int *err = nullptr;           // [1] kernel error flags
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;   // the pass graph last used
     uint64_t graphKey[4] = {0, 0, 0, 0};
+    cudaGraphExec_t graphAlt = nullptr;   // the one used before it (guided passes alternate
+    uint64_t graphKeyAlt[4] = {0, 0, 0, 0};   // with collection passes)
 };
 
 struct BatchState;
@@ -161,24 +167,16 @@ struct GuideView {
     const uint8_t *packFwd;   // packed bf16 forward weights
     const float *biasPad;     // biases
     float alpha;              // BSDF share of the one-sample proposal
+    bool collect;             // record training samples into the ring
+    float *ring;              // training-sample ring, 16 floats per entry
+    int capacity;
+    int *ringCtl;             // [0] entries written (monotonic)
 };
 
-// guide.cu: the network over one bounce's diffuse-hit queue of a wavefront pass, one
-// mixture per queue entry (kMixFloats floats at mix + 40 * entry)
-struct GuideInferArgs {
-    const int *count;           // queue length (device)
-    const int *queue;           // ray index of each entry
-    const float4 *rayO, *rayD;  // the bounce's rays
-    const HitRecord *hits;      // their closest hits
-    const TriRecord *tris;
-    const uint8_t *packFwd;
-    const float *biasPad;
-    float3 lo, invExt;          // scene box of the network's position input
-    float *mix;
-    int *err;                   // bit 1: a tensor-core wait timed out
-};
-int guideInferGrid(int device);   // call before stream capture
-void launchGuideInfer(const GuideInferArgs &a, int grid, cudaStream_t s);
+// guide.cu: grid of a persistent kernel that runs the network per 128-thread CTA
+// (kTileSmem bytes of dynamic shared memory, 64 TMEM columns): SMs x CTAs that fit one
+// SM; sets the kernel's shared-memory carveout (call before stream capture)
+int guideTileKernelGrid(const void *kernel, int device);
 
 // wavefront.cu: trace desc->spp samples per pixel into film (device, float4 per pixel);
 // with gv, diffuse hits sample the learned guiding proposal (path integrator only)

@@ -385,67 +385,6 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_forward(const uint8_t *__re
 constexpr int kForwardSmem = kPackFwdBytes + kBiasPad * 4 + kGTile * kGK0 * 2 + kGTile * kGHid * 2 + kGTile * 41 * 4 + 16;
 
 // ------------------------------------------------------------------ Adam
-// Network inference over a wavefront pass's diffuse-hit queue: persistent CTAs walk
-// 128-entry tiles; each thread forms its entry's inputs from the ray and its hit (the
-// same hit point and normal the megakernel uses), the tile runs through the four
-// tensor-core layers, and each row's mixture is written for the shade kernel.
-// shared memory: packed forward weights | biases (padded to 1 KB) | input/hidden tile
-// (bf16 [128][64]) | mbarrier, TMEM slot
-constexpr int kInferSmOffBias = kPackFwdBytes;
-constexpr int kInferSmOffXH = kInferSmOffBias + 1024;
-constexpr int kInferSmOffBar = kInferSmOffXH + kGTile * kGHid * 2;
-constexpr int kInferSmem = kInferSmOffBar + 16;
-__global__ void __launch_bounds__(kGTile) k_guide_infer(GuideInferArgs a) {
-    const int n = *a.count;
-    if (static_cast<int>(blockIdx.x) * kGTile >= n) return;   // no tile for this CTA
-    extern __shared__ __align__(128) uint8_t sm[];
-    uint8_t *wf = sm;
-    float *bias = reinterpret_cast<float *>(sm + kInferSmOffBias);
-    uint8_t *xh = sm + kInferSmOffXH;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kInferSmOffBar);
-    uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
-    const int t = threadIdx.x;
-    for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
-        reinterpret_cast<uint4 *>(wf)[i] = reinterpret_cast<const uint4 *>(a.packFwd)[i];
-    for (int i = t; i < kBiasPad; i += kGTile) bias[i] = a.biasPad[i];
-    if (t == 0) tc::mbarInit(bar, 1);
-    if (t < 32) {
-        tc::tmemAlloc(tmemSlot, 64);
-        tc::tmemRelinquish();
-    }
-    tc::fenceBeforeSync();
-    __syncthreads();
-    tc::fenceAfterSync();
-    const uint32_t tmem = *tmemSlot;
-    uint32_t phase = 0;
-    bool ok = true;
-    for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
-        const int j = tile * kGTile + t;
-        float xf[16];
-        for (int i = 0; i < 16; i++) xf[i] = 0.0f;
-        if (j < n) {
-            const int i = a.queue[j];
-            const float3 d = xyz(a.rayD[i]);
-            const HitRecord h = a.hits[i];
-            guideFeatures(hitPoint(xyz(a.rayO[i]), d, h.t), triNormal(a.tris[h.prim]), -d, a.lo, a.invExt, xf);
-        }
-        storeRow8(xh, t, 0, kGK0, xf);
-        storeRow8(xh, t, 8, kGK0, xf + 8);
-        float raw[kGOut];
-        ok = mlpForwardRow(tmem, wf, bias, xh, bar, phase, raw);
-        if (ok && j < n) {
-            Mixture M;
-            mixtureFromRaw(raw, M);
-            storeMixture(a.mix + static_cast<int64_t>(j) * kMixFloats, M);
-        }
-    }
-    if (!ok) tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);   // MMAs still in flight
-    tc::fenceBeforeSync();
-    __syncthreads();
-    if (t < 32) tc::tmemDealloc(tmem, 64);
-    if (!ok && t == 0) atomicOr(a.err, 2);
-}
-
 __global__ void k_adam(float *P, float *G, float *M, float *V, int n, float lr, float b1, float b2, float eps,
                        float c1, float c2) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -775,8 +714,6 @@ void setGuideKernelAttributes() {
                              cudaSharedmemCarveoutMaxShared);
         cudaFuncSetAttribute(k_guided<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
-        cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             cudaSharedmemCarveoutMaxShared);
         cudaGetLastError();
     });
 }
@@ -821,15 +758,12 @@ int packWeights(GuideState &G, cudaStream_t s) {
 
 }  // namespace
 
-int guideInferGrid(int device) {
-    setGuideKernelAttributes();
+int guideTileKernelGrid(const void *kernel, int device) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaGetLastError();
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    return sms * tmemKernelResidentCtas(reinterpret_cast<const void *>(k_guide_infer), device, kInferSmem);
-}
-
-void launchGuideInfer(const GuideInferArgs &a, int grid, cudaStream_t s) {
-    k_guide_infer<<<grid, kGTile, kInferSmem, s>>>(a);
+    return sms * tmemKernelResidentCtas(kernel, device, kTileSmem);
 }
 
 void freeGuide(GuideState *G) {
@@ -1041,14 +975,23 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
                 unsigned long long *statsOut, float *msOut, cudaStream_t s) {
     const bool guided = (flags & 1) && G;
     const bool collect = (flags & 2) && G;
-    if (!collect && !(flags & 4)) {
-        // the wavefront, with per-bounce network inference over the diffuse hits
+    if (!(flags & 4) && (guided || !collect)) {
+        // the wavefront, with per-bounce network inference over the diffuse hits (and
+        // training records when collecting)
         if (guided && d->integrator != SPGPU_INTEGRATOR_PATH) {
             setError("spgpu_guiding_render: guided rendering needs the path integrator");
             return SPGPU_EINVAL;
         }
-        GuideView gv{guided ? G->packFwd : nullptr, guided ? G->biasPad : nullptr,
-                     guided ? G->cfg.bsdf_fraction : 1.0f};
+        GuideView gv{};
+        if (guided) {
+            gv.packFwd = G->packFwd;
+            gv.biasPad = G->biasPad;
+            gv.alpha = G->cfg.bsdf_fraction;
+            gv.collect = collect;
+            gv.ring = G->samples;
+            gv.capacity = G->capacity;
+            gv.ringCtl = G->ctl;
+        }
         return renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
                            d->integrator, film, statsOut, msOut, s, guided ? &gv : nullptr);
     }

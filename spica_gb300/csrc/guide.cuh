@@ -49,11 +49,20 @@ constexpr int kBiasPad = 3 * kGHid + kGN4;                             // 240
 
 constexpr uint32_t kMmaWaitTries = 1u << 22;
 
+// shared memory of a kernel that evaluates the network for its 128-thread CTA, one tile
+// at a time: packed forward weights | biases (padded to 1 KB) | input/hidden tile (bf16
+// [128][64]) | mbarrier, TMEM slot
+constexpr int kTileSmOffBias = kPackFwdBytes;
+constexpr int kTileSmOffXH = kTileSmOffBias + 1024;
+constexpr int kTileSmOffBar = kTileSmOffXH + kGTile * kGHid * 2;
+constexpr int kTileSmem = kTileSmOffBar + 16;
+
 // ---------------------------------------------------------------- vMF mixture
 struct Mixture {
     float3 mu[kGLobes];
     float kappa[kGLobes];
     float w[kGLobes];
+    float wn[kGLobes];   // w times the lobe's normalisation, for the pdf
 };
 
 __device__ __forceinline__ float vmfNorm(float kappa) {   // kappa / (2 pi (1 - exp(-2 kappa)))
@@ -77,46 +86,14 @@ __device__ __forceinline__ void mixtureFromRaw(const float *raw, Mixture &M) {
         M.w[k] = __expf(raw[5 * k + 4] - mx);
         s += M.w[k];
     }
-    for (int k = 0; k < kGLobes; k++) M.w[k] /= s;
-}
-// a mixture in global memory: lobe axes (x, y, z per lobe) | concentrations | weights,
-// 40 floats (160 bytes, 16-byte aligned)
-constexpr int kMixFloats = 5 * kGLobes;
-__device__ __forceinline__ void storeMixture(float *dst, const Mixture &M) {
-    float v[kMixFloats];
-#pragma unroll
     for (int k = 0; k < kGLobes; k++) {
-        v[3 * k] = M.mu[k].x;
-        v[3 * k + 1] = M.mu[k].y;
-        v[3 * k + 2] = M.mu[k].z;
-        v[3 * kGLobes + k] = M.kappa[k];
-        v[4 * kGLobes + k] = M.w[k];
-    }
-#pragma unroll
-    for (int i = 0; i < kMixFloats / 4; i++)
-        reinterpret_cast<float4 *>(dst)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-}
-__device__ __forceinline__ void loadMixture(const float *src, Mixture &M) {
-    float v[kMixFloats];
-#pragma unroll
-    for (int i = 0; i < kMixFloats / 4; i++) {
-        const float4 q = __ldg(reinterpret_cast<const float4 *>(src) + i);
-        v[4 * i] = q.x;
-        v[4 * i + 1] = q.y;
-        v[4 * i + 2] = q.z;
-        v[4 * i + 3] = q.w;
-    }
-#pragma unroll
-    for (int k = 0; k < kGLobes; k++) {
-        M.mu[k] = mk(v[3 * k], v[3 * k + 1], v[3 * k + 2]);
-        M.kappa[k] = v[3 * kGLobes + k];
-        M.w[k] = v[4 * kGLobes + k];
+        M.w[k] /= s;
+        M.wn[k] = M.w[k] * vmfNorm(M.kappa[k]);
     }
 }
-
 __device__ __forceinline__ float mixturePdf(const Mixture &M, float3 w) {
     float p = 0.0f;
-    for (int k = 0; k < kGLobes; k++) p += M.w[k] * vmfPdf(w, M.mu[k], M.kappa[k]);
+    for (int k = 0; k < kGLobes; k++) p += M.wn[k] * __expf(M.kappa[k] * (dot(M.mu[k], w) - 1.0f));
     return p;
 }
 // Sampling a vMF lobe with the numerically stable inversion of W. Jakob, "Numerically
@@ -249,6 +226,36 @@ __device__ __forceinline__ bool mlpForwardTile(uint32_t tmem, const uint8_t *wf,
     tc::fenceBeforeSync();
     __syncthreads();
     return true;
+}
+
+// CTA prologue of such a kernel: weights and biases into shared memory, mbarrier, a
+// 64-column TMEM allocation (warp 0); returns the TMEM base
+__device__ __forceinline__ uint32_t tileKernelSetup(uint8_t *sm, const uint8_t *packFwd, const float *biasPad) {
+    const int t = threadIdx.x;
+    for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
+        reinterpret_cast<uint4 *>(sm)[i] = reinterpret_cast<const uint4 *>(packFwd)[i];
+    float *bias = reinterpret_cast<float *>(sm + kTileSmOffBias);
+    for (int i = t; i < kBiasPad; i += kGTile) bias[i] = biasPad[i];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    if (t == 0) tc::mbarInit(bar, 1);
+    if (t < 32) {
+        tc::tmemAlloc(slot, 64);
+        tc::tmemRelinquish();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    return *slot;
+}
+// its epilogue: after a failed (timed-out) wait, a bounded wait for the MMAs still in
+// flight; then the TMEM allocation is released
+__device__ __forceinline__ void tileKernelTeardown(uint8_t *sm, uint32_t tmem, bool ok, uint32_t phase) {
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+    if (!ok) tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmemDealloc(tmem, 64);
 }
 
 // Forward of one tile with the outputs left in registers: thread r receives row r's 40

@@ -26,6 +26,7 @@
 // one any-hit ray instead of a closest-hit ray, and no ray at all when the sampled
 // direction misses the light.
 #include <algorithm>
+#include <utility>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -66,7 +67,16 @@ struct PassArgs {
     const float *biasPad;
     float3 guideLo, guideInvExt;
     float guideAlpha;
-    float *mix;
+    // training-sample collection (guided passes with collect != 0): radiance gathered by
+    // each path, its record count (kRecOpen: the last record waits for the hit of its
+    // continuation ray), the records, and the training ring they end in
+    int collect;
+    float4 *pathL;
+    int *recCount;
+    float4 *recs;
+    float *ring;
+    int ringCapacity;
+    int *ringCtl;
     unsigned long long *stats;
     unsigned long long *visit;   // [0..1] extend nodes / triangles, [2..3] shadow nodes / triangles
     int *err;
@@ -79,6 +89,59 @@ __device__ __forceinline__ int filmIndex(const PassArgs &p, int pix) {
 
 __device__ __forceinline__ void filmAdd(float4 *film, int idx, float3 c) {
     atomicAdd(&film[idx], make_float4(c.x, c.y, c.z, 0.0f));
+}
+
+// ---------------------------------------------------------------- collection
+// A record is made at each guided vertex that continues (the megakernel's training
+// record): 7 float4 at recs[(k * cap + pid) * 7] for record k of path pid:
+//   [0] x0..x3  [1] x4..x7  [2] x8, w  [3] q, f cos  [4] beta, Lafter.x
+//   [5] Lafter.yz, E.xy  [6] E.z
+// x: network inputs, w: sampled direction, q: proposal pdf, beta: throughput after the
+// vertex, Lafter: the path's radiance once the vertex's light samples are resolved, E:
+// direct radiance found along w, times the MIS weight of the guided strategy.  At the
+// end of the pass each record becomes a ring entry with c = lum(f cos (E + (L_end -
+// Lafter) / beta)) / q.
+constexpr int kCollectRecs = 12;   // guided vertices per path (max_depth <= 12)
+constexpr int kRecOpen = 1 << 30;
+
+// radiance gathered by path pid: the film, and the path's own sum when collecting
+template <bool COLLECT>
+__device__ __forceinline__ void gather(const PassArgs &p, int pid, int fi, float3 c) {
+    filmAdd(p.film, fi, c);
+    if (COLLECT) {
+        const float4 L = p.pathL[pid];
+        p.pathL[pid] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+    }
+}
+
+// the continuation ray of path pid's open record met its hit (found) or escaped: fill in
+// Lafter and E (before anything of the new vertex is gathered)
+__device__ __forceinline__ void closeRecord(const PassArgs &p, int pid, bool found, int slot, float t, float3 d) {
+    const int rc = p.recCount[pid];
+    if (!(rc & kRecOpen)) return;
+    const int k = (rc & ~kRecOpen) - 1;
+    float *R = reinterpret_cast<float *>(p.recs + (static_cast<int64_t>(k) * p.cap + pid) * 7);
+    const float4 L = p.pathL[pid];
+    const float q = R[12];
+    float3 E = mk(0, 0, 0);
+    if (!found) {
+        if (p.sv.hasEnv) E = envLe(p.sv.env, d) * powerHeuristic(q, envPdf(p.sv.env, d));
+    } else {
+        const int lightOf = __ldg(&p.sv.slotShade[slot]).y;
+        const float3 n = triNormal(p.sv.tris[slot]);
+        if (lightOf >= 0 && dot(n, -d) > 0.0f) {
+            const LightRecord &Lr = p.sv.lights[lightOf];
+            const float lp = t * t / (dot(n, -d) * Lr.p0.w);
+            E = xyz(Lr.L) * powerHeuristic(q, lp);
+        }
+    }
+    R[19] = L.x;
+    R[20] = L.y;
+    R[21] = L.z;
+    R[22] = E.x;
+    R[23] = E.y;
+    R[24] = E.z;
+    p.recCount[pid] = rc & ~kRecOpen;
 }
 
 // append to a queue with one atomic per warp: returns this lane's slot (or -1)
@@ -106,12 +169,16 @@ __global__ void k_raygen(PassArgs p) {
         p.rayO0[pix] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
         p.rayD0[pix] = make_float4(d.x, d.y, d.z, kInfT);
         p.beta[pix] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        if (p.collect) {
+            p.pathL[pix] = make_float4(0, 0, 0, 0);
+            p.recCount[pix] = 0;
+        }
         atomicAdd(&p.film[fi].w, 1.0f);   // passes of other lanes may add to this pixel concurrently
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) p.counters[0] = p.npix;
 }
 
-template <bool STATS>
+template <bool STATS, bool COLLECT = false>
 __global__ void __launch_bounds__(kTraceBlock, 8) k_extend(PassArgs p, int b) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     uint32_t nodeCount = 0, triCount = 0;
@@ -132,6 +199,7 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_extend(PassArgs p, int b) {
         if (!__any_sync(0xffffffffu, i >= 0)) return;
         int cls = -1;
         if (i >= 0) {
+            if (COLLECT) closeRecord(p, __float_as_int(rO[i].w), L.found, L.hitSlot, L.tmax, L.d);
             if (L.found) {
                 HitRecord h;
                 h.t = L.tmax;
@@ -144,7 +212,7 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_extend(PassArgs p, int b) {
                 // escaped: the environment at the first hit or after a specular bounce
                 const int pid = __float_as_int(rO[i].w);
                 const float4 bt = p.beta[pid];
-                if (b == 0 || bt.w != 0.0f) filmAdd(p.film, filmIndex(p, pid), xyz(bt) * envLe(p.sv.env, L.d));
+                if (b == 0 || bt.w != 0.0f) gather<COLLECT>(p, pid, filmIndex(p, pid), xyz(bt) * envLe(p.sv.env, L.d));
             }
         }
 #pragma unroll
@@ -162,9 +230,30 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_extend(PassArgs p, int b) {
     }
 }
 
-// GUIDED (diffuse class, bounces before the last): the hit samples the learned proposal
-// whose mixture k_guide_infer wrote for its queue entry
-template <int CLS, bool GUIDED = false>
+// append a shaded hit's continuation ray and shadow rays (whole warps call this)
+__device__ __forceinline__ void appendShadeResult(const PassArgs &p, const ShadeResult &R, int pid, int *nextCnt,
+                                                  int *shCnt, float4 *nO, float4 *nD) {
+    const int k = warpAppend(R.cont && !p.direct, nextCnt);
+    if (k >= 0) {
+        nO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pid));
+        nD[k] = R.cD;
+        p.beta[pid] = make_float4(R.beta.x, R.beta.y, R.beta.z, R.spec ? 1.0f : 0.0f);
+    }
+    const int s0 = warpAppend(R.sh0, shCnt);
+    if (s0 >= 0) {
+        p.shO[s0] = R.s0O;
+        p.shD[s0] = R.s0D;
+        p.shL[s0] = R.s0L;
+    }
+    const int s1 = warpAppend(R.sh1, shCnt);
+    if (s1 >= 0) {
+        p.shO[s1] = R.s1O;
+        p.shD[s1] = R.s1D;
+        p.shL[s1] = R.s1L;
+    }
+}
+
+template <int CLS>
 __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
     const int *cnt = p.counters + b * kCountersPerBounce;
     const int n = cnt[1 + CLS];
@@ -188,44 +277,102 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
             pid = __float_as_int(o4.w);
             const float4 bt = p.beta[pid];
             const int fi = filmIndex(p, pid);
-            if (GUIDED) {
-                const HitRecord h = p.hits[i];
-                const int2 sh = __ldg(&p.sv.slotShade[h.prim]);
-                Mixture M;
-                loadMixture(p.mix + static_cast<int64_t>(j) * kMixFloats, M);
-                float3 fc;
-                float pdf;
-                shadeGuidedLambert(p.sv, hitPoint(xyz(o4), xyz(d4), h.t), triNormal(p.sv.tris[h.prim]),
-                                   p.sv.mats[sh.x], sh.y, xyz(d4), xyz(bt), bt.w != 0.0f, b, M, p.guideAlpha, p.seed,
-                                   static_cast<uint32_t>(fi), sample, R, &fc, &pdf);
-            } else {
-                shadeHit(p.sv, p.hits[i], xyz(o4), xyz(d4), xyz(bt), bt.w != 0.0f, b, p.maxDepth, p.seed,
-                         static_cast<uint32_t>(fi), sample, fi, R, p.direct != 0);
+            // shadow rays carry the film pixel, or the path when collecting (k_shadow)
+            shadeHit(p.sv, p.hits[i], xyz(o4), xyz(d4), xyz(bt), bt.w != 0.0f, b, p.maxDepth, p.seed,
+                     static_cast<uint32_t>(fi), sample, p.collect ? pid : fi, R, p.direct != 0);
+            if (!isBlack(R.emit)) {
+                if (p.collect) gather<true>(p, pid, fi, R.emit);
+                else filmAdd(p.film, fi, R.emit);
             }
-            if (!isBlack(R.emit)) filmAdd(p.film, fi, R.emit);
         }
-        const int k = warpAppend(R.cont && !p.direct, nextCnt);
-        if (k >= 0) {
-            nO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pid));
-            nD[k] = R.cD;
-            p.beta[pid] = make_float4(R.beta.x, R.beta.y, R.beta.z, R.spec ? 1.0f : 0.0f);
-        }
-        const int s0 = warpAppend(R.sh0, shCnt);
-        if (s0 >= 0) {
-            p.shO[s0] = R.s0O;
-            p.shD[s0] = R.s0D;
-            p.shL[s0] = R.s0L;
-        }
-        const int s1 = warpAppend(R.sh1, shCnt);
-        if (s1 >= 0) {
-            p.shO[s1] = R.s1O;
-            p.shD[s1] = R.s1D;
-            p.shL[s1] = R.s1L;
-        }
+        appendShadeResult(p, R, pid, nextCnt, shCnt, nO, nD);
     }
 }
 
-template <bool STATS>
+// Diffuse hits of a guided pass, bounces before the last.  Each CTA takes 128-entry
+// tiles of the diffuse queue: every thread forms its entry's network inputs, the tile
+// runs through the four layers on the tensor cores (tcgen05, accumulator in TMEM), and
+// each entry is shaded with its mixture straight from registers (shadeGuidedLambert, the
+// megakernel's shading).  Several CTAs per SM: one's MMA waits overlap another's shading.
+template <bool COLLECT>
+__global__ void __launch_bounds__(kGTile) k_shade_guided(PassArgs p, int b) {
+    const int *cnt = p.counters + b * kCountersPerBounce;
+    const int n = cnt[1 + kMatLambert];
+    if (static_cast<int>(blockIdx.x) * kGTile >= n) return;   // no tile for this CTA
+    extern __shared__ __align__(128) uint8_t sm[];
+    int *nextCnt = p.counters + (b + 1) * kCountersPerBounce;
+    int *shCnt = p.counters + b * kCountersPerBounce + 4;
+    const float4 *rO = (b & 1) ? p.rayO1 : p.rayO0;
+    const float4 *rD = (b & 1) ? p.rayD1 : p.rayD0;
+    float4 *nO = (b & 1) ? p.rayO0 : p.rayO1;
+    float4 *nD = (b & 1) ? p.rayD0 : p.rayD1;
+    const uint32_t sample = static_cast<uint32_t>(p.ctl[0]);
+    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad);
+    const float *bias = reinterpret_cast<const float *>(sm + kTileSmOffBias);
+    uint8_t *xh = sm + kTileSmOffXH;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile * kGTile < n; tile += gridDim.x) {
+        const int j = tile * kGTile + static_cast<int>(threadIdx.x);
+        const bool live = j < n;
+        float4 o4 = make_float4(0, 0, 0, 0), d4 = make_float4(0, 0, 1, 0);
+        HitRecord h;
+        h.t = 0.0f;
+        h.prim = 0;
+        float3 ps = mk(0, 0, 0), nn = mk(0, 0, 1);
+        float xf[16];
+        for (int k = 0; k < 16; k++) xf[k] = 0.0f;
+        if (live) {
+            const int i = p.classQ[kMatLambert * p.cap + j];
+            o4 = rO[i];
+            d4 = rD[i];
+            h = p.hits[i];
+            ps = hitPoint(xyz(o4), xyz(d4), h.t);
+            nn = triNormal(p.sv.tris[h.prim]);
+            guideFeatures(ps, nn, -xyz(d4), p.guideLo, p.guideInvExt, xf);
+        }
+        storeRow8(xh, threadIdx.x, 0, kGK0, xf);
+        storeRow8(xh, threadIdx.x, 8, kGK0, xf + 8);
+        float raw[kGOut];
+        ok = mlpForwardRow(tmem, sm, bias, xh, bar, phase, raw);   // CTA-uniform
+        if (!ok) break;
+        ShadeResult R;
+        R.cont = R.sh0 = R.sh1 = false;
+        int pid = 0;
+        if (live) {
+            pid = __float_as_int(o4.w);
+            const float4 bt = p.beta[pid];
+            const int fi = filmIndex(p, pid);
+            const int2 sh = __ldg(&p.sv.slotShade[h.prim]);
+            Mixture M;
+            mixtureFromRaw(raw, M);
+            float3 fc;
+            float pdf;
+            shadeGuidedLambert(p.sv, ps, nn, p.sv.mats[sh.x], sh.y, xyz(d4), xyz(bt), bt.w != 0.0f, b, M,
+                               p.guideAlpha, p.seed, static_cast<uint32_t>(fi), sample, R, &fc, &pdf);
+            if (!isBlack(R.emit)) gather<COLLECT>(p, pid, fi, R.emit);
+            if (COLLECT) {
+                R.s0O.w = R.s1O.w = __int_as_float(pid);   // k_shadow gathers per path
+                const int nrec = p.recCount[pid];
+                if (R.cont && nrec < kCollectRecs) {
+                    float4 *Q = p.recs + (static_cast<int64_t>(nrec) * p.cap + pid) * 7;
+                    Q[0] = make_float4(xf[0], xf[1], xf[2], xf[3]);
+                    Q[1] = make_float4(xf[4], xf[5], xf[6], xf[7]);
+                    Q[2] = make_float4(xf[8], R.cD.x, R.cD.y, R.cD.z);
+                    Q[3] = make_float4(pdf, fc.x, fc.y, fc.z);
+                    Q[4] = make_float4(R.beta.x, R.beta.y, R.beta.z, 0.0f);
+                    p.recCount[pid] = (nrec + 1) | kRecOpen;
+                }
+            }
+        }
+        appendShadeResult(p, R, pid, nextCnt, shCnt, nO, nD);
+    }
+    tileKernelTeardown(sm, tmem, ok, phase);
+    if (!ok && threadIdx.x == 0) atomicOr(p.err, 2);
+}
+
+template <bool STATS, bool COLLECT = false>
 __global__ void __launch_bounds__(kTraceBlock, 8) k_shadow(PassArgs p, int b) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     int *cnt = p.counters + b * kCountersPerBounce;
@@ -240,7 +387,18 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_shadow(PassArgs p, int b) {
         *t1 = d4.w;
     };
     auto done = [&](int i, const TraceLane &L) {
-        if (i >= 0 && !L.found) filmAdd(p.film, __float_as_int(p.shO[i].w), xyz(p.shL[i]));
+        if (i >= 0 && !L.found) {
+            const int w = __float_as_int(p.shO[i].w);   // film pixel, or the path when collecting
+            const float3 c = xyz(p.shL[i]);
+            if (COLLECT) {
+                filmAdd(p.film, filmIndex(p, w), c);
+                atomicAdd(&p.pathL[w].x, c.x);   // a path's two light samples may finish together
+                atomicAdd(&p.pathL[w].y, c.y);
+                atomicAdd(&p.pathL[w].z, c.z);
+            } else {
+                filmAdd(p.film, w, c);
+            }
+        }
     };
     tracePersistent<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, cnt + 6, stack + threadIdx.x,
                                  kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
@@ -248,6 +406,35 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_shadow(PassArgs p, int b) {
     if (STATS) {
         atomicAdd(&p.visit[2], static_cast<unsigned long long>(nodeCount));
         atomicAdd(&p.visit[3], static_cast<unsigned long long>(triCount));
+    }
+}
+
+// end of a collection pass: every record of every path becomes a training-ring entry
+// (16 floats: x[9], w[3], c, q, 0, 0); records whose c is not a positive finite number
+// are dropped
+__global__ void k_collect(PassArgs p) {
+    for (int pid = blockIdx.x * blockDim.x + threadIdx.x; pid < p.npix; pid += gridDim.x * blockDim.x) {
+        const int nrec = p.recCount[pid] & ~kRecOpen;
+        const float3 Lend = xyz(p.pathL[pid]);
+        for (int k = 0; k < nrec; k++) {
+            const float4 *Q = p.recs + (static_cast<int64_t>(k) * p.cap + pid) * 7;
+            const float4 q3 = Q[3], q4 = Q[4], q5 = Q[5], q6 = Q[6];
+            const float3 beta = mk(q4.x, q4.y, q4.z), Lafter = mk(q4.w, q5.x, q5.y);
+            float3 Li = mk(q5.z, q5.w, q6.x);   // E
+            const float3 rest = Lend - Lafter;
+            Li.x += beta.x > 0.0f ? rest.x / beta.x : 0.0f;
+            Li.y += beta.y > 0.0f ? rest.y / beta.y : 0.0f;
+            Li.z += beta.z > 0.0f ? rest.z / beta.z : 0.0f;
+            const float c = gray(mk(q3.y, q3.z, q3.w) * Li) / q3.x;
+            if (!(c > 0.0f) || !isfinite(c)) continue;
+            const unsigned slot =
+                atomicAdd(reinterpret_cast<unsigned *>(p.ringCtl), 1u) % static_cast<unsigned>(p.ringCapacity);
+            float4 *D = reinterpret_cast<float4 *>(p.ring + 16 * static_cast<int64_t>(slot));
+            D[0] = Q[0];
+            D[1] = Q[1];
+            D[2] = Q[2];
+            D[3] = make_float4(c, q3.x, 0.0f, 0.0f);
+        }
     }
 }
 
@@ -300,7 +487,7 @@ int ensureQueues(RenderQueues &q, int64_t npix, int maxDepth) {
 }
 
 struct Grids {
-    int trace, shade, raygen, infer;
+    int trace, shade, raygen, guided;
 };
 
 Grids passGrids(int device, int64_t npix) {
@@ -313,7 +500,7 @@ Grids passGrids(int device, int64_t npix) {
     g.trace = sms * std::max(occT, 1);
     g.shade = sms * std::max(occS, 1);
     g.raygen = static_cast<int>(std::min<int64_t>((npix + 255) / 256, static_cast<int64_t>(sms) * 8));
-    g.infer = 0;
+    g.guided = 0;
     return g;
 }
 
@@ -339,25 +526,13 @@ void launchPass(const PassArgs &a, const Grids &g, cudaStream_t cs, size_t ctrBy
     done();
     for (int b = 0; b <= a.maxDepth; b++) {
         mark(kExtend);
-        k_extend<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
+        if (a.collect) k_extend<STATS, true><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
+        else k_extend<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
         done();
         mark(kShadeL);
         if (a.packFwd && b < a.maxDepth) {
-            GuideInferArgs ia;
-            ia.count = a.counters + b * kCountersPerBounce + 1 + kMatLambert;
-            ia.queue = a.classQ + kMatLambert * a.cap;
-            ia.rayO = (b & 1) ? a.rayO1 : a.rayO0;
-            ia.rayD = (b & 1) ? a.rayD1 : a.rayD0;
-            ia.hits = a.hits;
-            ia.tris = a.sv.tris;
-            ia.packFwd = a.packFwd;
-            ia.biasPad = a.biasPad;
-            ia.lo = a.guideLo;
-            ia.invExt = a.guideInvExt;
-            ia.mix = a.mix;
-            ia.err = a.err;
-            launchGuideInfer(ia, g.infer, cs);
-            k_shade<kMatLambert, true><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
+            if (a.collect) k_shade_guided<true><<<g.guided, kGTile, kTileSmem, cs>>>(a, b);
+            else k_shade_guided<false><<<g.guided, kGTile, kTileSmem, cs>>>(a, b);
         } else {
             k_shade<kMatLambert><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
         }
@@ -369,9 +544,11 @@ void launchPass(const PassArgs &a, const Grids &g, cudaStream_t cs, size_t ctrBy
         k_shade<kMatDielectric><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
         done();
         mark(kShadow);
-        k_shadow<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
+        if (a.collect) k_shadow<STATS, true><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
+        else k_shadow<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
         done();
     }
+    if (a.collect) k_collect<<<g.raygen, 256, 0, cs>>>(a);
     mark(kFinish);
     k_finish<<<1, 32, 0, cs>>>(a);
     done();
@@ -387,13 +564,16 @@ uint64_t hashBytes(const void *d, size_t n, uint64_t h = 1469598103934665603ull)
 
 void freeRenderQueues(RenderQueues *q) {
     if (q->graph) cudaGraphExecDestroy(q->graph);
+    if (q->graphAlt) cudaGraphExecDestroy(q->graphAlt);
+    cudaFree(q->pathL);
+    cudaFree(q->recCount);
+    cudaFree(q->recs);
     cudaFree(q->pathBeta);
     for (int k = 0; k < 2; k++) {
         cudaFree(q->rayO[k]);
         cudaFree(q->rayD[k]);
     }
     cudaFree(q->hits);
-    cudaFree(q->mix);
     cudaFree(q->classQ);
     cudaFree(q->shO);
     cudaFree(q->shD);
@@ -410,11 +590,6 @@ int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int ma
     const int64_t npix = static_cast<int64_t>(W) * H;
     int rc = ensureQueues(q, npix, maxDepth);
     if (rc) return rc;
-    if (gv && !q.mix && cudaMalloc(&q.mix, sizeof(float) * kMixFloats * q.capacity) != cudaSuccess) {
-        q.mix = nullptr;
-        setError("spgpu_render: device allocation of the guiding mixtures failed");
-        return SPGPU_ENOMEM;
-    }
     PassArgs &a = *out;
     std::memset(&a, 0, sizeof(a));
     a.sv = C.view();
@@ -447,7 +622,25 @@ int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int ma
         a.packFwd = gv->packFwd;
         a.biasPad = gv->biasPad;
         a.guideAlpha = gv->alpha;
-        a.mix = q.mix;
+        if (gv->collect) {
+            if (!q.recs) {
+                cudaMalloc(&q.pathL, sizeof(float4) * q.capacity);
+                cudaMalloc(&q.recCount, sizeof(int) * q.capacity);
+                if (cudaMalloc(&q.recs, sizeof(float4) * 7 * kCollectRecs * q.capacity) != cudaSuccess || !q.pathL ||
+                    !q.recCount) {
+                    cudaGetLastError();
+                    setError("spgpu_guiding_render: device allocation of the collection records failed");
+                    return SPGPU_ENOMEM;
+                }
+            }
+            a.collect = 1;
+            a.pathL = q.pathL;
+            a.recCount = q.recCount;
+            a.recs = q.recs;
+            a.ring = gv->ring;
+            a.ringCapacity = gv->capacity;
+            a.ringCtl = gv->ringCtl;
+        }
         const float3 ext = C.bvh.hi - C.bvh.lo;
         a.guideLo = C.bvh.lo;
         a.guideInvExt = mk(ext.x > 0 ? 1.0f / ext.x : 0.0f, ext.y > 0 ? 1.0f / ext.y : 0.0f,
@@ -465,12 +658,21 @@ int ensurePassGraph(Ctx &C, RenderQueues &q, const PassArgs &a, int W, int H, in
     key[2] = static_cast<uint64_t>(maxDepth) << 32 | seed;
     key[3] = reinterpret_cast<uint64_t>(film);
     if (q.graph && std::memcmp(key, q.graphKey, sizeof(key)) == 0) return 0;
-    if (q.graph) {
-        cudaGraphExecDestroy(q.graph);
-        q.graph = nullptr;
+    if (q.graphAlt && std::memcmp(key, q.graphKeyAlt, sizeof(key)) == 0) {   // swap in the other one
+        std::swap(q.graph, q.graphAlt);
+        std::swap(q.graphKey, q.graphKeyAlt);
+        return 0;
     }
+    // keep the current graph as the alternative, capture a new one
+    if (q.graphAlt) cudaGraphExecDestroy(q.graphAlt);
+    q.graphAlt = q.graph;
+    std::memcpy(q.graphKeyAlt, q.graphKey, sizeof(key));
+    q.graph = nullptr;
     Grids gr = passGrids(C.device, static_cast<int64_t>(W) * H);
-    if (a.packFwd) gr.infer = guideInferGrid(C.device);   // attributes and grid before capture
+    if (a.packFwd)   // attributes and grid before the capture
+        gr.guided = guideTileKernelGrid(a.collect ? reinterpret_cast<const void *>(k_shade_guided<true>)
+                                                  : reinterpret_cast<const void *>(k_shade_guided<false>),
+                                        C.device);
     const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;
     cudaStream_t cs = C.stream;
     cudaGraph_t g = nullptr;

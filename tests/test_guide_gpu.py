@@ -146,6 +146,37 @@ def test_guided_wavefront_matches_guided_megakernel(gpulib):
     np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=2e-3, atol=2e-3)
 
 
+def test_wavefront_collection_matches_megakernel(gpulib):
+    """Training records collected in the wavefront (per-path records closed when their
+    continuation ray finds its hit, turned into ring entries at the end of the pass)
+    are the megakernel's: the same entries, with the same weights c up to the order in
+    which a path's radiance was summed."""
+    import torch
+    sc = _room(30)
+    W, H = 128, 96
+    acc = GpuBVHAccel(sc).construct()
+    p = {"width": W, "height": H, "maxDepth": sc.max_depth}
+    rings = []
+    for flags in (GUIDE_GUIDED | GUIDE_COLLECT, GUIDE_GUIDED | GUIDE_COLLECT | GUIDE_MEGAKERNEL):
+        g = GpuGuide(acc, seed=6)   # the same initial weights
+        f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        g.render(sc.camera, dict(p, sampleCount=16), f, flags, seed=21, sample_offset=0)
+        rings.append(g.ring(1 << 20))
+    a, b = rings
+    assert len(a) > 500, len(a)
+    assert abs(len(a) - len(b)) <= 0.002 * len(b) + 2, (len(a), len(b))
+    ka = {r[:12].tobytes(): r for r in a}
+    kb = {r[:12].tobytes(): r for r in b}
+    common = ka.keys() & kb.keys()
+    assert len(common) >= 0.998 * min(len(ka), len(kb)), (len(common), len(ka), len(kb))
+    ca = np.array([ka[k][12] for k in common])
+    cb = np.array([kb[k][12] for k in common])
+    qa = np.array([ka[k][13] for k in common])
+    qb = np.array([kb[k][13] for k in common])
+    np.testing.assert_array_equal(qa, qb)
+    assert np.mean(np.abs(ca - cb) <= 1e-4 * np.abs(cb) + 1e-12) > 0.999
+
+
 def test_trained_guide_lowers_error_per_sample(gpulib):
     """What the trained network gains over plain BSDF sampling on the indirect-lit room:
     after online training (collection passes + Adam steps on the device), a guided
