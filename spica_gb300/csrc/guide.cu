@@ -131,9 +131,12 @@ struct TrainLayout {
     static constexpr int gb = dy + kGTile * kTrainStride * 4;
     static constexpr int bar = gb + kBiasPad * 4;
     static constexpr int tmem = bar + 8;
-    static constexpr int total = tmem + 8;
+    static constexpr int loadBar = tmem + 8;
+    static constexpr int total = loadBar + 8;
 };
 static_assert(TrainLayout::x % 16 == 0 && TrainLayout::h1 % 16 == 0 && TrainLayout::dyb % 16 == 0, "alignment");
+static_assert(TrainLayout::wb % 16 == 0 && TrainLayout::bias % 16 == 0 && TrainLayout::loadBar % 8 == 0,
+              "bulk-copy destinations 16-byte aligned");
 static_assert(TrainLayout::bar % 8 == 0, "alignment");
 // one training CTA per SM: its 512-column TMEM allocation (all of the SM's tensor
 // memory) then never waits for another CTA's
@@ -219,13 +222,17 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
     const float cSum = wsum[0];
     const float cScale = cSum > 0.0f ? 1.0f / cSum : 0.0f;
     const float cMax = 1000.0f * cSum / static_cast<float>(n);
-    for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
-        reinterpret_cast<uint4 *>(wf)[i] = reinterpret_cast<const uint4 *>(packFwd)[i];
-    for (int i = t; i < kPackBwdBytes / 16; i += kGTile)
-        reinterpret_cast<uint4 *>(wb)[i] = reinterpret_cast<const uint4 *>(packBwd)[i];
-    for (int i = t; i < kBiasPad; i += kGTile) bias[i] = biasPad[i];
+    uint64_t *loadBar = reinterpret_cast<uint64_t *>(sm + TrainLayout::loadBar);
     for (int i = t; i < kBiasPad; i += kGTile) gb[i] = 0.0f;
-    if (t == 0) tc::mbarInit(bar, 1);
+    if (t == 0) {
+        // forward and backward weights and biases: one bulk copy (TMA) each
+        tc::mbarInit(bar, 1);
+        tc::mbarInit(loadBar, 1);
+        tc::mbarExpectTx(loadBar, kPackFwdBytes + kPackBwdBytes + kBiasPad * 4);
+        tc::bulkLoad(wf, packFwd, kPackFwdBytes, loadBar);
+        tc::bulkLoad(wb, packBwd, kPackBwdBytes, loadBar);
+        tc::bulkLoad(bias, biasPad, kBiasPad * 4, loadBar);
+    }
     if (t < 32) {
         tc::tmemAlloc(tmemSlot, kTrainTmemCols);
         tc::tmemRelinquish();
@@ -235,7 +242,7 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
     tc::fenceAfterSync();
     const uint32_t tmem = *tmemSlot;
     uint32_t phase = 0;
-    bool ok = true;
+    bool ok = bulkLoadWait(loadBar);
     float lossSum = 0.0f, wSum = 0.0f;
     bool acc = false;   // weight-gradient accumulators hold this CTA's earlier tiles
     const uint8_t *w2b = wb, *w3b = wb + kW2fBytes, *w4b = wb + 2 * kW2fBytes;
@@ -302,7 +309,9 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
         acc = true;
     }
     if (!ok) {
-        // a wait gave up: wait (bounded) for the MMAs still in flight before freeing TMEM
+        // a wait gave up: wait (bounded) for the copies and MMAs still in flight before
+        // freeing TMEM
+        tc::mbarWait(loadBar, 0, kMmaWaitTries);
         tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);
         tc::fenceBeforeSync();
         __syncthreads();

@@ -51,11 +51,19 @@ constexpr uint32_t kMmaWaitTries = 1u << 22;
 
 // shared memory of a kernel that evaluates the network for its 128-thread CTA, one tile
 // at a time: packed forward weights | biases (padded to 1 KB) | input/hidden tile (bf16
-// [128][64]) | mbarrier, TMEM slot
+// [128][64]) | MMA mbarrier, TMEM slot, load mbarrier
 constexpr int kTileSmOffBias = kPackFwdBytes;
 constexpr int kTileSmOffXH = kTileSmOffBias + 1024;
 constexpr int kTileSmOffBar = kTileSmOffXH + kGTile * kGHid * 2;
-constexpr int kTileSmem = kTileSmOffBar + 16;
+constexpr int kTileSmem = kTileSmOffBar + 24;
+static_assert(kBiasPad * 4 % 16 == 0 && kPackFwdBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+
+// Bounded wait of all threads for a bulk load announced on *bar (phase 0); false if it
+// did not complete within kMmaWaitTries polls (CTA-wide result)
+__device__ __forceinline__ bool bulkLoadWait(uint64_t *bar) {
+    const bool ok = tc::mbarWait(bar, 0, kMmaWaitTries);
+    return __syncthreads_and(ok) != 0;
+}
 
 // ---------------------------------------------------------------- vMF mixture
 struct Mixture {
@@ -228,17 +236,22 @@ __device__ __forceinline__ bool mlpForwardTile(uint32_t tmem, const uint8_t *wf,
     return true;
 }
 
-// CTA prologue of such a kernel: weights and biases into shared memory, mbarrier, a
-// 64-column TMEM allocation (warp 0); returns the TMEM base
-__device__ __forceinline__ uint32_t tileKernelSetup(uint8_t *sm, const uint8_t *packFwd, const float *biasPad) {
+// CTA prologue of such a kernel: weights and biases into shared memory by one bulk
+// copy each (TMA), the MMA mbarrier, a 64-column TMEM allocation (warp 0); returns the
+// TMEM base, and in *ok whether the copies arrived
+__device__ __forceinline__ uint32_t tileKernelSetup(uint8_t *sm, const uint8_t *packFwd, const float *biasPad,
+                                                    bool *ok) {
     const int t = threadIdx.x;
-    for (int i = t; i < kPackFwdBytes / 16; i += kGTile)
-        reinterpret_cast<uint4 *>(sm)[i] = reinterpret_cast<const uint4 *>(packFwd)[i];
-    float *bias = reinterpret_cast<float *>(sm + kTileSmOffBias);
-    for (int i = t; i < kBiasPad; i += kGTile) bias[i] = biasPad[i];
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
     uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
-    if (t == 0) tc::mbarInit(bar, 1);
+    uint64_t *loadBar = bar + 2;
+    if (t == 0) {
+        tc::mbarInit(bar, 1);
+        tc::mbarInit(loadBar, 1);
+        tc::mbarExpectTx(loadBar, kPackFwdBytes + kBiasPad * 4);
+        tc::bulkLoad(sm, packFwd, kPackFwdBytes, loadBar);
+        tc::bulkLoad(sm + kTileSmOffBias, biasPad, kBiasPad * 4, loadBar);
+    }
     if (t < 32) {
         tc::tmemAlloc(slot, 64);
         tc::tmemRelinquish();
@@ -246,13 +259,17 @@ __device__ __forceinline__ uint32_t tileKernelSetup(uint8_t *sm, const uint8_t *
     tc::fenceBeforeSync();
     __syncthreads();
     tc::fenceAfterSync();
+    *ok = bulkLoadWait(loadBar);
     return *slot;
 }
-// its epilogue: after a failed (timed-out) wait, a bounded wait for the MMAs still in
-// flight; then the TMEM allocation is released
+// its epilogue: after a failed (timed-out) wait, bounded waits for the copies and MMAs
+// still in flight; then the TMEM allocation is released
 __device__ __forceinline__ void tileKernelTeardown(uint8_t *sm, uint32_t tmem, bool ok, uint32_t phase) {
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
-    if (!ok) tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);
+    if (!ok) {
+        tc::mbarWait(bar + 2, 0, kMmaWaitTries);
+        tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);
+    }
     tc::fenceBeforeSync();
     __syncthreads();
     if (threadIdx.x < 32) tc::tmemDealloc(tmem, 64);

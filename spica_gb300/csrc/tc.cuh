@@ -59,6 +59,22 @@ __device__ __forceinline__ bool mbarWait(uint64_t *bar, uint32_t phase, uint32_t
     return false;
 }
 
+// ---------------------------------------------------------------- bulk copies (TMA)
+// One thread: announce `bytes` of transfer on *bar (its arrival for this phase) ...
+__device__ __forceinline__ void mbarExpectTx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes)
+                 : "memory");
+}
+// ... and copy global -> shared with the tensor memory accelerator; the bytes complete
+// on *bar.  dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulkLoad(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smemAddr(dst)),
+        "l"(src), "r"(bytes), "r"(smemAddr(bar))
+        : "memory");
+}
+
 // ---------------------------------------------------------------- TMEM
 // Executed by one full warp.  The allocated column base is written to *dst (shared).
 __device__ __forceinline__ void tmemAlloc(uint32_t *dst, uint32_t ncols) {

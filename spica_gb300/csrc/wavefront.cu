@@ -307,13 +307,13 @@ __global__ void __launch_bounds__(kGTile) k_shade_guided(PassArgs p, int b) {
     float4 *nO = (b & 1) ? p.rayO0 : p.rayO1;
     float4 *nD = (b & 1) ? p.rayD0 : p.rayD1;
     const uint32_t sample = static_cast<uint32_t>(p.ctl[0]);
-    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad);
+    bool ok = true;
+    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad, &ok);
     const float *bias = reinterpret_cast<const float *>(sm + kTileSmOffBias);
     uint8_t *xh = sm + kTileSmOffXH;
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
     uint32_t phase = 0;
-    bool ok = true;
-    for (int tile = blockIdx.x; tile * kGTile < n; tile += gridDim.x) {
+    for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
         const int j = tile * kGTile + static_cast<int>(threadIdx.x);
         const bool live = j < n;
         float4 o4 = make_float4(0, 0, 0, 0), d4 = make_float4(0, 0, 1, 0);

@@ -74,6 +74,7 @@ def render_equal_time(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, b
     p = {"width": W, "height": H, "maxDepth": scene.max_depth}
     film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
     spent, spp, trained, offset, losses, kept = 0.0, 0, 0, 0, [], 0
+    collect_ms = train_ms = render_ms = 0.0
     if guided:
         scratch = torch.zeros_like(film)
         t_train = train_fraction * budget_ms
@@ -86,14 +87,19 @@ def render_equal_time(torch, accel: GpuBVHAccel, guide: GpuGuide, scene, W, H, b
             t0 = time.perf_counter()
             losses.append(guide.train(train_steps))
             torch.cuda.synchronize()
-            spent += st.ms + 1e3 * (time.perf_counter() - t0)
+            dt = 1e3 * (time.perf_counter() - t0)
+            spent += st.ms + dt
+            collect_ms += st.ms
+            train_ms += dt
             trained += train_steps
     flags = GUIDE_GUIDED if guided else 0
     while spent < budget_ms:
         st = guide.render(scene.camera, dict(p, sampleCount=chunk_spp), film, flags, seed=seed, sample_offset=spp)
         spent += st.ms
+        render_ms += st.ms
         spp += chunk_spp
     torch.cuda.synchronize()
     return _mean(film), {"ms": spent, "render_spp": spp, "adam_steps": trained, "training_spp": offset,
-                         "kept_training_spp": kept,
+                         "kept_training_spp": kept, "collect_ms": collect_ms, "train_ms": train_ms,
+                         "render_ms": render_ms,
                          "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None}
