@@ -319,11 +319,15 @@ def batch_bench(torch, GpuBatch, scenes, reps=3, count=64, autotune=True):
             "prepare_s": prep_s}
 
 
-def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=1024, ref_spp=4096):
-    """Learned guiding on the indirect-lit room: relMSE against a plain reference at
-    equal device time (the time of budget_spp plain samples per pixel), the guided run
-    training online for the first 25% of it (its collection passes' samples kept in the
-    image); plus the per-sample gain of the same two images."""
+def guiding_bench(torch, GpuBVHAccel, scenes, W=1280, H=720, budget_spp=1024, ref_spp=4096):
+    """Learned guiding on the indirect-lit room (1280 x 720, max depth 12): relMSE at equal
+    device time (the time of budget_spp plain wavefront samples per pixel) against the
+    plain wavefront path tracer, the guided run training online for the first 25% of it
+    (collection passes of 2 spp, each followed by 128 Adam steps; their samples kept in
+    the image).  relMSE is taken against a ref_spp plain reference with the reference's
+    own noise subtracted (its per-pixel variance from 16 independent chunks), which
+    estimates the error against the converged image, as a far longer reference would.
+    Also the per-sample gain of the same two images."""
     from spica_gb300 import guiding
     from spica_gb300.gpu import GpuGuide
     sc = scenes.guiding_room(width=W, height=H)
@@ -337,7 +341,7 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=1024, ref
     budget = ms8 / 8 * budget_spp
     plain, pi = guiding.render_equal_time(torch, acc, g, sc, W, H, budget, guided=False, seed=11)
     gg = GpuGuide(acc, seed=2)
-    img, gi = guiding.render_equal_time(torch, acc, gg, sc, W, H, budget, guided=True, seed=11, train_steps=32,
+    img, gi = guiding.render_equal_time(torch, acc, gg, sc, W, H, budget, guided=True, seed=11, train_steps=128,
                                         keep_training_samples=1.0)
     raw_p, raw_g = guiding.relmse(plain, ref), guiding.relmse(img, ref)
     e_p, e_g = raw_p - noise, raw_g - noise   # against the converged image
@@ -363,7 +367,32 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=640, H=360, budget_spp=1024, ref
             "plain_spp": pi["render_spp"], "guided_spp": gi["render_spp"] + gi["kept_training_spp"],
             "adam_steps": gi["adam_steps"],
             "training_spp": gi["training_spp"], "train_fraction": 0.25,
-            "plain_ms_per_spp": ms8 / 8, "training_roofline": train_roof}
+            "plain_ms_per_spp": ms8 / 8,
+            "guided_ms_per_spp": gi["render_ms"] / max(gi["render_spp"], 1),
+            "collect_ms_per_spp": gi["collect_ms"] / max(gi["training_spp"], 1),
+            "train_ms_per_step": gi["train_ms"] / max(gi["adam_steps"], 1),
+            "training_roofline": train_roof}
+
+
+def guided_passes(torch, GpuBVHAccel, scenes, W=640, H=360):
+    """Profiling case for the guided wavefront: brief online training, then one plain and
+    one guided 8-spp render of the guiding room inside the NVTX range 'profiled'."""
+    from spica_gb300.gpu import GUIDE_COLLECT, GUIDE_GUIDED, GpuGuide
+    sc = scenes.guiding_room(width=W, height=H)
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=2)
+    p = {"width": W, "height": H, "maxDepth": sc.max_depth}
+    f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    for k in range(8):
+        g.render(sc.camera, dict(p, sampleCount=2), f, GUIDE_GUIDED | GUIDE_COLLECT, seed=1, sample_offset=2 * k)
+        g.train(32)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("profiled")
+    sp = g.render(sc.camera, dict(p, sampleCount=8), f, 0, seed=2)
+    sg = g.render(sc.camera, dict(p, sampleCount=8), f, GUIDE_GUIDED, seed=2)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    return {"width": W, "height": H, "spp": 8, "plain_ms": sp.ms, "guided_ms": sg.ms}
 
 
 def main():
@@ -385,6 +414,10 @@ def main():
                          "shape (profiling cases)")
     ap.add_argument("--guiding-only", action="store_true",
                     help="only the learned-guiding comparison, on a small case (320x180, profiling)")
+    ap.add_argument("--guided-passes", action="store_true",
+                    help="profiling case: the guiding room at 640x360, 8 collection passes of 2 spp with 32 Adam "
+                         "steps each, then one plain and one guided render of 8 spp inside the NVTX range "
+                         "'profiled'")
     ap.add_argument("--micro-only", type=int, default=0, metavar="RAYS",
                     help="only the intersection microbench, on RAYS rays (profiling cases)")
     args = ap.parse_args()
@@ -410,6 +443,9 @@ def main():
     if args.guiding_only:
         print(json.dumps({"guiding": guiding_bench(torch, GpuBVHAccel, scenes, W=320, H=180, budget_spp=64,
                                                    ref_spp=512)}), flush=True)
+        return 0
+    if args.guided_passes:
+        print(json.dumps({"guided_passes": guided_passes(torch, GpuBVHAccel, scenes)}), flush=True)
         return 0
     scene = scenes.mid_scale(width=args.width, height=args.height)
     W, H, md = scene.width, scene.height, scene.max_depth
