@@ -287,6 +287,36 @@ int spgpu_film_resolve(spgpu_ctx *ctx, const float *film, int32_t width, int32_t
 int spgpu_write_hdr(const char *path, const uint8_t *rgbe, int32_t width, int32_t height);
 int spgpu_write_png(const char *path, const uint8_t *rgb, int32_t width, int32_t height);
 
+/* ---- scene files ---------------------------------------------------------------
+ * replaces: SceneParser (spica/sceneparser.cc:72-335) with meshio::loadPLY / loadOBJ
+ * (core/meshio.cc:76-250), up to the point where it hands the camera, primitives and
+ * lights to Integrator::render.  spgpu_scene_load reads a scene file of the reference's
+ * XML format into the arrays spgpu_upload_scene takes and the request spgpu_render
+ * takes (camera, film size, sampleCount, maxDepth, integrator; seed and sample_offset
+ * 0).  Accepted: perspective sensors, hdr / ldr films, the independent sampler, the
+ * path and direct-lighting integrators (or the gpupath / gpudirect drop-ins), BSDFs
+ * diffuse, roughconductor (ggx), dielectric, roughdielectric and plastic with constant
+ * parameters, PLY (binary little endian) and OBJ meshes, area emitters and one
+ * untransformed .hdr environment map; anything else is SPGPU_EINVAL with the element
+ * and the reason in spgpu_last_error().  Free the result with spgpu_scene_free. */
+typedef struct {
+    int32_t ntri;
+    const float *verts;        /* ntri*9 */
+    const int32_t *tri_mat;    /* ntri */
+    int32_t nmat;
+    const float *materials;    /* nmat*8 */
+    const float *tri_emit;     /* ntri*3 */
+    int32_t env_width, env_height;
+    const float *env;          /* env_width*env_height*3, or NULL */
+    spgpu_render_desc desc;
+    void *internal;            /* owned by the library */
+} spgpu_scene_file;
+int spgpu_scene_load(const char *path, spgpu_scene_file **out);
+void spgpu_scene_free(spgpu_scene_file *scene);
+/* Image::loadHdr (core/image.cc:252-385): a Radiance .hdr file (run-length-encoded
+ * scanlines) as RGB floats; with rgb NULL only the size is returned */
+int spgpu_load_hdr(const char *path, float *rgb, int32_t max_pixels, int32_t *width, int32_t *height);
+
 /* Profiling (no counterpart in the reference, which has only a progress printf,
  * core/integrator.cc:92-96): the same samples as spgpu_render, launched kernel by
  * kernel without the graph and timed with CUDA events on `stream`, then repeated

@@ -65,6 +65,7 @@
 #include <thread>
 #include <vector>
 
+#include "core/meshio.h"
 #include "material_probe.h"   // the drop-in plugin's material translation, under test
 #include "spo_api.h"
 
@@ -326,6 +327,71 @@ int spo_bsdf_eval(const double *mat, int64_t n, const double *wo, const double *
         f[3 * i + 2] = v.blue();
         pdf[i] = b.isect.bsdf()->pdf(o, d);
     }
+    return 0;
+}
+
+int spo_load_ply(const char *path, const double *m16, int64_t max_tris, double *verts, int64_t *ntri) {
+    double m[4][4];
+    for (int i = 0; i < 16; i++) m[i / 4][i % 4] = m16[i];
+    const std::vector<ShapeGroup> groups = meshio::loadPLY(path, Transform(m));
+    int64_t n = 0;
+    for (const auto &g : groups) {
+        for (const auto &s : g.shapes()) {
+            for (const Triangle &t : s->triangulate()) {
+                if (n < max_tris) {
+                    for (int k = 0; k < 3; k++) {
+                        verts[9 * n + 3 * k] = t[k].x();
+                        verts[9 * n + 3 * k + 1] = t[k].y();
+                        verts[9 * n + 3 * k + 2] = t[k].z();
+                    }
+                }
+                n++;
+            }
+        }
+    }
+    *ntri = n;
+    return 0;
+}
+
+int spo_load_hdr(const char *path, int64_t max_pixels, double *rgb, int *width, int *height) {
+    Image img;
+    img.load(path);
+    *width = img.width();
+    *height = img.height();
+    if (static_cast<int64_t>(img.width()) * img.height() > max_pixels) return 1;
+    for (int y = 0; y < img.height(); y++) {
+        for (int x = 0; x < img.width(); x++) {
+            const RGBSpectrum &p = img(x, y);
+            double *o = rgb + 3 * (static_cast<int64_t>(y) * img.width() + x);
+            o[0] = p.red();
+            o[1] = p.green();
+            o[2] = p.blue();
+        }
+    }
+    return 0;
+}
+
+int spo_transform_chain(int n, const int *kinds, const double *params, double *out16) {
+    Transform trans;
+    for (int i = 0; i < n; i++) {
+        const double *q = params + 16 * i;
+        Transform sub;
+        if (kinds[i] == 0) {
+            sub = Transform::translate(Vector3d(q[0], q[1], q[2]));
+        } else if (kinds[i] == 1) {
+            sub = Transform::scale(q[0], q[1], q[2]);
+        } else if (kinds[i] == 2) {
+            sub = Transform::rotate(q[0], Vector3d(q[1], q[2], q[3]));
+        } else if (kinds[i] == 3) {
+            sub = Transform::lookAt(Point3d(q[0], q[1], q[2]), Point3d(q[3], q[4], q[5]), Vector3d(q[6], q[7], q[8]));
+        } else {
+            double m[4][4];
+            for (int k = 0; k < 16; k++) m[k / 4][k % 4] = q[k];
+            sub = Transform(m);
+        }
+        trans = sub * trans;   // spica/sceneparser.cc:168
+    }
+    for (int k = 0; k < 16; k++) out16[k] = trans.getMat()(k / 4, k % 4);
     return 0;
 }
 

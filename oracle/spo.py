@@ -115,6 +115,34 @@ class Oracle:
         rc = self.lib.spo_probe_material(mat, rec.ctypes.data, why, 256)
         return (rec, None) if rc == 0 else (None, why.value.decode())
 
+    # ---------------------------------------------------------------- scene files
+    def load_ply(self, path, m16, max_tris=1 << 20):
+        """meshio::loadPLY with objectToWorld m16 (row-major 4x4): (n, 9) float64."""
+        m = np.ascontiguousarray(m16, np.float64).reshape(16)
+        out = np.zeros((max_tris, 9), np.float64)
+        n = C.c_int64(0)
+        self.lib.spo_load_ply.argtypes = [C.c_char_p, _dp, C.c_int64, C.c_void_p, C.POINTER(C.c_int64)]
+        self.lib.spo_load_ply(str(path).encode(), m, max_tris, out.ctypes.data, C.byref(n))
+        return out[:min(n.value, max_tris)]
+
+    def transform_chain(self, kinds, params):
+        """The scene parser's composition of transform elements (kinds 0 translate,
+        1 scale, 2 rotate, 3 lookAt, 4 matrix; 16 parameters each): row-major 4x4."""
+        k = np.ascontiguousarray(kinds, np.int32)
+        q = np.ascontiguousarray(params, np.float64).reshape(-1)
+        out = np.zeros(16, np.float64)
+        self.lib.spo_transform_chain.argtypes = [C.c_int, C.c_void_p, _dp, C.c_void_p]
+        self.lib.spo_transform_chain(len(k), k.ctypes.data, q, out.ctypes.data)
+        return out.reshape(4, 4)
+
+    def load_hdr(self, path, max_pixels=1 << 22):
+        """Image::load of a .hdr file: (H, W, 3) float64."""
+        out = np.zeros(max_pixels * 3, np.float64)
+        w, h = C.c_int(0), C.c_int(0)
+        self.lib.spo_load_hdr.argtypes = [C.c_char_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        self.lib.spo_load_hdr(str(path).encode(), max_pixels, out.ctypes.data, C.byref(w), C.byref(h))
+        return out[:w.value * h.value * 3].reshape(h.value, w.value, 3)
+
     # ---------------------------------------------------------------- film output
     # (compiled reference only: the restatement does not carry the image code)
     def _film(self, film):

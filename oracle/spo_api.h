@@ -88,6 +88,20 @@ int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out
  * reference only): 0 and the spgpu record in rec[0..7], or -1 and the refusal in why. */
 int spo_probe_material(const double *mat, float *rec, char *why, int why_len);
 
+/* Scene front-end pieces of the reference (compiled reference only):
+ *   spo_load_ply         meshio::loadPLY (core/meshio.cc:76) with the row-major 4x4
+ *                        objectToWorld m16: world-space triangles (9 doubles each) of up
+ *                        to max_tris into verts, the count into *ntri
+ *   spo_transform_chain  the scene parser's composition of <transform> children
+ *                        (spica/sceneparser.cc:128-171): for each element, kind 0
+ *                        translate(x,y,z), 1 scale(x,y,z), 2 rotate(angle, axis x,y,z),
+ *                        3 lookAt(origin, target, up), 4 matrix (16 values), parameters
+ *                        16 doubles per element; trans = sub * trans; row-major result */
+int spo_load_ply(const char *path, const double *m16, int64_t max_tris, double *verts, int64_t *ntri);
+/* Image::load of a .hdr file (core/image.cc:252): RGB doubles, row-major */
+int spo_load_hdr(const char *path, int64_t max_pixels, double *rgb, int *width, int *height);
+int spo_transform_chain(int n, const int *kinds, const double *params, double *out16);
+
 /* per-pixel sampler seed: splitmix-style mix of (seed, pixel) folded to 32 bits */
 static inline uint32_t spo_pixel_seed(uint32_t seed, uint32_t pixel) {
     uint64_t z = ((uint64_t)seed << 32) ^ (uint64_t)pixel;

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libspica_gpu.so")
-SOURCES = ["api.cu", "bvh.cu", "wavefront.cu", "batch.cu", "guide.cu", "film.cu"]
+SOURCES = ["api.cu", "bvh.cu", "wavefront.cu", "batch.cu", "guide.cu", "film.cu", "sceneio.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
@@ -55,7 +55,7 @@ def build(verbose: bool = False, extra_flags=None) -> str:
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT, src.replace(".cu", ".o"))
+        o = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         if _stale(o, [s] + headers + [__file__]):
             jobs.append([nv, *ARCH, *flags, "-c", s, "-o", o])
     if jobs:
@@ -63,7 +63,7 @@ def build(verbose: bool = False, extra_flags=None) -> str:
             for out in ex.map(_run, jobs):
                 if verbose and out.strip():
                     print(out)
-    objs = [os.path.join(OUT, s.replace(".cu", ".o")) for s in SOURCES]
+    objs = [os.path.join(OUT, os.path.splitext(s)[0] + ".o") for s in SOURCES]
     if _stale(LIB, objs):
         _run([nv, *ARCH, "-shared", "-o", LIB, *objs])
     return LIB

@@ -105,6 +105,57 @@ def write_hdr(path: str, rgbe) -> None:
            "spgpu_write_hdr")
 
 
+class SceneFile(C.Structure):
+    _fields_ = [("ntri", C.c_int32), ("verts", C.c_void_p), ("tri_mat", C.c_void_p), ("nmat", C.c_int32),
+                ("materials", C.c_void_p), ("tri_emit", C.c_void_p), ("env_width", C.c_int32),
+                ("env_height", C.c_int32), ("env", C.c_void_p), ("desc", RenderDesc), ("internal", C.c_void_p)]
+
+
+def load_scene(path: str):
+    """spgpu_scene_load: a scene file of the reference's XML format (SceneParser,
+    spica/sceneparser.cc) as a scenes.Scene (arrays copied out) plus the integrator
+    ("path" or "direct")."""
+    from .scenes import Scene
+    lib = load_library()
+    out = C.POINTER(SceneFile)()
+    _check(lib.spgpu_scene_load(str(path).encode(), C.byref(out)), "spgpu_scene_load")
+    try:
+        f = out.contents
+        n, m = f.ntri, f.nmat
+
+        def arr(ptr, count, dtype):
+            if count == 0:
+                return np.zeros((0,), dtype)
+            ct = {np.float32: C.c_float, np.int32: C.c_int32}[dtype]
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), shape=(count,)).copy()
+
+        env = None
+        if f.env:
+            env = arr(f.env, f.env_width * f.env_height * 3, np.float32).reshape(f.env_height, f.env_width, 3)
+        d = f.desc
+        sc = Scene(verts=arr(f.verts, 9 * n, np.float32).reshape(n, 9), tri_mat=arr(f.tri_mat, n, np.int32),
+                   materials=arr(f.materials, 8 * m, np.float32).reshape(m, 8).astype(np.float64),
+                   tri_emit=arr(f.tri_emit, 3 * n, np.float32).reshape(n, 3), env=env,
+                   camera=np.array(list(d.camera), np.float32), width=d.width, height=d.height, spp=d.spp,
+                   max_depth=d.max_depth, name=os.path.basename(str(path)))
+        integrator = "direct" if d.integrator == 1 else "path"
+    finally:
+        lib.spgpu_scene_free(out)
+    return sc, integrator
+
+
+def load_hdr(path: str) -> np.ndarray:
+    """spgpu_load_hdr: a Radiance .hdr file as (H, W, 3) float32, as the reference's
+    Image::loadHdr reads it."""
+    lib = load_library()
+    w, h = C.c_int32(0), C.c_int32(0)
+    _check(lib.spgpu_load_hdr(str(path).encode(), None, 0, C.byref(w), C.byref(h)), "spgpu_load_hdr")
+    out = np.zeros((h.value, w.value, 3), np.float32)
+    _check(lib.spgpu_load_hdr(str(path).encode(), out.ctypes.data, w.value * h.value, C.byref(w), C.byref(h)),
+           "spgpu_load_hdr")
+    return out
+
+
 def write_png(path: str, rgb) -> None:
     """spgpu_write_png: (H, W, 3) uint8 pixels to an 8-bit RGB PNG."""
     a = np.ascontiguousarray(rgb, np.uint8)
@@ -124,7 +175,7 @@ EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version",
            "spgpu_render", "spgpu_render_host", "spgpu_render_profile", "spgpu_batch_prepare",
            "spgpu_batch_film_pixels", "spgpu_batch_run", "spgpu_guiding_init", "spgpu_guiding_render",
            "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_ring", "spgpu_guiding_params", "spgpu_guiding_mlp",
-           "spgpu_guiding_grad"]
+           "spgpu_guiding_grad", "spgpu_scene_load", "spgpu_scene_free", "spgpu_load_hdr"]
 
 _lib = None
 
@@ -153,6 +204,10 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_film_resolve.argtypes = [vp, vp, i32, i32, i32, C.c_double, vp, vp]
     lib.spgpu_write_hdr.argtypes = [C.c_char_p, vp, i32, i32]
     lib.spgpu_write_png.argtypes = [C.c_char_p, vp, i32, i32]
+    lib.spgpu_scene_load.argtypes = [C.c_char_p, C.POINTER(C.POINTER(SceneFile))]
+    lib.spgpu_scene_free.argtypes = [C.POINTER(SceneFile)]
+    lib.spgpu_scene_free.restype = None
+    lib.spgpu_load_hdr.argtypes = [C.c_char_p, vp, i32, C.POINTER(i32), C.POINTER(i32)]
     lib.spgpu_trace_stats.argtypes = [vp, C.c_int, vp, vp, i64, vp, C.POINTER(TraceCounters)]
     lib.spgpu_render.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats), vp]
     lib.spgpu_render_host.argtypes = [vp, C.POINTER(RenderDesc), vp, C.POINTER(RenderStats)]
