@@ -1,6 +1,7 @@
 """A scene file rendered on the GPU: the box room written in the reference's XML format
 (PLY meshes, diffuse BSDFs, an area emitter) and loaded by spgpu_scene_load renders
-exactly the film of the procedurally built box room with the same camera."""
+the film of the procedurally built box room with the same camera: the same samples,
+equal up to the order in which concurrent pass lanes add into the film (last bits)."""
 import numpy as np
 import pytest
 
@@ -19,4 +20,5 @@ def test_scene_file_renders_like_the_procedural_scene(gpulib, tmp_path):
     f_file = GpuPathIntegrator(seed=3).render(got.camera, GpuBVHAccel(got).construct(), p)
     f_proc = GpuPathIntegrator(seed=3).render(got.camera, GpuBVHAccel(sc).construct(), p)
     assert np.all(f_file[..., 3] == got.spp) and f_file[..., :3].sum() > 0
-    np.testing.assert_array_equal(f_file, f_proc)
+    np.testing.assert_array_equal(f_file[..., 3], f_proc[..., 3])
+    np.testing.assert_allclose(f_file[..., :3], f_proc[..., :3], rtol=1e-5, atol=1e-6)
