@@ -3,7 +3,8 @@
 // Replaces the reference's serial binary SAH build (accelerators/bvh.cc:150-237,
 // BVHAccel::constructRec) with a data-parallel one on the GPU:
 //   1. per-triangle bounds and centroid bounds              (k_prim_bounds)
-//   2. 63-bit Morton codes of the centroids, radix sort     (k_morton + cub)
+//   2. 63-bit Morton codes of the centroids under a large-triangle bit, radix sort
+//                                                            (k_morton + cub)
 //   3. binary radix tree over the sorted codes              (k_karras)
 //      -- Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees,
 //         and k-d Trees" (HPG 2012)
@@ -86,19 +87,33 @@ __device__ __forceinline__ uint64_t spread21(uint32_t x) {
     return v;
 }
 
+// Sort key: bit 63 marks a large triangle (box diagonal above 1/8 of the scene's), bits
+// 0-62 are the 63-bit Morton code of its box centre.  The size bit is the extended
+// Morton code idea of Vinkler, Bittner and Havran ("Extended Morton codes for high
+// performance bounding volume hierarchy construction", HPG 2017) reduced to one class:
+// the radix tree's root splits the large triangles (a floor quad, room walls) into a
+// subtree of their own, instead of leaving them deep among small ones where every
+// ancestor's box would span them.
+constexpr float kLargeTriangle = 1.0f / 8.0f;
+
 __global__ void k_morton(const float *__restrict__ verts, int n, const float *__restrict__ bounds,
                          uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float *v = verts + 9 * static_cast<int64_t>(i);
     uint32_t q[3];
+    float d2 = 0.0f, s2 = 0.0f;
     for (int a = 0; a < 3; a++) {
-        const float c = 0.5f * (fminf(v[a], fminf(v[3 + a], v[6 + a])) + fmaxf(v[a], fmaxf(v[3 + a], v[6 + a])));
+        const float mn = fminf(v[a], fminf(v[3 + a], v[6 + a])), mx = fmaxf(v[a], fmaxf(v[3 + a], v[6 + a]));
+        const float c = 0.5f * (mn + mx);
         const float lo = bounds[6 + a], ext = bounds[9 + a] - bounds[6 + a];
         const float u = ext > 0.0f ? (c - lo) / ext : 0.5f;
         q[a] = static_cast<uint32_t>(fminf(fmaxf(u * 2097152.0f, 0.0f), 2097151.0f));
+        d2 += (mx - mn) * (mx - mn);
+        s2 += (bounds[3 + a] - bounds[a]) * (bounds[3 + a] - bounds[a]);
     }
-    keys[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    const uint64_t large = d2 > kLargeTriangle * kLargeTriangle * s2 ? 1ull << 63 : 0ull;
+    keys[i] = large | (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
     vals[i] = static_cast<uint32_t>(i);
 }
 
@@ -426,12 +441,12 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
         k_morton<<<(n + T - 1) / T, T, 0, stream>>>(d_verts, n, d_bounds, keys[0], vals[0]);
         cub::DoubleBuffer<uint64_t> kb(keys[0], keys[1]);
         cub::DoubleBuffer<uint32_t> vb(vals[0], vals[1]);
-        cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, kb, vb, n, 0, 63, stream);
+        cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, kb, vb, n, 0, 64, stream);
         if (cudaMalloc(&tmp, tmpBytes) != cudaSuccess) {
             snprintf(err, errlen, "buildWideBVH: sort scratch allocation failed");
             rc = -4;
         } else {
-            cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, kb, vb, n, 0, 63, stream);
+            cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, kb, vb, n, 0, 64, stream);
             const uint64_t *sk = kb.Current();
             const uint32_t *order = vb.Current();
             if (n > 1) k_karras<<<(n - 1 + T - 1) / T, T, 0, stream>>>(sk, n, child, parent, range);
