@@ -5,11 +5,14 @@
 //   1. per-triangle bounds and centroid bounds              (k_prim_bounds)
 //   2. 63-bit Morton codes of the centroids under a large-triangle bit, radix sort
 //                                                            (k_morton + cub)
-//   3. binary radix tree over the sorted codes              (k_karras)
-//      -- Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees,
-//         and k-d Trees" (HPG 2012)
-//   4. bottom-up bounds refit with arrival counters         (k_refit)
-//   5. top-down collapse into 8-wide nodes, level by level  (k_collapse)
+//   3. binary tree by parallel locally-ordered clustering   (k_leaf_bounds, k_ploc_*)
+//      -- Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding
+//         Volume Hierarchy Construction" (IEEE TVCG 2018): clusters start as the
+//         triangles in code order; each round every cluster finds the neighbour
+//         within kPlocRadius positions whose merged box has the least surface area,
+//         mutual nearest neighbours merge into a new node, and the clusters are
+//         compacted in order, until one is left
+//   4. top-down collapse into 8-wide nodes, level by level  (k_collapse)
 //      each wide node takes its binary node's two children and repeatedly opens
 //      the internal child of largest surface area until it has 8 children;
 //      children of at most 3 triangles that are left over become leaves.
@@ -20,6 +23,7 @@
 // The triangle set, and so the closest hit of every ray, is the reference's; only
 // the tree differs.  Its build is deterministic (no atomics decide structure).
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include <algorithm>
 #include <cstdio>
@@ -117,78 +121,100 @@ __global__ void k_morton(const float *__restrict__ verts, int n, const float *__
     vals[i] = static_cast<uint32_t>(i);
 }
 
-// common prefix length of sorted keys i, j (index tie-break for equal keys)
-__device__ __forceinline__ int delta(const uint64_t *__restrict__ k, int n, int i, int j) {
-    if (j < 0 || j >= n) return -1;
-    const uint64_t a = k[i], b = k[j];
-    if (a == b) return 64 + __clz(static_cast<uint32_t>(i ^ j));
-    return __clzll(a ^ b);
-}
-
-// internal nodes 0..n-2, leaf j is node n-1+j
-__global__ void k_karras(const uint64_t *__restrict__ keys, int n, int2 *__restrict__ child, int *__restrict__ parent,
-                         int2 *__restrict__ range) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int dir = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = delta(keys, n, i, i - dir);
-    int lmax = 2;
-    while (delta(keys, n, i, i + lmax * dir) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (delta(keys, n, i, i + (l + t) * dir) > dmin) l += t;
-    const int j = i + l * dir;
-    const int dnode = delta(keys, n, i, j);
-    int s = 0;
-    int div = 2;
-    int t;
-    do {
-        t = (l + div - 1) / div;
-        if (delta(keys, n, i, i + (s + t) * dir) > dnode) s += t;
-        div <<= 1;
-    } while (t > 1);
-    const int gamma = i + s * dir + min(dir, 0);
-    const int lo = min(i, j), hi = max(i, j);
-    const int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
-    const int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
-    child[i] = make_int2(left, right);
-    range[i] = make_int2(lo, hi);
-    parent[left] = i;
-    parent[right] = i;
-}
-
-__global__ void k_refit(const float *__restrict__ verts, const uint32_t *__restrict__ order, int n,
-                        const int2 *__restrict__ child, const int *__restrict__ parent, float4 *bmin, float4 *bmax,
-                        int *flags) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const float *v = verts + 9 * static_cast<int64_t>(order[j]);
-    int node = n - 1 + j;
-    bmin[node] = make_float4(fminf(v[0], fminf(v[3], v[6])), fminf(v[1], fminf(v[4], v[7])),
-                             fminf(v[2], fminf(v[5], v[8])), 0.0f);
-    bmax[node] = make_float4(fmaxf(v[0], fmaxf(v[3], v[6])), fmaxf(v[1], fmaxf(v[4], v[7])),
-                             fmaxf(v[2], fmaxf(v[5], v[8])), 0.0f);
-    __threadfence();
-    if (n == 1) return;
-    int p = parent[node];
-    while (true) {
-        if (atomicAdd(&flags[p], 1) == 0) return;   // the sibling finishes this node
-        __threadfence();
-        const int2 c = child[p];
-        const float4 a0 = __ldcg(&bmin[c.x]), a1 = __ldcg(&bmax[c.x]);
-        const float4 b0 = __ldcg(&bmin[c.y]), b1 = __ldcg(&bmax[c.y]);
-        __stcg(&bmin[p], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f));
-        __stcg(&bmax[p], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f));
-        __threadfence();
-        if (p == 0) return;
-        p = parent[p];
-    }
-}
-
 __device__ __forceinline__ float areaOf(float4 lo, float4 hi) {
     const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
     return 2.0f * (dx * dy + dy * dz + dz * dx);
 }
+
+// ---------------------------------------------------------------- clustering
+constexpr int kPlocRadius = 32;   // neighbours searched on each side, in code order
+constexpr int kPlocBlock = 256;
+
+// leaves: node n-1+j is the j-th triangle in code order
+__global__ void k_leaf_bounds(const float *__restrict__ verts, const uint32_t *__restrict__ order, int n,
+                              float4 *bmin, float4 *bmax, int *count, int *clusters) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const float *v = verts + 9 * static_cast<int64_t>(order[j]);
+    const int node = n - 1 + j;
+    bmin[node] = make_float4(fminf(v[0], fminf(v[3], v[6])), fminf(v[1], fminf(v[4], v[7])),
+                             fminf(v[2], fminf(v[5], v[8])), 0.0f);
+    bmax[node] = make_float4(fmaxf(v[0], fmaxf(v[3], v[6])), fmaxf(v[1], fmaxf(v[4], v[7])),
+                             fmaxf(v[2], fmaxf(v[5], v[8])), 0.0f);
+    count[node] = 1;
+    clusters[j] = node;
+}
+
+// nearest neighbour of each cluster: least surface area of the merged box among the
+// clusters within kPlocRadius positions (ties: the lower position); the window's boxes
+// are staged in shared memory
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const int *__restrict__ clusters, int m,
+                                                        const float4 *__restrict__ bmin,
+                                                        const float4 *__restrict__ bmax, int *nn) {
+    __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+    const int base = blockIdx.x * kPlocBlock - kPlocRadius;
+    for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += kPlocBlock) {
+        const int p = base + k;
+        if (p >= 0 && p < m) {
+            const int c = clusters[p];
+            slo[k] = bmin[c];
+            shi[k] = bmax[c];
+        }
+    }
+    __syncthreads();
+    const int i = blockIdx.x * kPlocBlock + threadIdx.x;
+    if (i >= m) return;
+    const int li = threadIdx.x + kPlocRadius;
+    const float4 lo = slo[li], hi = shi[li];
+    float best = 3.0e38f;
+    int bestJ = -1;
+    for (int d = -kPlocRadius; d <= kPlocRadius; d++) {
+        const int j = i + d;
+        if (d == 0 || j < 0 || j >= m) continue;
+        const float4 a = slo[li + d], b = shi[li + d];
+        const float area = areaOf(make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0.0f),
+                                  make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0.0f));
+        if (area < best) {
+            best = area;
+            bestJ = j;
+        }
+    }
+    nn[i] = bestJ;
+}
+
+// a cluster leads a merge when it and its neighbour chose each other and it comes
+// first; it survives the round unless it is the second of such a pair
+__global__ void k_ploc_flags(const int *__restrict__ nn, int m, int *lead, int *keep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    lead[i] = mutual && i < j ? 1 : 0;
+    keep[i] = mutual && i > j ? 0 : 1;
+}
+
+// merged nodes take ids top - leadOffset (descending, so the last merge, the root, is
+// node 0); survivors are compacted in order
+__global__ void k_ploc_merge(const int *__restrict__ clusters, int m, const int *__restrict__ nn,
+                             const int *__restrict__ lead, const int *__restrict__ leadOff,
+                             const int *__restrict__ keep, const int *__restrict__ keepOff, int top, int2 *child,
+                             float4 *bmin, float4 *bmax, int *count, int *next) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !keep[i]) return;
+    int node = clusters[i];
+    if (lead[i]) {
+        const int a = node, b = clusters[nn[i]];
+        const int id = top - leadOff[i];
+        child[id] = make_int2(a, b);
+        const float4 a0 = bmin[a], a1 = bmax[a], b0 = bmin[b], b1 = bmax[b];
+        bmin[id] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f);
+        bmax[id] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f);
+        count[id] = count[a] + count[b];
+        node = id;
+    }
+    next[keepOff[i]] = node;
+}
+
 
 struct CollapseArgs {
     const float *verts;
@@ -197,7 +223,7 @@ struct CollapseArgs {
     const int *tri_light;
     int n;
     const int2 *child;
-    const int2 *range;
+    const int *count;   // triangles under each binary node
     const float4 *bmin;
     const float4 *bmax;
     WideNode *nodes;
@@ -206,15 +232,22 @@ struct CollapseArgs {
     int *counters;   // [0] wide nodes allocated, [1] triangles placed, [2] next-level items
 };
 
-__device__ __forceinline__ void nodeRange(const CollapseArgs &A, int b, int *first, int *count) {
-    if (b >= A.n - 1) {
-        *first = b - (A.n - 1);
-        *count = 1;
-    } else {
-        const int2 r = A.range[b];
-        *first = r.x;
-        *count = r.y - r.x + 1;
+// the triangles (code-order positions) under binary node b, at most kLeafMax of them,
+// left subtree first
+__device__ __forceinline__ int leafPrims(const CollapseArgs &A, int b, int *pos) {
+    int stack[2 * kLeafMax], sp = 0, k = 0;
+    stack[sp++] = b;
+    while (sp > 0 && k < kLeafMax) {
+        const int x = stack[--sp];
+        if (x >= A.n - 1) {
+            pos[k++] = x - (A.n - 1);
+        } else if (sp + 2 <= 2 * kLeafMax) {
+            const int2 c = A.child[x];
+            stack[sp++] = c.y;
+            stack[sp++] = c.x;
+        }
     }
+    return k;
 }
 
 // one thread per wide node of the current level; items are (binary node, wide node)
@@ -294,8 +327,7 @@ __global__ void k_collapse(CollapseArgs A, const int2 *__restrict__ items, int n
     for (int s = 0; s < 8; s++) {
         const int c = slotChild[s];
         if (c < 0) continue;
-        int first, count;
-        nodeRange(A, c, &first, &count);
+        const int count = A.count[c];
         if (count > kLeafMax) {
             imask |= 1u << s;
             nInt++;
@@ -360,11 +392,11 @@ __global__ void k_collapse(CollapseArgs A, const int2 *__restrict__ items, int n
             next[itemBase + rank] = make_int2(c, childBase + rank);
             rank++;
         } else {
-            int first, count;
-            nodeRange(A, c, &first, &count);
+            int pos[kLeafMax];
+            const int count = leafPrims(A, c, pos);
             node.meta[s] = static_cast<uint8_t>((((1u << count) - 1u) << 5) | static_cast<uint32_t>(triOff));
             for (int q = 0; q < count; q++) {
-                const uint32_t prim = A.order[first + q];
+                const uint32_t prim = A.order[pos[q]];
                 const float *v = A.verts + 9 * static_cast<int64_t>(prim);
                 TriRecord r;
                 r.v0 = make_float4(v[0], v[1], v[2], __int_as_float(static_cast<int>(prim)));
@@ -408,9 +440,10 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
     uint64_t *keys[2] = {dalloc<uint64_t>(n), dalloc<uint64_t>(n)};
     uint32_t *vals[2] = {dalloc<uint32_t>(n), dalloc<uint32_t>(n)};
     int2 *child = dalloc<int2>(n);
-    int2 *range = dalloc<int2>(n);
-    int *parent = dalloc<int>(nNodes);
-    int *flags = dalloc<int>(n);
+    int *count = dalloc<int>(nNodes);
+    int *clusters[2] = {dalloc<int>(n), dalloc<int>(n)};
+    int *nn = dalloc<int>(n), *lead = dalloc<int>(n), *keep = dalloc<int>(n);
+    int *leadOff = dalloc<int>(n), *keepOff = dalloc<int>(n);
     float4 *bmin = dalloc<float4>(nNodes);
     float4 *bmax = dalloc<float4>(nNodes);
     int2 *items[2] = {dalloc<int2>(n), dalloc<int2>(n)};
@@ -419,14 +452,15 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
     out->tris = dalloc<TriRecord>(n);
     out->slot_shade = dalloc<int2>(n);
     int rc = 0;
-    void *tmp = nullptr;
-    size_t tmpBytes = 0;
+    void *tmp = nullptr, *scanTmp = nullptr;
+    size_t tmpBytes = 0, scanBytes = 0;
     auto fail = [&](const char *what, cudaError_t e) {
         snprintf(err, errlen, "buildWideBVH: %s: %s", what, cudaGetErrorString(e));
         rc = -3;
     };
-    if (!d_bounds || !keys[0] || !keys[1] || !vals[0] || !vals[1] || !child || !range || !parent || !flags ||
-        !bmin || !bmax || !items[0] || !items[1] || !counters || !out->nodes || !out->tris || !out->slot_shade) {
+    if (!d_bounds || !keys[0] || !keys[1] || !vals[0] || !vals[1] || !child || !count || !clusters[0] ||
+        !clusters[1] || !nn || !lead || !keep || !leadOff || !keepOff || !bmin || !bmax || !items[0] || !items[1] ||
+        !counters || !out->nodes || !out->tris || !out->slot_shade) {
         snprintf(err, errlen, "buildWideBVH: device allocation failed for %d triangles", n);
         rc = -4;
     }
@@ -434,7 +468,6 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
         const float init[12] = {3e38f, 3e38f, 3e38f, -3e38f, -3e38f, -3e38f,
                                 3e38f, 3e38f, 3e38f, -3e38f, -3e38f, -3e38f};
         cudaMemcpyAsync(d_bounds, init, sizeof(init), cudaMemcpyHostToDevice, stream);
-        cudaMemsetAsync(flags, 0, sizeof(int) * n, stream);
         cudaMemsetAsync(counters, 0, sizeof(int) * 4, stream);
         const int T = 256;
         k_prim_bounds<<<std::min((n + T - 1) / T, 1216), T, 0, stream>>>(d_verts, n, d_bounds);
@@ -442,23 +475,57 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
         cub::DoubleBuffer<uint64_t> kb(keys[0], keys[1]);
         cub::DoubleBuffer<uint32_t> vb(vals[0], vals[1]);
         cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, kb, vb, n, 0, 64, stream);
-        if (cudaMalloc(&tmp, tmpBytes) != cudaSuccess) {
+        cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, lead, leadOff, n, stream);
+        if (cudaMalloc(&tmp, tmpBytes) != cudaSuccess || cudaMalloc(&scanTmp, scanBytes) != cudaSuccess) {
             snprintf(err, errlen, "buildWideBVH: sort scratch allocation failed");
             rc = -4;
         } else {
             cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, kb, vb, n, 0, 64, stream);
             const uint64_t *sk = kb.Current();
             const uint32_t *order = vb.Current();
-            if (n > 1) k_karras<<<(n - 1 + T - 1) / T, T, 0, stream>>>(sk, n, child, parent, range);
-            k_refit<<<(n + T - 1) / T, T, 0, stream>>>(d_verts, order, n, child, parent, bmin, bmax, flags);
-            CollapseArgs A{d_verts, order, d_tri_mat, d_tri_light, n, child, range, bmin, bmax,
+            (void)sk;
+            k_leaf_bounds<<<(n + T - 1) / T, T, 0, stream>>>(d_verts, order, n, bmin, bmax, count, clusters[0]);
+            // clustering rounds: m clusters, merged nodes numbered downwards from top
+            int m = n, top = n - 2, cl = 0, rounds = 0;
+            while (m > 1 && rc == 0) {
+                const int B = (m + kPlocBlock - 1) / kPlocBlock;
+                k_ploc_nn<<<B, kPlocBlock, 0, stream>>>(clusters[cl], m, bmin, bmax, nn);
+                k_ploc_flags<<<B, kPlocBlock, 0, stream>>>(nn, m, lead, keep);
+                cub::DeviceScan::ExclusiveSum(scanTmp, scanBytes, lead, leadOff, m, stream);
+                cub::DeviceScan::ExclusiveSum(scanTmp, scanBytes, keep, keepOff, m, stream);
+                k_ploc_merge<<<B, kPlocBlock, 0, stream>>>(clusters[cl], m, nn, lead, leadOff, keep, keepOff, top,
+                                                           child, bmin, bmax, count, clusters[cl ^ 1]);
+                int tail[4] = {0, 0, 0, 0};   // leadOff, lead, keepOff, keep of the last cluster
+                cudaMemcpyAsync(&tail[0], leadOff + m - 1, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                cudaMemcpyAsync(&tail[1], lead + m - 1, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                cudaMemcpyAsync(&tail[2], keepOff + m - 1, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                cudaMemcpyAsync(&tail[3], keep + m - 1, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                const cudaError_t e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess) {
+                    fail("clustering", e);
+                    break;
+                }
+                const int merges = tail[0] + tail[1];
+                top -= merges;
+                m = tail[2] + tail[3];
+                cl ^= 1;
+                if (merges == 0 || ++rounds > 100000) {
+                    snprintf(err, errlen, "buildWideBVH: clustering made no progress");
+                    rc = -5;
+                }
+            }
+            if (rc == 0 && n > 1 && top != -1) {
+                snprintf(err, errlen, "buildWideBVH: clustering left %d node ids unused", top + 1);
+                rc = -5;
+            }
+            CollapseArgs A{d_verts, order, d_tri_mat, d_tri_light, n, child, count, bmin, bmax,
                            out->nodes, out->tris, out->slot_shade, counters};
             // root: wide node 0 from binary root (internal 0, or the single leaf)
             const int one = 1;
             const int2 root = make_int2(n > 1 ? 0 : 0 + (n - 1), 0);
             cudaMemcpyAsync(items[0], &root, sizeof(int2), cudaMemcpyHostToDevice, stream);
             cudaMemcpyAsync(counters, &one, sizeof(int), cudaMemcpyHostToDevice, stream);
-            int nitems = 1, depth = 0, cur = 0;
+            int nitems = rc == 0 ? 1 : 0, depth = 0, cur = 0;
             while (nitems > 0) {
                 cudaMemsetAsync(counters + 2, 0, sizeof(int), stream);
                 k_collapse<<<(nitems + 127) / 128, 128, 0, stream>>>(A, items[cur], nitems, items[cur ^ 1]);
@@ -500,15 +567,21 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
         }
     }
     cudaFree(tmp);
+    cudaFree(scanTmp);
     cudaFree(d_bounds);
     cudaFree(keys[0]);
     cudaFree(keys[1]);
     cudaFree(vals[0]);
     cudaFree(vals[1]);
     cudaFree(child);
-    cudaFree(range);
-    cudaFree(parent);
-    cudaFree(flags);
+    cudaFree(count);
+    cudaFree(clusters[0]);
+    cudaFree(clusters[1]);
+    cudaFree(nn);
+    cudaFree(lead);
+    cudaFree(keep);
+    cudaFree(leadOff);
+    cudaFree(keepOff);
     cudaFree(bmin);
     cudaFree(bmax);
     cudaFree(items[0]);
