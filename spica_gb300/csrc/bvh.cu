@@ -12,10 +12,14 @@
 //         within kPlocRadius positions whose merged box has the least surface area,
 //         mutual nearest neighbours merge into a new node, and the clusters are
 //         compacted in order, until one is left
-//   4. top-down collapse into 8-wide nodes, level by level  (k_collapse)
-//      each wide node takes its binary node's two children and repeatedly opens
-//      the internal child of largest surface area until it has 8 children;
-//      children of at most 3 triangles that are left over become leaves.
+//   4. SAH-optimal choice of the wide tree, bottom-up over the clustering rounds
+//      (k_dp_round) -- the dynamic programme of Ylitie, Karras and Laine,
+//      "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs"
+//      (HPG 2017): for every binary node, the least SAH cost of spreading 1..8
+//      child slots over its subtree, where a node is a leaf (at most 3 triangles),
+//      a wide node, or passes slots on to its two children
+//   5. top-down collapse into 8-wide nodes, level by level  (k_collapse),
+//      following those decisions
 //      Children are placed in slots by a greedy octant assignment so that the
 //      traversal's slot order s ^ (7 - octant) runs roughly front to back, their
 //      boxes are quantised conservatively to 8 bits on the node's grid, and leaf
@@ -131,18 +135,44 @@ constexpr int kPlocRadius = 32;   // neighbours searched on each side, in code o
 constexpr int kPlocBlock = 256;
 
 // leaves: node n-1+j is the j-th triangle in code order
+// SAH weights of the wide tree: a wide-node visit, a triangle test.  Equal weights were
+// measured best for this traversal (triangle weight 0.3 / 0.6 / 1.0 / 1.5: 884 / 892 /
+// 900 / 887 M path samples/s on the 1080p render; the 1M-triangle microbench also peaks
+// at 1.0)
+constexpr float kCostNode = 1.0f, kCostTri = 1.0f;
+
+// per binary node: cost[8 * node + j - 1] = least SAH cost of its subtree over j child
+// slots; split[8 * node + j - 1] = slots given to the left child (0: the node itself
+// takes one slot); split of j = 8 before that choice is the node's own split as a wide
+// node (wideSplit); leaf[node]: the node itself is cheaper as a leaf than as a wide node
+struct DpArgs {
+    float *cost;
+    uint8_t *split;
+    uint8_t *wideSplit;
+    uint8_t *leaf;
+};
+
 __global__ void k_leaf_bounds(const float *__restrict__ verts, const uint32_t *__restrict__ order, int n,
-                              float4 *bmin, float4 *bmax, int *count, int *clusters) {
+                              float4 *bmin, float4 *bmax, int *count, int *clusters, DpArgs D) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const float *v = verts + 9 * static_cast<int64_t>(order[j]);
     const int node = n - 1 + j;
-    bmin[node] = make_float4(fminf(v[0], fminf(v[3], v[6])), fminf(v[1], fminf(v[4], v[7])),
-                             fminf(v[2], fminf(v[5], v[8])), 0.0f);
-    bmax[node] = make_float4(fmaxf(v[0], fmaxf(v[3], v[6])), fmaxf(v[1], fmaxf(v[4], v[7])),
-                             fmaxf(v[2], fmaxf(v[5], v[8])), 0.0f);
+    const float4 lo = make_float4(fminf(v[0], fminf(v[3], v[6])), fminf(v[1], fminf(v[4], v[7])),
+                                  fminf(v[2], fminf(v[5], v[8])), 0.0f);
+    const float4 hi = make_float4(fmaxf(v[0], fmaxf(v[3], v[6])), fmaxf(v[1], fmaxf(v[4], v[7])),
+                                  fmaxf(v[2], fmaxf(v[5], v[8])), 0.0f);
+    bmin[node] = lo;
+    bmax[node] = hi;
     count[node] = 1;
     clusters[j] = node;
+    const float2 dx = make_float2(hi.x - lo.x, hi.y - lo.y);
+    const float c = kCostTri * 2.0f * (dx.x * dx.y + dx.y * (hi.z - lo.z) + (hi.z - lo.z) * dx.x);
+    for (int k = 0; k < 8; k++) {
+        D.cost[8 * static_cast<int64_t>(node) + k] = c;
+        D.split[8 * static_cast<int64_t>(node) + k] = 0;
+    }
+    D.leaf[node] = 1;
 }
 
 // nearest neighbour of each cluster: least surface area of the merged box among the
@@ -216,6 +246,53 @@ __global__ void k_ploc_merge(const int *__restrict__ clusters, int m, const int 
 }
 
 
+// one clustering round's nodes (ids lo..hi; their children are from earlier rounds)
+__global__ void k_dp_round(const int2 *__restrict__ child, const int *__restrict__ count,
+                           const float4 *__restrict__ bmin, const float4 *__restrict__ bmax, int lo, int hi,
+                           DpArgs D, int kLeafLimit) {
+    const int id = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (id > hi) return;
+    const int2 c = child[id];
+    const float *CL = D.cost + 8 * static_cast<int64_t>(c.x), *CR = D.cost + 8 * static_cast<int64_t>(c.y);
+    float S[9];
+    uint8_t K[9];
+    S[1] = 3.0e38f;
+    K[1] = 0;
+    for (int j = 2; j <= 8; j++) {
+        float best = 3.0e38f;
+        uint8_t bk = 1;
+        for (int k = 1; k < j; k++) {
+            const float v = CL[k - 1] + CR[j - k - 1];
+            if (v < best) {
+                best = v;
+                bk = static_cast<uint8_t>(k);
+            }
+        }
+        S[j] = best;
+        K[j] = bk;
+        if (j > 2 && S[j - 1] <= S[j]) {   // fewer slots may be cheaper: keep that split
+            S[j] = S[j - 1];
+            K[j] = K[j - 1];
+        }
+    }
+    const float A = areaOf(bmin[id], bmax[id]);
+    const float cInternal = kCostNode * A + S[8];
+    const float cLeaf = count[id] <= kLeafLimit ? kCostTri * A * static_cast<float>(count[id]) : 3.0e38f;
+    const bool asLeaf = cLeaf <= cInternal;
+    const float C = asLeaf ? cLeaf : cInternal;
+    float *out = D.cost + 8 * static_cast<int64_t>(id);
+    uint8_t *sp = D.split + 8 * static_cast<int64_t>(id);
+    out[0] = C;
+    sp[0] = 0;
+    for (int j = 2; j <= 8; j++) {
+        const bool self = C <= S[j];
+        out[j - 1] = self ? C : S[j];
+        sp[j - 1] = self ? 0 : K[j];
+    }
+    D.wideSplit[id] = K[8];
+    D.leaf[id] = asLeaf ? 1 : 0;
+}
+
 struct CollapseArgs {
     const float *verts;
     const uint32_t *order;
@@ -224,6 +301,7 @@ struct CollapseArgs {
     int n;
     const int2 *child;
     const int *count;   // triangles under each binary node
+    DpArgs dp;
     const float4 *bmin;
     const float4 *bmax;
     WideNode *nodes;
@@ -261,24 +339,25 @@ __global__ void k_collapse(CollapseArgs A, const int2 *__restrict__ items, int n
     if (rootLeaf) {
         C[nc++] = b;
     } else {
-        C[nc++] = A.child[b].x;
-        C[nc++] = A.child[b].y;
-        while (nc < 8) {
-            int best = -1;
-            float bestA = -1.0f;
-            for (int k = 0; k < nc; k++) {
-                if (C[k] < A.n - 1) {
-                    const float a = areaOf(A.bmin[C[k]], A.bmax[C[k]]);
-                    if (a > bestA) {
-                        bestA = a;
-                        best = k;
-                    }
-                }
+        // the 8 slots of wide node b, spread as the SAH programme decided: (node, slots)
+        int stN[8], stJ[8], sp = 0;
+        const int k0 = A.dp.wideSplit[b];
+        stN[sp] = A.child[b].y;
+        stJ[sp++] = 8 - k0;
+        stN[sp] = A.child[b].x;
+        stJ[sp++] = k0;
+        while (sp > 0 && nc < 8) {
+            const int x = stN[--sp], j = stJ[sp];
+            const int k = (x < A.n - 1 && j > 1) ? A.dp.split[8 * static_cast<int64_t>(x) + j - 1] : 0;
+            if (k == 0 || sp + 2 > 8) {
+                C[nc++] = x;
+            } else {
+                const int2 cc = A.child[x];
+                stN[sp] = cc.y;
+                stJ[sp++] = j - k;
+                stN[sp] = cc.x;
+                stJ[sp++] = k;
             }
-            if (best < 0) break;
-            const int2 cc = A.child[C[best]];
-            C[best] = cc.x;
-            C[nc++] = cc.y;
         }
     }
     // node box
@@ -328,7 +407,7 @@ __global__ void k_collapse(CollapseArgs A, const int2 *__restrict__ items, int n
         const int c = slotChild[s];
         if (c < 0) continue;
         const int count = A.count[c];
-        if (count > kLeafMax) {
+        if (c < A.n - 1 && (count > kLeafMax || !A.dp.leaf[c])) {
             imask |= 1u << s;
             nInt++;
         } else {
@@ -446,6 +525,8 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
     int *leadOff = dalloc<int>(n), *keepOff = dalloc<int>(n);
     float4 *bmin = dalloc<float4>(nNodes);
     float4 *bmax = dalloc<float4>(nNodes);
+    DpArgs dp{dalloc<float>(8 * static_cast<size_t>(nNodes)), dalloc<uint8_t>(8 * static_cast<size_t>(nNodes)),
+              dalloc<uint8_t>(n), dalloc<uint8_t>(nNodes)};
     int2 *items[2] = {dalloc<int2>(n), dalloc<int2>(n)};
     int *counters = dalloc<int>(4);
     out->nodes = dalloc<WideNode>(n);
@@ -459,7 +540,8 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
         rc = -3;
     };
     if (!d_bounds || !keys[0] || !keys[1] || !vals[0] || !vals[1] || !child || !count || !clusters[0] ||
-        !clusters[1] || !nn || !lead || !keep || !leadOff || !keepOff || !bmin || !bmax || !items[0] || !items[1] ||
+        !clusters[1] || !nn || !lead || !keep || !leadOff || !keepOff || !bmin || !bmax || !dp.cost || !dp.split ||
+        !dp.wideSplit || !dp.leaf || !items[0] || !items[1] ||
         !counters || !out->nodes || !out->tris || !out->slot_shade) {
         snprintf(err, errlen, "buildWideBVH: device allocation failed for %d triangles", n);
         rc = -4;
@@ -484,9 +566,11 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
             const uint64_t *sk = kb.Current();
             const uint32_t *order = vb.Current();
             (void)sk;
-            k_leaf_bounds<<<(n + T - 1) / T, T, 0, stream>>>(d_verts, order, n, bmin, bmax, count, clusters[0]);
+            k_leaf_bounds<<<(n + T - 1) / T, T, 0, stream>>>(d_verts, order, n, bmin, bmax, count, clusters[0],
+                                                                 dp);
             // clustering rounds: m clusters, merged nodes numbered downwards from top
             int m = n, top = n - 2, cl = 0, rounds = 0;
+            std::vector<int2> roundIds;   // node ids created by each round, in round order
             while (m > 1 && rc == 0) {
                 const int B = (m + kPlocBlock - 1) / kPlocBlock;
                 k_ploc_nn<<<B, kPlocBlock, 0, stream>>>(clusters[cl], m, bmin, bmax, nn);
@@ -506,6 +590,7 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
                     break;
                 }
                 const int merges = tail[0] + tail[1];
+                if (merges > 0) roundIds.push_back(make_int2(top - merges + 1, top));
                 top -= merges;
                 m = tail[2] + tail[3];
                 cl ^= 1;
@@ -518,7 +603,12 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
                 snprintf(err, errlen, "buildWideBVH: clustering left %d node ids unused", top + 1);
                 rc = -5;
             }
-            CollapseArgs A{d_verts, order, d_tri_mat, d_tri_light, n, child, count, bmin, bmax,
+            // the SAH programme, one launch per clustering round (children before parents)
+            for (const int2 r : roundIds) {
+                const int cnt = r.y - r.x + 1;
+                k_dp_round<<<(cnt + T - 1) / T, T, 0, stream>>>(child, count, bmin, bmax, r.x, r.y, dp, kLeafMax);
+            }
+            CollapseArgs A{d_verts, order, d_tri_mat, d_tri_light, n, child, count, dp, bmin, bmax,
                            out->nodes, out->tris, out->slot_shade, counters};
             // root: wide node 0 from binary root (internal 0, or the single leaf)
             const int one = 1;
@@ -584,6 +674,10 @@ int buildWideBVH(const float *d_verts, int n, const int *d_tri_mat, const int *d
     cudaFree(keepOff);
     cudaFree(bmin);
     cudaFree(bmax);
+    cudaFree(dp.cost);
+    cudaFree(dp.split);
+    cudaFree(dp.wideSplit);
+    cudaFree(dp.leaf);
     cudaFree(items[0]);
     cudaFree(items[1]);
     cudaFree(counters);
