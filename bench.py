@@ -50,7 +50,7 @@ CONFIG = {"workload": "mid-scale plain render: 500 instances, ~2.03M triangles, 
 
 
 E2E_SPP = 16   # samples per pixel per host-API render call in the end-to-end measurement
-EXTEND_DRAM_BYTES_PER_LAUNCH = 29.27e6   # measured with ncu on the 1920x1080 workload
+EXTEND_DRAM_BYTES_PER_LAUNCH = 28.68e6   # measured with ncu on the 1920x1080 workload
 
 
 def max_over_ranks(torch, x: float, ws: int, device: str = "cuda") -> float:
