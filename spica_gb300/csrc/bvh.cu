@@ -99,8 +99,9 @@ __device__ __forceinline__ uint64_t spread21(uint32_t x) {
 // 0-62 are the 63-bit Morton code of its box centre.  The size bit is the extended
 // Morton code idea of Vinkler, Bittner and Havran ("Extended Morton codes for high
 // performance bounding volume hierarchy construction", HPG 2017) reduced to one class:
-// the radix tree's root splits the large triangles (a floor quad, room walls) into a
-// subtree of their own, instead of leaving them deep among small ones where every
+// large triangles (a floor quad, room walls) sort after all others, so the clustering,
+// which merges only within a window of this order, joins them with each other first and
+// with the rest near the root, instead of leaving them deep among small ones where every
 // ancestor's box would span them.
 constexpr float kLargeTriangle = 1.0f / 8.0f;
 
