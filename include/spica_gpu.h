@@ -42,6 +42,8 @@ typedef struct spgpu_ctx spgpu_ctx;
 #define SPGPU_MAT_ROUGH_DIELECTRIC 3 /* [1] alpha, [2] interior IOR, [3] 0 Beckmann / 1 GGX
                                         (bsdfs/roughdielectric.cc, white Kr / Kt) */
 #define SPGPU_MAT_PLASTIC 4    /* [1..3] Kd, [4..6] Ks, [7] IOR (bsdfs/plastic.cc) */
+#define SPGPU_MAT_CONDUCTOR_BECKMANN 5 /* as SPGPU_MAT_CONDUCTOR with the Beckmann distribution
+                                          (bsdfs/roughconductor.cc, distribution "beckmann") */
 
 typedef struct {
     int device;          /* CUDA device ordinal */
@@ -295,7 +297,7 @@ int spgpu_write_png(const char *path, const uint8_t *rgb, int32_t width, int32_t
  * takes (camera, film size, sampleCount, maxDepth, integrator; seed and sample_offset
  * 0).  Accepted: perspective sensors, hdr / ldr films, the independent sampler, the
  * path and direct-lighting integrators (or the gpupath / gpudirect drop-ins), BSDFs
- * diffuse, roughconductor (ggx), dielectric, roughdielectric and plastic with constant
+ * diffuse, roughconductor, dielectric, roughdielectric and plastic with constant
  * parameters, PLY (binary little endian) and OBJ meshes, area emitters and one
  * untransformed .hdr environment map; anything else is SPGPU_EINVAL with the element
  * and the reason in spgpu_last_error().  Free the result with spgpu_scene_free. */

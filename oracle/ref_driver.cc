@@ -84,11 +84,11 @@ std::shared_ptr<SurfaceMaterial> makeSurface(const double *m) {
     if (type == SPO_MAT_LAMBERT) {
         return std::make_shared<Diffuse>(constTex(Spectrum(m[1], m[2], m[3])));
     }
-    if (type == SPO_MAT_CONDUCTOR) {
+    if (type == SPO_MAT_CONDUCTOR || type == SPO_MAT_CONDUCTOR_BECKMANN) {
         auto alpha = constTex(Spectrum(m[1]));
         return std::make_shared<RoughConductor>(constTex(Spectrum(m[2], m[3], m[4])),
-                                                constTex(Spectrum(m[5], m[6], m[7])),
-                                                alpha, alpha, "ggx", nullptr, false);
+                                                constTex(Spectrum(m[5], m[6], m[7])), alpha, alpha,
+                                                type == SPO_MAT_CONDUCTOR ? "ggx" : "beckmann", nullptr, false);
     }
     if (type == SPO_MAT_ROUGH_DIELECTRIC) {
         auto alpha = constTex(Spectrum(m[1]));

@@ -998,7 +998,7 @@ struct BSDF {
     GGX ggx{1, 1};
     RGB eta, k;           // conductor
     double ior = 1.0;     // dielectric, rough dielectric, plastic
-    bool beckmann = true; // rough dielectric distribution
+    bool beckmann = true; // microfacet distribution (rough dielectric, rough conductor)
     Beckmann bk{1, 1};
     RGB Kd, Ks;           // plastic
     double specWeight = 0.0;
@@ -1065,7 +1065,7 @@ struct BSDF {
             if (wh.x == 0.0 && wh.y == 0.0 && wh.z == 0.0) return RGB(0.0);
             wh = normalizedMul(wh);
             const RGB F = frConductor(std::abs(dot(wi, wh)), RGB(1.0), eta, k);
-            return RGB(1.0) * ggx.D(wh) * ggx.G(wo, wi, wh) * F / (4.0 * cI * cO);
+            return RGB(1.0) * mD(wh) * mG(wo, wi, wh) * F / (4.0 * cI * cO);
         }
         if (kind == SPO_MAT_DIELECTRIC) {   // FresnelSpecular::f, bxdf.cc:171
             const double F = frDielectric(cosT(wo), 1.0, ior);
@@ -1103,7 +1103,7 @@ struct BSDF {
         if (kind == SPO_MAT_CONDUCTOR) {
             if (!sameHemi(wo, wi)) return 0.0;
             const V3 wh = normalizeDiv(wo + wi);
-            return ggx.pdf(wo, wh) / (4.0 * dot(wo, wh));
+            return mPdf(wo, wh) / (4.0 * dot(wo, wh));
         }
         if (kind == SPO_MAT_DIELECTRIC) {
             const double F = frDielectric(cosT(wo), 1.0, ior);
@@ -1163,12 +1163,12 @@ struct BSDF {
             *pdf = pdfLocal(wo, wi);
             ret = fLocal(wo, wi);
         } else if (kind == SPO_MAT_CONDUCTOR) {   // MicrofacetReflection::sample, bxdf.cc:282
-            const V3 wh = ggx.sample(wo, ur);
+            const V3 wh = mSample(wo, ur);
             wi = reflectV(wo, wh);
             if (!sameHemi(wo, wi)) {
                 ret = RGB(0.0);
             } else {
-                *pdf = ggx.pdf(wo, wh) / (4.0 * dot(wo, wh));
+                *pdf = mPdf(wo, wh) / (4.0 * dot(wo, wh));
                 ret = fLocal(wo, wi);
             }
         } else if (kind == SPO_MAT_ROUGH_DIELECTRIC) {   // MicrofacetTransmission::sample, bxdf.cc:356
@@ -1247,10 +1247,13 @@ inline BSDF makeBSDF(const double *m, const V3 &ns, const V3 &ts, const V3 &bs) 
     if (type == SPO_MAT_LAMBERT) {   // Diffuse::setScatterFuncs, diffuse.cc:23
         b.R = RGB(std::max(0.0, m[1]), std::max(0.0, m[2]), std::max(0.0, m[3]));
         if (!b.R.isBlack()) b.kind = SPO_MAT_LAMBERT;
-    } else if (type == SPO_MAT_CONDUCTOR) {   // RoughConductor::setScatterFuncs, roughconductor.cc:38
+    } else if (type == SPO_MAT_CONDUCTOR || type == SPO_MAT_CONDUCTOR_BECKMANN) {
+        // RoughConductor::setScatterFuncs, roughconductor.cc:38
         b.kind = SPO_MAT_CONDUCTOR;
         const double a = RGB(m[1]).gray();
+        b.beckmann = type == SPO_MAT_CONDUCTOR_BECKMANN;
         b.ggx = GGX{a, a};
+        b.bk = Beckmann{a, a};
         b.eta = RGB(m[2], m[3], m[4]);
         b.k = RGB(m[5], m[6], m[7]);
     } else if (type == SPO_MAT_ROUGH_DIELECTRIC) {   // RoughDielectric::setScatterFuncs, roughdielectric.cc:41

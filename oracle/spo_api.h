@@ -30,6 +30,7 @@ extern "C" {
 #define SPO_MAT_ROUGH_DIELECTRIC 3 /* [1] alpha, [2] interior IOR, [3] 0 Beckmann / 1 GGX, white Kr/Kt
                                      (bsdfs/roughdielectric.cc)                                  */
 #define SPO_MAT_PLASTIC    4 /* [1..3] Kd RGB, [4..6] Ks RGB, [7] IOR     (bsdfs/plastic.cc)          */
+#define SPO_MAT_CONDUCTOR_BECKMANN 5 /* as SPO_MAT_CONDUCTOR, distribution "beckmann"                  */
 #define SPO_MAT_STRIDE     8
 
 typedef struct spo_scene spo_scene;

@@ -542,11 +542,13 @@ int spgpu_upload_scene(spgpu_ctx *h, int32_t ntri, const float *verts, const int
         MaterialRecord &M = mats[m];
         std::memset(&M, 0, sizeof(M));
         M.type = static_cast<int>(r[0]);
+        const bool beckmannConductor = M.type == SPGPU_MAT_CONDUCTOR_BECKMANN;
+        if (beckmannConductor) M.type = kMatConductor;
         if (M.type == kMatLambert) {
             M.a = make_float4(fmaxf(r[1], 0.0f), fmaxf(r[2], 0.0f), fmaxf(r[3], 0.0f), 0.0f);
         } else if (M.type == kMatConductor) {
             M.a = make_float4(r[2], r[3], r[4], static_cast<float>(gray1(r[1])));
-            M.b = make_float4(r[5], r[6], r[7], 0.0f);
+            M.b = make_float4(r[5], r[6], r[7], beckmannConductor ? 1.0f : 0.0f);   // b.w: distribution
             if (!(M.a.w > 0.0f)) {
                 setError("spgpu_upload_scene: conductor roughness must be positive (smooth conductors are not supported)");
                 return SPGPU_EINVAL;

@@ -272,18 +272,6 @@ __device__ __forceinline__ float ggxLambda(float3 w, float a) {
     const float ai = a * at;
     return (-1.0f + sqrtf(1.0f + ai * ai)) * 0.5f;
 }
-__device__ __forceinline__ float ggxG1(float3 w, float3 wh, float a) {
-    if (w.z * dot(w, wh) <= 0.0f) return 0.0f;
-    return 1.0f / (1.0f + ggxLambda(w, a));
-}
-__device__ __forceinline__ float ggxG(float3 wo, float3 wi, float3 wh, float a) {
-    if (wi.z * dot(wi, wh) <= 0.0f) return 0.0f;
-    if (wo.z * dot(wo, wh) <= 0.0f) return 0.0f;
-    return 1.0f / (1.0f + ggxLambda(wo, a) + ggxLambda(wi, a));
-}
-__device__ __forceinline__ float ggxPdf(float3 wo, float3 wh, float a) {   // visible normals
-    return ggxD(wh, a) * ggxG1(wo, wh, a) * fabsf(dot(wo, wh)) / fabsf(wo.z);
-}
 // visible-normal sampling, Heitz and d'Eon, "Importance Sampling Microfacet-Based
 // BSDFs using the Distribution of Visible Normals" (EGSR 2014): stretch, sample the
 // slopes of the unit-roughness distribution, rotate, unstretch.
@@ -318,22 +306,6 @@ __device__ __forceinline__ void ggxSample11(float cosTheta, float u0, float u1, 
     const float z = (U * (U * (U * 0.27385f - 0.73369f) + 0.46341f)) /
                     (U * (U * (U * 0.093073f + 0.309420f) - 1.0f) + 0.597999f);
     *sy = S * z * sqrtf(1.0f + (*sx) * (*sx));
-}
-__device__ __forceinline__ float3 ggxSampleWh(float3 wo, float a, float u0, float u1) {
-    const bool flip = wo.z < 0.0f;
-    const float3 w = flip ? -wo : wo;
-    const float3 ws = normalize(mk(a * w.x, a * w.y, w.z));
-    float sx, sy;
-    ggxSample11(ws.z, u0, u1, &sx, &sy);
-    const float st = sqrtf(fmaxf(0.0f, 1.0f - ws.z * ws.z));
-    const float cp = st == 0.0f ? 1.0f : clampf(ws.x / st, -1.0f, 1.0f);
-    const float sp = st == 0.0f ? 0.0f : clampf(ws.y / st, -1.0f, 1.0f);
-    const float tmp = cp * sx - sp * sy;
-    sy = sp * sx + cp * sy;
-    sx = tmp * a;
-    sy = sy * a;
-    float3 wh = normalize(mk(-sx, -sy, 1.0f));
-    return flip ? -wh : wh;
 }
 
 // The reference's own erfinv and erf (core/math.h:14-67): Giles' single-precision
@@ -445,6 +417,24 @@ __device__ __forceinline__ float3 visibleNormal(float3 wo, float a, float u0, fl
     return flip ? -wh : wh;
 }
 
+// microfacet distribution of a rough conductor (a.w alpha, b.w 0 GGX / 1 Beckmann):
+// MicrofacetDistribution's D, G and visible-normal pdf (microfacet.cc:15-60)
+__device__ __forceinline__ float condD(const MaterialRecord &m, float3 wh) {
+    return m.b.w != 0.0f ? beckD(wh, m.a.w) : ggxD(wh, m.a.w);
+}
+__device__ __forceinline__ float condLambda(const MaterialRecord &m, float3 w) {
+    return m.b.w != 0.0f ? beckLambda(w, m.a.w) : ggxLambda(w, m.a.w);
+}
+__device__ __forceinline__ float condG(const MaterialRecord &m, float3 wo, float3 wi, float3 wh) {
+    if (wi.z * dot(wi, wh) <= 0.0f) return 0.0f;
+    if (wo.z * dot(wo, wh) <= 0.0f) return 0.0f;
+    return 1.0f / (1.0f + condLambda(m, wo) + condLambda(m, wi));
+}
+__device__ __forceinline__ float condPdf(const MaterialRecord &m, float3 wo, float3 wh) {
+    const float g1 = wo.z * dot(wo, wh) <= 0.0f ? 0.0f : 1.0f / (1.0f + condLambda(m, wo));
+    return condD(m, wh) * g1 * fabsf(dot(wo, wh)) / fabsf(wo.z);
+}
+
 // microfacet distribution of a rough dielectric (a.x alpha, a.z 0 Beckmann / 1 GGX)
 __device__ __forceinline__ float mfD(const MaterialRecord &m, float3 wh) {
     return m.a.z == 0.0f ? beckD(wh, m.a.x) : ggxD(wh, m.a.x);
@@ -551,9 +541,8 @@ __device__ __forceinline__ float3 bsdfF(const MaterialRecord &m, float3 wo, floa
         float3 wh = wi + wo;
         if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return mk(0, 0, 0);
         wh = normalize(wh);
-        const float a = m.a.w;
         const float3 F = frConductor(fabsf(dot(wi, wh)), xyz(m.a), xyz(m.b));
-        return F * (ggxD(wh, a) * ggxG(wo, wi, wh, a) / (4.0f * cI * cO));
+        return F * (condD(m, wh) * condG(m, wo, wi, wh) / (4.0f * cI * cO));
     }
     if (m.type == kMatRoughDielectric) {
         if (wo.z == 0.0f || wi.z == 0.0f) return mk(0, 0, 0);
@@ -577,7 +566,7 @@ __device__ __forceinline__ float bsdfPdf(const MaterialRecord &m, float3 wo, flo
     if (m.type == kMatLambert) return fabsf(wi.z) * kInvPi;
     if (m.type == kMatConductor) {
         const float3 wh = normalize(wo + wi);
-        return ggxPdf(wo, wh, m.a.w) / (4.0f * dot(wo, wh));
+        return condPdf(m, wo, wh) / (4.0f * dot(wo, wh));
     }
     if (m.type == kMatPlastic) {
         const float ps = plasticProbSpecular(m, wo);
@@ -606,12 +595,13 @@ __device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo,
         *type = kReflection | kDiffuse;
         return bsdfF(m, wo, w);
     }
-    if (m.type == kMatConductor) {
-        const float3 wh = ggxSampleWh(wo, m.a.w, ur0, u1);
+    if (m.type == kMatConductor) {   // MicrofacetReflection::sample, bxdf.cc:282
+        const float3 wh = m.b.w != 0.0f ? visibleNormal<true>(wo, m.a.w, ur0, u1)
+                                        : visibleNormal<false>(wo, m.a.w, ur0, u1);
         const float3 w = -wo + wh * (2.0f * dot(wh, wo));
         if (wo.z * w.z <= 0.0f) return mk(0, 0, 0);
         *wi = w;
-        *pdf = ggxPdf(wo, wh, m.a.w) / (4.0f * dot(wo, wh));
+        *pdf = condPdf(m, wo, wh) / (4.0f * dot(wo, wh));
         *type = kReflection | kGlossy;
         return bsdfF(m, wo, w);
     }

@@ -21,8 +21,8 @@
 //     radians (core/transform.cc:136), lookAt is Transform::lookAt.
 // Only what the GPU path renders is accepted: perspective sensors (no depth of field),
 // hdr / ldr films, the independent sampler, the path and direct-lighting integrators
-// (and the gpupath / gpudirect drop-ins), BSDFs diffuse, roughconductor (GGX),
-// dielectric, roughdielectric and plastic with constant parameters, PLY and OBJ meshes,
+// (and the gpupath / gpudirect drop-ins), BSDFs diffuse, roughconductor, dielectric,
+// roughdielectric and plastic with constant parameters, PLY and OBJ meshes,
 // area lights and an untransformed .hdr environment map.  Anything else is refused
 // with the element and the reason.
 #include <cctype>
@@ -765,8 +765,8 @@ private:
                 if (!tex("eta", a, true, nullptr) || !tex("k", b, true, nullptr) || !tex("alpha", c, false, alpha0))
                     return false;
                 store_.strings.get("distribution", &dist, true);
-                if (dist != "ggx") return fail(e, "roughconductor: only the ggx distribution has a GPU counterpart");
-                M[0] = SPGPU_MAT_CONDUCTOR;
+                if (dist != "ggx" && dist != "beckmann") return fail(e, "unknown distribution " + dist);
+                M[0] = dist == "ggx" ? SPGPU_MAT_CONDUCTOR : SPGPU_MAT_CONDUCTOR_BECKMANN;
                 M[1] = static_cast<float>(grayOf(c));
                 for (int i = 0; i < 3; i++) {
                     M[2 + i] = static_cast<float>(a[i]);

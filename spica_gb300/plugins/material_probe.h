@@ -7,11 +7,12 @@
 // The BSDF must be built in a unit frame (shading normal z, dpdu x, dpdv y), so that
 // world and local directions coincide.  BxDF types (core/bxdf.cc) decide the material:
 //   Reflection|Diffuse                     Lambert          R = pi f(z, z)
-//   Reflection|Glossy                      GGX conductor    alpha from pdf(z, z) = 1 / (4 pi alpha^2),
+//   Reflection|Glossy                      rough conductor  alpha from pdf(z, z) = 1 / (4 pi alpha^2),
 //                                                           F0 = 4 pi alpha^2 f(z, z), stored as
 //                                                           eta = 1, k = 2 sqrt(F0 / (1 - F0)) (exact
 //                                                           for F0-authored conductors; others are
-//                                                           matched at normal incidence)
+//                                                           matched at normal incidence); GGX or
+//                                                           Beckmann from f along a retro direction
 //   Reflection|Transmission|Specular       dielectric       IOR = BSDF::eta() (bsdfs/dielectric.cc:38)
 //   Reflection|Transmission|Glossy         rough dielectric IOR = BSDF::eta(); alpha from
 //                                                           pdf(z, z) = F0 / (4 pi alpha^2); Beckmann
@@ -188,7 +189,21 @@ inline int probeMaterial(const BSDF *b, float rec[8], std::string *why) {
         const double alpha = std::sqrt(1.0 / (4.0 * ::PI * pdf));
         const Spectrum f = b->f(z, z);
         const double f0[3] = {f.red(), f.green(), f.blue()};
-        rec[0] = SPGPU_MAT_CONDUCTOR;
+        // the distribution: along the retro-reflection direction w (half vector w, so the
+        // Fresnel factor is the normal-incidence one) f(w, w) / f(z, z) is
+        // D(w) G(w, w, w) / (cos^2 D(z)), which tells Beckmann from GGX
+        const Vector3d w = direction(0.9, 0.4);
+        const double ratio = b->f(w, w).gray() / f.gray();
+        spica::BeckmannDistribution beckmann(alpha, alpha);
+        spica::TrowbridgeReitzDistribution ggx(alpha, alpha);
+        auto shape = [&](const spica::MicrofacetDistribution &d) {
+            return d.D(w) * d.G(w, w, w) / (w.z() * w.z() * d.D(z));
+        };
+        int type;
+        if (relDiff(ratio, shape(ggx)) < 1e-6) type = SPGPU_MAT_CONDUCTOR;
+        else if (relDiff(ratio, shape(beckmann)) < 1e-6) type = SPGPU_MAT_CONDUCTOR_BECKMANN;
+        else return refuse(why, "rough conductor that is anisotropic or neither Beckmann nor GGX");
+        rec[0] = static_cast<float>(type);
         rec[1] = static_cast<float>(alpha);
         for (int c = 0; c < 3; c++) {
             const double F0 = std::min(0.999, 4.0 * ::PI * alpha * alpha * f0[c]);

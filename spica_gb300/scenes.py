@@ -29,6 +29,7 @@ from typing import Optional
 import numpy as np
 
 MAT_LAMBERT, MAT_CONDUCTOR, MAT_DIELECTRIC, MAT_ROUGH_DIELECTRIC, MAT_PLASTIC = 0, 1, 2, 3, 4
+MAT_CONDUCTOR_BECKMANN = 5
 
 
 @dataclasses.dataclass
@@ -63,6 +64,13 @@ def conductor_f0(alpha, f0):
     f0 = np.minimum(np.asarray(f0, np.float64), 0.999)
     k = 2.0 * np.sqrt(f0 / (1.0 - f0))
     return [MAT_CONDUCTOR, alpha, 1.0, 1.0, 1.0, float(k[0]), float(k[1]), float(k[2])]
+
+
+def conductor(alpha, eta, k, distribution="ggx"):
+    """bsdfs/roughconductor.cc with per-channel eta and k; distribution "ggx" or "beckmann"
+    (the reference's default)."""
+    t = MAT_CONDUCTOR if distribution == "ggx" else MAT_CONDUCTOR_BECKMANN
+    return [t, alpha, *eta, *k]
 
 
 def dielectric(ior):
@@ -241,6 +249,22 @@ def material_room(width=64, height=64, spp=64, max_depth=8, distribution="beckma
     tri_mat = sc.tri_mat.copy()
     tri_mat[10:22] = 3   # tall box
     tri_mat[22:34] = 4   # short box
+    sc.materials = np.array(mats, np.float64)
+    sc.tri_mat = tri_mat
+    return sc
+
+
+def conductor_room(width=64, height=64, spp=64, max_depth=8) -> Scene:
+    """The box room with its tall box a rough conductor of the Beckmann distribution (the
+    reference's default; alpha 0.2, copper-like eta and k) and its short box a GGX
+    conductor (alpha 0.1, gold-like)."""
+    sc = box_room(width=width, height=height, spp=spp, max_depth=max_depth, name="conductor_room")
+    mats = [list(m) for m in sc.materials] + [
+        conductor(0.2, (0.27, 0.68, 1.22), (3.61, 2.63, 2.29), "beckmann"),
+        conductor(0.1, (0.18, 0.42, 1.37), (3.42, 2.35, 1.77), "ggx")]
+    tri_mat = sc.tri_mat.copy()
+    tri_mat[10:22] = len(mats) - 2   # tall box
+    tri_mat[22:34] = len(mats) - 1   # short box
     sc.materials = np.array(mats, np.float64)
     sc.tri_mat = tri_mat
     return sc

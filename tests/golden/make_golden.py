@@ -122,6 +122,7 @@ def main():
     direct_renders(ref)
     film_outputs(ref)
     more_materials(ref)
+    conductors(ref)
     print(f"golden fixtures written in {time.time() - t0:.1f} s")
 
 
@@ -196,21 +197,55 @@ def more_materials(ref):
 MATERIAL_BATCHES = 32
 
 
+def conductors(ref):
+    """9. rough conductors of both distributions (Beckmann is the reference's default):
+    BSDF tables, and a path render of the conductor room with batch moments."""
+    rng = np.random.default_rng(23)
+    n = 2000
+    wo = rng.normal(size=(n, 3))
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    wi = rng.normal(size=(n, 3))
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    wi[: n // 2, 2] = np.abs(wi[: n // 2, 2]) * np.sign(wo[: n // 2, 2])   # half on wo's side
+    u = rng.random((n, 2))
+    mats = np.array([scenes.conductor(0.2, (0.27, 0.68, 1.22), (3.61, 2.63, 2.29), "beckmann"),
+                     scenes.conductor(0.05, (1.1, 0.9, 0.6), (2.0, 2.5, 3.0), "beckmann"),
+                     scenes.conductor(0.6, (0.2, 0.3, 0.4), (4.0, 3.0, 2.0), "beckmann"),
+                     scenes.conductor(0.3, (0.18, 0.42, 1.37), (3.42, 2.35, 1.77), "ggx")], np.float64)
+    out = {"mats": mats, "wo": wo, "wi": wi, "u": u}
+    for k, m in enumerate(mats):
+        f, pdf = ref.bsdf_eval(m, wo, wi)
+        swi, sf, spdf, st = ref.bsdf_sample(m, wo, u)
+        out.update({f"f{k}": f, f"pdf{k}": pdf, f"swi{k}": swi, f"sf{k}": sf, f"spdf{k}": spdf, f"stype{k}": st})
+    np.savez_compressed(os.path.join(HERE, "bsdf_tables_conductor.npz"), **out)
+    sc = scenes.conductor_room(width=48, height=48)
+    S, S2 = ref.scene(sc).render(sc.camera, 48, 48, 1024, 8, seed=31, nthreads=1)
+    bmean, bvar = batch_moments("path", MATERIAL_BATCHES, 1024, seed0=2000, room="conductor")
+    np.savez_compressed(os.path.join(HERE, "render_conductor_room.npz"), sum=S, sumsq=S2, spp=1024, seed=31, W=48,
+                        H=48, max_depth=8, camera=sc.camera, verts=sc.verts, tri_mat=sc.tri_mat,
+                        materials=sc.materials, tri_emit=sc.tri_emit, env=np.zeros((0,), np.float32), bmean=bmean,
+                        bvar=bvar, batches=MATERIAL_BATCHES, batch_spp=1024)
+
+
+def _room(name):
+    return (scenes.conductor_room if name == "conductor" else scenes.material_room)(width=48, height=48)
+
+
 def _material_batch(args):
-    integ, spp, seed = args
-    sc = scenes.material_room(width=48, height=48)
+    integ, spp, seed, room = args
+    sc = _room(room)
     S, _ = spo.Oracle("ref").scene(sc).render(sc.camera, 48, 48, spp, 8, seed=seed, nthreads=1, integrator=integ)
     return S / spp
 
 
-def batch_moments(integ, batches, spp, seed0):
+def batch_moments(integ, batches, spp, seed0, room="material"):
     """Per-pixel mean and variance of the mean over independent batches (seeds seed0..).
     Light refracted through the glass box reaches the walls along rare bright paths; the
     per-sample variance of a 1024-sample render under-reads that tail, so the 3-sigma
     comparison uses the spread of batch means instead."""
     import multiprocessing as mp
     with mp.get_context("spawn").Pool(min(batches, os.cpu_count() or 1)) as pool:
-        m = np.stack(pool.map(_material_batch, [(integ, spp, seed0 + k) for k in range(batches)]))
+        m = np.stack(pool.map(_material_batch, [(integ, spp, seed0 + k, room) for k in range(batches)]))
     return m.mean(0), m.var(0, ddof=1) / batches
 
 

@@ -72,11 +72,13 @@ def test_bsdf_tables_match_reference_golden(port):
         assert np.array_equal(st, g[f"stype{k}"])
 
 
-def test_more_bsdf_tables_match_reference_golden(port):
+@pytest.mark.parametrize("fixture", ["bsdf_tables_more.npz", "bsdf_tables_conductor.npz"])
+def test_more_bsdf_tables_match_reference_golden(port, fixture):
     """Rough dielectric (Beckmann, GGX) and plastic, including the draws the reference
     takes from its BxDFs' hidden generators (sampling runs in a fresh thread on both
-    sides, where those generators start from their seed)."""
-    g = np.load(os.path.join(GOLDEN, "bsdf_tables_more.npz"))
+    sides, where those generators start from their seed); rough conductors of both
+    distributions."""
+    g = np.load(os.path.join(GOLDEN, fixture))
     for k, m in enumerate(g["mats"]):
         f, pdf = port.bsdf_eval(m, g["wo"], g["wi"])
         np.testing.assert_allclose(f, g[f"f{k}"], rtol=1e-12, atol=1e-14)
@@ -91,7 +93,7 @@ def test_more_bsdf_tables_match_reference_golden(port):
 
 @pytest.mark.parametrize("name", ["render_boxroom", "render_envscene", "render_direct_boxroom",
                                   "render_direct_envscene", "render_material_room",
-                                  "render_direct_material_room"])
+                                  "render_direct_material_room", "render_conductor_room"])
 def test_render_matches_reference_golden(port, name):
     """Same per-pixel sampler streams => the restatement reproduces the reference's
     per-pixel sums (exactly on the host that made the fixture; libm differences in
@@ -103,6 +105,8 @@ def test_render_matches_reference_golden(port, name):
     nthreads = 1 if "material" in name else None
     if "material_room" in name:
         sc = scenes.material_room(width=int(g["W"]), height=int(g["H"]))
+    elif "conductor_room" in name:
+        sc = scenes.conductor_room(width=int(g["W"]), height=int(g["H"]))
     elif "boxroom" in name:
         sc = scenes.box_room(width=int(g["W"]), height=int(g["H"]))
     else:

@@ -14,6 +14,7 @@ from spica_gb300 import scenes
 CASES = {
     "lambert": scenes.lambert(0.3, 0.5, 0.7),
     "conductor": scenes.conductor_f0(0.2, (0.9, 0.6, 0.3)),
+    "conductor_beckmann": [scenes.MAT_CONDUCTOR_BECKMANN] + scenes.conductor_f0(0.15, (0.5, 0.7, 0.95))[1:],
     "dielectric": scenes.dielectric(1.5),
     "beckmann": scenes.rough_dielectric(0.25, 1.5, "beckmann"),
     "ggx": scenes.rough_dielectric(0.15, 1.33, "ggx"),

@@ -51,13 +51,15 @@ def ref_moments(g):
 
 @pytest.mark.parametrize("name", ["render_boxroom", "render_envscene", "render_direct_boxroom",
                                   "render_direct_envscene", "render_material_room",
-                                  "render_direct_material_room"])
+                                  "render_direct_material_room", "render_conductor_room"])
 def test_matches_reference_render(gpulib, name):
     """Path integrator and direct-lighting integrator against the reference's renders."""
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     W, H, md = int(g["W"]), int(g["H"]), int(g["max_depth"])
     if "material_room" in name:   # rough dielectric and plastic boxes
         sc = scenes.material_room(width=W, height=H)
+    elif "conductor_room" in name:   # Beckmann and GGX rough conductor boxes
+        sc = scenes.conductor_room(width=W, height=H)
     else:
         sc = scenes.box_room(width=W, height=H) if "boxroom" in name else _scene_from(g)
     acc = GpuBVHAccel(sc).construct()

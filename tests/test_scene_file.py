@@ -220,6 +220,26 @@ def test_parameter_store_rules(tmp_path):
     assert (got.width, got.height, got.max_depth, got.spp) == (8, 6, 5, 4)
 
 
+def test_rough_conductors(tmp_path):
+    """roughconductor: Beckmann by default (bsdfs/roughconductor.cc:34), GGX on request;
+    alpha defaults to 0.1 and is read without removal, so it persists to the next one."""
+    write_ply(tmp_path / "t.ply", [[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 2]])
+    shapes = """
+<shape type="ply"><string name="filename" value="t.ply"/>
+  <bsdf type="roughconductor"><rgb name="eta" value="0.2 0.3 0.4"/><rgb name="k" value="3 2 1"/></bsdf></shape>
+<shape type="ply"><string name="filename" value="t.ply"/>
+  <bsdf type="roughconductor"><float name="alpha" value="0.25"/><string name="distribution" value="ggx"/>
+    <rgb name="eta" value="1 1 1"/><rgb name="k" value="2 2 2"/></bsdf></shape>
+<shape type="ply"><string name="filename" value="t.ply"/>
+  <bsdf type="roughconductor"><rgb name="eta" value="1 1 1"/><rgb name="k" value="2 2 2"/></bsdf></shape>"""
+    (tmp_path / "s.xml").write_text(_minimal(shapes))
+    got, _ = load_scene(tmp_path / "s.xml")
+    M = got.materials[got.tri_mat]
+    np.testing.assert_allclose(M[0], [scenes.MAT_CONDUCTOR_BECKMANN, 0.1, 0.2, 0.3, 0.4, 3, 2, 1], rtol=1e-6)
+    np.testing.assert_allclose(M[1], [scenes.MAT_CONDUCTOR, 0.25, 1, 1, 1, 2, 2, 2], rtol=1e-6)
+    np.testing.assert_allclose(M[2], [scenes.MAT_CONDUCTOR_BECKMANN, 0.25, 1, 1, 1, 2, 2, 2], rtol=1e-6)
+
+
 def test_obj_meshes(tmp_path):
     """OBJ: positions with /texcoord/normal parts ignored, negative (relative) indices,
     polygons as fans around their first vertex."""
@@ -234,8 +254,9 @@ def test_obj_meshes(tmp_path):
 @pytest.mark.parametrize("snippet, message", [
     ('<bsdf type="conductor" id="c"/><shape type="ply"><string name="filename" value="t.ply"/></shape>',
      "no GPU counterpart"),
-    ('<bsdf type="roughconductor"><rgb name="eta" value="1 1 1"/><rgb name="k" value="2 2 2"/></bsdf>'
-     '<shape type="ply"><string name="filename" value="t.ply"/></shape>', "ggx"),
+    ('<bsdf type="roughconductor"><rgb name="eta" value="1 1 1"/><rgb name="k" value="2 2 2"/>'
+     '<string name="distribution" value="phong"/></bsdf>'
+     '<shape type="ply"><string name="filename" value="t.ply"/></shape>', "unknown distribution"),
     ('<shape type="sphere"><float name="radius" value="1"/></shape>', "not created by the reference"),
     ('<shape type="ply"><string name="filename" value="missing.ply"/></shape>', "cannot open"),
     ('<medium type="homogeneous"/>', "not supported"),
