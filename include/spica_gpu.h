@@ -275,10 +275,18 @@ int spgpu_guiding_grad(spgpu_ctx *ctx, const float *samples, int32_t n, float *g
  *                           core/tmo.cc:53, core/image.cc:476)
  *   SPGPU_FILM_REINHARD     out = W*H*3 floats: ReinhardTmo(param = alpha)::apply of the
  *                           resolved image (core/tmo.cc:81-124)
+ *   SPGPU_FILM_DRAGO        out = W*H*3 floats: DragoTmo(Ldmax = 100, param = p)::apply
+ *                           (core/tmo.cc:125-159)
+ *   SPGPU_FILM_DURAND       out = W*H*3 floats: DurandTMO(sigmaSpace = 0.02, sigmaColor =
+ *                           0.4, param = targetContrast)::apply (core/tmo.cc:161-243) with
+ *                           the reference's domain-transform bilateral filter
+ *                           (core/birateral.cc, 20 iterations)
  * Blocking on `stream`. */
 #define SPGPU_FILM_RGBE 0
 #define SPGPU_FILM_GAMMA_BYTES 1
 #define SPGPU_FILM_REINHARD 2
+#define SPGPU_FILM_DRAGO 3
+#define SPGPU_FILM_DURAND 4
 int spgpu_film_resolve(spgpu_ctx *ctx, const float *film, int32_t width, int32_t height, int32_t format,
                        double param, void *out, void *stream);
 /* Host-side writers.  spgpu_write_hdr writes W*H RGBE pixels in the byte layout of the

@@ -466,8 +466,8 @@ int spo_film_gamma(const float *film, int W, int H, double gamma, uint8_t *out) 
     return 0;
 }
 
-int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out) {
-    const Image r = ReinhardTmo(alpha).apply(resolveFilm(film, W, H));
+namespace {
+void copyImage(const Image &r, int W, int H, double *out) {
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             const RGBSpectrum &c = r(x, y);
@@ -476,6 +476,21 @@ int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out
             o[1] = c.green();
             o[2] = c.blue();
         }
+}
+}  // namespace
+
+int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out) {
+    copyImage(ReinhardTmo(alpha).apply(resolveFilm(film, W, H)), W, H, out);
+    return 0;
+}
+
+int spo_film_drago(const float *film, int W, int H, double p, double *out) {
+    copyImage(DragoTmo(100.0, p).apply(resolveFilm(film, W, H)), W, H, out);
+    return 0;
+}
+
+int spo_film_durand(const float *film, int W, int H, double contrast, double *out) {
+    copyImage(DurandTMO(0.02, 0.4, contrast).apply(resolveFilm(film, W, H)), W, H, out);
     return 0;
 }
 }  // extern "C"

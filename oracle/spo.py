@@ -170,6 +170,21 @@ class Oracle:
         return out
 
 
+    def film_drago(self, film, p):
+        film, W, H = self._film(film)
+        out = np.zeros((H, W, 3), np.float64)
+        self.lib.spo_film_drago.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p]
+        self.lib.spo_film_drago(film.ctypes.data, W, H, p, out.ctypes.data)
+        return out
+
+    def film_durand(self, film, contrast):
+        film, W, H = self._film(film)
+        out = np.zeros((H, W, 3), np.float64)
+        self.lib.spo_film_durand.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p]
+        self.lib.spo_film_durand(film.ctypes.data, W, H, contrast, out.ctypes.data)
+        return out
+
+
 class OracleScene:
     """A scene held by one oracle library (see spica_gb300.scenes.Scene for the layout)."""
 

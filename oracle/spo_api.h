@@ -83,6 +83,10 @@ const char *spo_name(void);
 int spo_film_save_hdr(const float *film, int W, int H, const char *path);
 int spo_film_gamma(const float *film, int W, int H, double gamma, uint8_t *out);
 int spo_film_reinhard(const float *film, int W, int H, double alpha, double *out);
+/* DragoTmo(Ldmax 100, bias p)::apply and DurandTMO(sigmaSpace 0.02, sigmaColor 0.4,
+ * targetContrast)::apply of the resolved film (core/tmo.cc:135, 171): W*H*3 doubles */
+int spo_film_drago(const float *film, int W, int H, double p, double *out);
+int spo_film_durand(const float *film, int W, int H, double contrast, double *out);
 
 /* The drop-in integrator plugin's material translation (spica_gb300/plugins/
  * material_probe.h) run on the reference's own BSDF for a material record (compiled

@@ -1024,7 +1024,7 @@ int spgpu_film_resolve(spgpu_ctx *h, const float *film, int32_t width, int32_t h
                        double param, void *out, void *stream) {
     NvtxRange nvtxRange("spgpu_film_resolve");
     if (!h || !film || !out || width <= 0 || height <= 0 || static_cast<int64_t>(width) * height > (int64_t(1) << 28) ||
-        format < SPGPU_FILM_RGBE || format > SPGPU_FILM_REINHARD ||
+        format < SPGPU_FILM_RGBE || format > SPGPU_FILM_DURAND ||
         (format != SPGPU_FILM_RGBE && !(param > 0.0)) || (reinterpret_cast<uintptr_t>(film) & 15) ||
         (format != SPGPU_FILM_GAMMA_BYTES && (reinterpret_cast<uintptr_t>(out) & 3))) {
         setError("spgpu_film_resolve: invalid arguments (16-byte aligned film, 4-byte aligned RGBE or float "

@@ -77,13 +77,13 @@ class GuidingConfig(C.Structure):
 
 
 GUIDE_GUIDED, GUIDE_COLLECT, GUIDE_MEGAKERNEL = 1, 2, 4
-FILM_RGBE, FILM_GAMMA_BYTES, FILM_REINHARD = 0, 1, 2
+FILM_RGBE, FILM_GAMMA_BYTES, FILM_REINHARD, FILM_DRAGO, FILM_DURAND = 0, 1, 2, 3, 4
 
 
 def film_resolve(ctx: "Context", film_dev, fmt: int, param: float = 0.0, stream: int = 0):
     """spgpu_film_resolve of a device film (torch (H, W, 4) float32): RGBE bytes (H, W, 4),
-    gamma-corrected bytes (H, W, 3) or a Reinhard-mapped image (H, W, 3) float32, on the
-    device."""
+    gamma-corrected bytes (H, W, 3), or a Reinhard-, Drago- or Durand-mapped image
+    (H, W, 3) float32, on the device."""
     import torch
     H, W = int(film_dev.shape[0]), int(film_dev.shape[1])
     if fmt == FILM_RGBE:

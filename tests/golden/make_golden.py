@@ -161,7 +161,8 @@ def film_outputs(ref):
         ref.film_save_hdr(film, path)
         hdr = np.frombuffer(open(path, "rb").read(), np.uint8)
     np.savez_compressed(os.path.join(HERE, "film_output.npz"), film=film, hdr=hdr,
-                        gamma22=ref.film_gamma(film, 2.2), reinhard=ref.film_reinhard(film, 0.18))
+                        gamma22=ref.film_gamma(film, 2.2), reinhard=ref.film_reinhard(film, 0.18),
+                        drago=ref.film_drago(film, 0.85), durand=ref.film_durand(film, 5.0))
 
 
 def more_materials(ref):

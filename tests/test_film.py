@@ -86,3 +86,16 @@ def test_png_writer_round_trip(tmp_path):
     raw = np.frombuffer(zlib.decompress(chunks[b"IDAT"]), np.uint8).reshape(H, 3 * W + 1)
     assert not raw[:, 0].any()
     np.testing.assert_array_equal(raw[:, 1:].reshape(img.shape), img)
+
+
+def test_tone_mapping_restatement_matches_reference():
+    """The numpy restatement of ReinhardTmo, DragoTmo and DurandTMO (oracle/tmo_oracle.py),
+    which checks the device operators, against the compiled reference's images."""
+    from oracle import tmo_oracle
+    g = np.load(os.path.join(GOLDEN, "film_output.npz"))
+    np.testing.assert_allclose(tmo_oracle.reinhard(g["film"], 0.18), g["reinhard"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(tmo_oracle.drago(g["film"], 0.85), g["drago"], rtol=1e-13, atol=0)
+    durand = tmo_oracle.durand(g["film"], 5.0)
+    np.testing.assert_allclose(durand, g["durand"], rtol=1e-13, atol=1e-15)
+    inside = (g["durand"] > 0) & (g["durand"] < 1)
+    assert inside.mean() > 0.5   # the image is mostly not clipped: the comparison means something

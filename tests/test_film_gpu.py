@@ -1,6 +1,6 @@
 """Film output on the device (spgpu_film_resolve) against the compiled reference's
 outputs for the same float film (tests/golden/film_output.npz): the .hdr file byte for
-byte, LDRFilm's gamma-2.2 bytes, ReinhardTmo's image."""
+byte, LDRFilm's gamma-2.2 bytes, the images of ReinhardTmo, DragoTmo and DurandTMO."""
 import os
 
 import numpy as np
@@ -47,6 +47,43 @@ def test_reinhard_matches_reference(gpulib):
     out = gpu.film_resolve(ctx, _dev(g["film"]), gpu.FILM_REINHARD, 0.18).cpu().numpy()
     # float output of FP64 arithmetic; the log-mean is summed in a different order
     np.testing.assert_allclose(out, g["reinhard"], rtol=2e-6, atol=1e-30)
+
+
+def test_drago_matches_reference(gpulib):
+    from spica_gb300 import gpu
+    g = np.load(os.path.join(GOLDEN, "film_output.npz"))
+    ctx = gpu.Context(0)
+    out = gpu.film_resolve(ctx, _dev(g["film"]), gpu.FILM_DRAGO, 0.85).cpu().numpy()
+    # float output of FP64 arithmetic; the log-mean is summed in a different order
+    np.testing.assert_allclose(out, g["drago"], rtol=2e-6, atol=1e-30)
+
+
+def test_durand_matches_reference(gpulib):
+    from spica_gb300 import gpu
+    g = np.load(os.path.join(GOLDEN, "film_output.npz"))
+    ctx = gpu.Context(0)
+    out = gpu.film_resolve(ctx, _dev(g["film"]), gpu.FILM_DURAND, 5.0).cpu().numpy()
+    # float output of FP64 arithmetic (device pow / log10 may differ from the host libm in
+    # the last ulp), clamped to [0, 1] as the reference clamps
+    np.testing.assert_allclose(out, g["durand"], rtol=2e-6, atol=1e-12)
+
+
+def test_durand_on_a_rendered_film_matches_restatement(gpulib):
+    """A larger film (a box-room render, 320 x 200) through the device Durand operator
+    against the numpy restatement of the reference's operator."""
+    import torch
+    from oracle import tmo_oracle
+    from spica_gb300 import GpuBVHAccel, GpuPathIntegrator, gpu, scenes
+    sc = scenes.box_room(width=320, height=200)
+    acc = GpuBVHAccel(sc).construct()
+    film = torch.zeros((200, 320, 4), dtype=torch.float32, device="cuda")
+    GpuPathIntegrator(seed=3).render_device(sc.camera, acc, {"width": 320, "height": 200, "maxDepth": 6,
+                                                              "sampleCount": 4}, film)
+    out = gpu.film_resolve(acc.ctx, film, gpu.FILM_DURAND, 8.0).cpu().numpy()
+    ref = tmo_oracle.durand(film.cpu().numpy(), 8.0)
+    np.testing.assert_allclose(out, ref, rtol=2e-6, atol=1e-12)
+    dr = gpu.film_resolve(acc.ctx, film, gpu.FILM_DRAGO, 0.7).cpu().numpy()
+    np.testing.assert_allclose(dr, tmo_oracle.drago(film.cpu().numpy(), 0.7), rtol=2e-6, atol=1e-30)
 
 
 def test_rendered_film_to_files(gpulib, tmp_path):
