@@ -30,10 +30,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <fstream>
 #include <iterator>
 #include <map>
 #include <memory>
+#include <new>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -411,6 +413,16 @@ bool loadPly(const std::string &path, const Mat4 &toWorld, std::vector<float> *t
         *why = path + ": vertex and face counts must be positive";
         return false;
     }
+    // the body holds 12 bytes per vertex and at least 13 per face: refuse counts that the
+    // file cannot hold before allocating for them
+    const std::streamoff body = f.tellg();
+    f.seekg(0, std::ios::end);
+    const std::streamoff avail = f.tellg() - body;
+    f.seekg(body);
+    if (body < 0 || nv > avail / 12 || nf > (avail - 12 * nv) / 13) {
+        *why = path + ": truncated vertex data or face data (the header's counts exceed the file)";
+        return false;
+    }
     std::vector<double> v(3 * nv);
     for (long i = 0; i < nv; i++) {
         unsigned char b[12];
@@ -535,6 +547,10 @@ bool loadHdr(const std::string &path, std::vector<float> *rgb, int *W, int *H, s
     if (std::sscanf(line.c_str(), "%16s %d %16s %d", by, &h, bx, &w) != 4 || std::strcmp(by, "-Y") != 0 ||
         std::strcmp(bx, "+X") != 0 || w <= 0 || h <= 0) {
         *why = path + ": unsupported HDR size line";
+        return false;
+    }
+    if (w > 0x7FFF || static_cast<int64_t>(w) * h > (int64_t(1) << 28)) {   // RLE widths are 15-bit
+        *why = path + ": image too large (width < 32768, at most 2^28 pixels)";
         return false;
     }
     std::vector<unsigned char> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
@@ -917,7 +933,23 @@ private:
 extern "C" {
 
 
+static int sceneLoad(const char *path, spgpu_scene_file **out);
+
+// No C++ exception leaves the C ABI: an allocation failure or any other exception becomes
+// a status and a message.
 int spgpu_scene_load(const char *path, spgpu_scene_file **out) {
+    try {
+        return sceneLoad(path, out);
+    } catch (const std::bad_alloc &) {
+        setError("spgpu_scene_load: out of host memory");
+        return SPGPU_ENOMEM;
+    } catch (const std::exception &e) {
+        setError(std::string("spgpu_scene_load: ") + e.what());
+        return SPGPU_EINVAL;
+    }
+}
+
+static int sceneLoad(const char *path, spgpu_scene_file **out) {
     if (!path || !out) {
         setError("spgpu_scene_load: invalid arguments");
         return SPGPU_EINVAL;
@@ -1006,7 +1038,14 @@ int spgpu_load_hdr(const char *path, float *rgb, int32_t max_pixels, int32_t *wi
     std::vector<float> px;
     int w = 0, h = 0;
     std::string why;
-    if (!loadHdr(path, &px, &w, &h, &why)) {
+    bool ok;
+    try {
+        ok = loadHdr(path, &px, &w, &h, &why);
+    } catch (const std::bad_alloc &) {
+        setError("spgpu_load_hdr: out of host memory");
+        return SPGPU_ENOMEM;
+    }
+    if (!ok) {
         setError("spgpu_load_hdr: " + why);
         return SPGPU_EINVAL;
     }

@@ -274,3 +274,20 @@ def test_missing_sample_count_is_refused(tmp_path):
     (tmp_path / "s.xml").write_text(xml)
     with pytest.raises(SpgpuError, match="sampleCount"):
         load_scene(tmp_path / "s.xml")
+
+
+def test_headers_that_overstate_the_data_are_refused(tmp_path):
+    """A PLY header whose counts the file cannot hold, and an .hdr size line beyond what
+    the format encodes, are refused with a message before anything is allocated for
+    them (no exception or abort crosses the C ABI)."""
+    write_ply(tmp_path / "t.ply", [[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 2]])
+    data = (tmp_path / "t.ply").read_bytes()
+    (tmp_path / "big.ply").write_bytes(data.replace(b"element vertex 3", b"element vertex 1000000000000"))
+    (tmp_path / "faces.ply").write_bytes(data.replace(b"element face 1", b"element face 2"))
+    for name in ("big.ply", "faces.ply"):
+        (tmp_path / "s.xml").write_text(_minimal(f'<shape type="ply"><string name="filename" value="{name}"/></shape>'))
+        with pytest.raises(SpgpuError, match="exceed the file"):
+            load_scene(tmp_path / "s.xml")
+    (tmp_path / "huge.hdr").write_bytes(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 2000000000 +X 30000\n")
+    with pytest.raises(SpgpuError, match="too large"):
+        load_hdr(tmp_path / "huge.hdr")
