@@ -5,7 +5,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <mutex>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -335,6 +337,22 @@ int noallocScratch(int device, unsigned char **base) {
 
 void setError(const std::string &msg) { g_lastError = msg; }
 
+// Runs the body of a C entry point so that no C++ exception crosses the C ABI: a failed
+// host allocation becomes SPGPU_ENOMEM, any other exception SPGPU_EINVAL, each with a
+// message.
+template <class F>
+int guarded(const char *name, F &&body) noexcept {
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        setError(std::string(name) + ": out of host memory");
+        return SPGPU_ENOMEM;
+    } catch (const std::exception &e) {
+        setError(std::string(name) + ": " + e.what());
+        return SPGPU_EINVAL;
+    }
+}
+
 int cudaFail(const char *what, cudaError_t e) {
     g_lastError = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? SPGPU_ENOMEM : SPGPU_ECUDA;
@@ -462,36 +480,38 @@ const char *spgpu_last_error(void) { return g_lastError.c_str(); }
 const char *spgpu_version(void) { return "spica-gb300 0.1 (sm_103a)"; }
 
 int spgpu_create(const spgpu_config *cfg, spgpu_ctx **out) {
-    if (!out) {
-        setError("spgpu_create: null output pointer");
-        return SPGPU_EINVAL;
-    }
-    *out = nullptr;
-    auto *h = new spgpu_ctx();
-    Ctx &C = h->c;
-    C.device = cfg ? cfg->device : 0;
-    if (cfg && (cfg->pass_lanes < 0 || cfg->pass_lanes > Ctx::kPassLanes)) {
-        setError("spgpu_create: pass_lanes must be 0 (default) or 1.." + std::to_string(Ctx::kPassLanes));
-        delete h;
-        return SPGPU_EINVAL;
-    }
-    C.passLanes = cfg && cfg->pass_lanes > 0 ? cfg->pass_lanes : Ctx::kPassLanes;
-    cudaError_t e = cudaSetDevice(C.device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking);
-    for (int k = 0; k < Ctx::kPassLanes - 1 && e == cudaSuccess; k++) {
-        e = cudaStreamCreateWithFlags(&C.laneStream[k], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&C.laneJoin[k], cudaEventDisableTiming);
-    }
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&C.laneFork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMalloc(&C.traceErr, 4 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&C.traceStats, 4 * sizeof(unsigned long long));
-    if (e != cudaSuccess) {
-        const int rc = cudaFail("spgpu_create", e);
-        delete h;
-        return rc;
-    }
-    *out = h;
-    return 0;
+    return guarded("spgpu_create", [&]() -> int {
+        if (!out) {
+            setError("spgpu_create: null output pointer");
+            return SPGPU_EINVAL;
+        }
+        *out = nullptr;
+        auto *h = new spgpu_ctx();
+        Ctx &C = h->c;
+        C.device = cfg ? cfg->device : 0;
+        if (cfg && (cfg->pass_lanes < 0 || cfg->pass_lanes > Ctx::kPassLanes)) {
+            setError("spgpu_create: pass_lanes must be 0 (default) or 1.." + std::to_string(Ctx::kPassLanes));
+            delete h;
+            return SPGPU_EINVAL;
+        }
+        C.passLanes = cfg && cfg->pass_lanes > 0 ? cfg->pass_lanes : Ctx::kPassLanes;
+        cudaError_t e = cudaSetDevice(C.device);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking);
+        for (int k = 0; k < Ctx::kPassLanes - 1 && e == cudaSuccess; k++) {
+            e = cudaStreamCreateWithFlags(&C.laneStream[k], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&C.laneJoin[k], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&C.laneFork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMalloc(&C.traceErr, 4 * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc(&C.traceStats, 4 * sizeof(unsigned long long));
+        if (e != cudaSuccess) {
+            const int rc = cudaFail("spgpu_create", e);
+            delete h;
+            return rc;
+        }
+        *out = h;
+        return 0;
+    });
 }
 
 void spgpu_destroy(spgpu_ctx *h) {
@@ -519,157 +539,164 @@ void spgpu_destroy(spgpu_ctx *h) {
 
 int spgpu_upload_scene(spgpu_ctx *h, int32_t ntri, const float *verts, const int32_t *tri_mat, int32_t nmat,
                        const float *materials, const float *tri_emit, int32_t env_w, int32_t env_h, const float *env) {
-    NvtxRange nvtxRange("spgpu_upload_scene");
-    if (!h || ntri <= 0 || !verts || !tri_mat || nmat <= 0 || !materials || (env && (env_w <= 0 || env_h <= 0))) {
-        setError("spgpu_upload_scene: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    Ctx &C = h->c;
-    cudaSetDevice(C.device);
-    freeScene(C);
-    for (int i = 0; i < ntri; i++) {
-        if (tri_mat[i] < 0 || tri_mat[i] >= nmat) {
-            setError("spgpu_upload_scene: triangle material index out of range");
+    return guarded("spgpu_upload_scene", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_upload_scene");
+        if (!h || ntri <= 0 || !verts || !tri_mat || nmat <= 0 || !materials || (env && (env_w <= 0 || env_h <= 0))) {
+            setError("spgpu_upload_scene: invalid arguments");
             return SPGPU_EINVAL;
         }
-    }
-    // materials: the plugins read alpha and IOR through Spectrum::gray() of a constant
-    // texture (roughconductor.cc:48, dielectric.cc:33), kept here for the same value
-    auto gray1 = [](double v) { return 0.2126 * v + 0.7152 * v + 0.0722 * v; };
-    std::vector<MaterialRecord> mats(nmat);
-    for (int m = 0; m < nmat; m++) {
-        const float *r = materials + 8 * m;
-        MaterialRecord &M = mats[m];
-        std::memset(&M, 0, sizeof(M));
-        M.type = static_cast<int>(r[0]);
-        const bool beckmannConductor = M.type == SPGPU_MAT_CONDUCTOR_BECKMANN;
-        if (beckmannConductor) M.type = kMatConductor;
-        if (M.type == kMatLambert) {
-            M.a = make_float4(fmaxf(r[1], 0.0f), fmaxf(r[2], 0.0f), fmaxf(r[3], 0.0f), 0.0f);
-        } else if (M.type == kMatConductor) {
-            M.a = make_float4(r[2], r[3], r[4], static_cast<float>(gray1(r[1])));
-            M.b = make_float4(r[5], r[6], r[7], beckmannConductor ? 1.0f : 0.0f);   // b.w: distribution
-            if (!(M.a.w > 0.0f)) {
-                setError("spgpu_upload_scene: conductor roughness must be positive (smooth conductors are not supported)");
+        Ctx &C = h->c;
+        cudaSetDevice(C.device);
+        freeScene(C);
+        for (int i = 0; i < ntri; i++) {
+            if (tri_mat[i] < 0 || tri_mat[i] >= nmat) {
+                setError("spgpu_upload_scene: triangle material index out of range");
                 return SPGPU_EINVAL;
             }
-        } else if (M.type == kMatDielectric) {
-            M.a = make_float4(0.0f, 0.0f, 0.0f, static_cast<float>(gray1(r[1])));
-        } else if (M.type == kMatRoughDielectric) {
-            // roughdielectric.cc:41-84: zero roughness is the smooth dielectric's FresnelSpecular
-            const float alpha = static_cast<float>(gray1(r[1])), ior = static_cast<float>(gray1(r[2]));
-            if (alpha == 0.0f) {
-                M.type = kMatDielectric;
-                M.a = make_float4(0.0f, 0.0f, 0.0f, ior);
-            } else if (!(alpha > 0.0f) || !(ior > 0.0f) || (r[3] != 0.0f && r[3] != 1.0f)) {
-                setError("spgpu_upload_scene: rough dielectric needs alpha >= 0, ior > 0, distribution 0 or 1");
-                return SPGPU_EINVAL;
+        }
+        // materials: the plugins read alpha and IOR through Spectrum::gray() of a constant
+        // texture (roughconductor.cc:48, dielectric.cc:33), kept here for the same value
+        auto gray1 = [](double v) { return 0.2126 * v + 0.7152 * v + 0.0722 * v; };
+        std::vector<MaterialRecord> mats(nmat);
+        for (int m = 0; m < nmat; m++) {
+            const float *r = materials + 8 * m;
+            MaterialRecord &M = mats[m];
+            std::memset(&M, 0, sizeof(M));
+            M.type = static_cast<int>(r[0]);
+            const bool beckmannConductor = M.type == SPGPU_MAT_CONDUCTOR_BECKMANN;
+            if (beckmannConductor) M.type = kMatConductor;
+            if (M.type == kMatLambert) {
+                M.a = make_float4(fmaxf(r[1], 0.0f), fmaxf(r[2], 0.0f), fmaxf(r[3], 0.0f), 0.0f);
+            } else if (M.type == kMatConductor) {
+                M.a = make_float4(r[2], r[3], r[4], static_cast<float>(gray1(r[1])));
+                M.b = make_float4(r[5], r[6], r[7], beckmannConductor ? 1.0f : 0.0f);   // b.w: distribution
+                if (!(M.a.w > 0.0f)) {
+                    setError("spgpu_upload_scene: conductor roughness must be positive (smooth conductors are not "
+                             "supported)");
+                    return SPGPU_EINVAL;
+                }
+            } else if (M.type == kMatDielectric) {
+                M.a = make_float4(0.0f, 0.0f, 0.0f, static_cast<float>(gray1(r[1])));
+            } else if (M.type == kMatRoughDielectric) {
+                // roughdielectric.cc:41-84: zero roughness is the smooth dielectric's FresnelSpecular
+                const float alpha = static_cast<float>(gray1(r[1])), ior = static_cast<float>(gray1(r[2]));
+                if (alpha == 0.0f) {
+                    M.type = kMatDielectric;
+                    M.a = make_float4(0.0f, 0.0f, 0.0f, ior);
+                } else if (!(alpha > 0.0f) || !(ior > 0.0f) || (r[3] != 0.0f && r[3] != 1.0f)) {
+                    setError("spgpu_upload_scene: rough dielectric needs alpha >= 0, ior > 0, distribution 0 or 1");
+                    return SPGPU_EINVAL;
+                } else {
+                    M.a = make_float4(alpha, ior, r[3], 0.0f);
+                }
+            } else if (M.type == kMatPlastic) {
+                // plastic.cc:112-122 and PlasticBRDF's specular sampling weight (plastic.cc:26)
+                const double kd = 0.2126 * r[1] + 0.7152 * r[2] + 0.0722 * r[3];
+                const double ks = 0.2126 * r[4] + 0.7152 * r[5] + 0.0722 * r[6];
+                const float ior = static_cast<float>(gray1(r[7]));
+                if (!(ior > 0.0f) || !(kd + ks > 0.0)) {
+                    setError("spgpu_upload_scene: plastic needs ior > 0 and a non-black Kd + Ks");
+                    return SPGPU_EINVAL;
+                }
+                M.a = make_float4(r[1], r[2], r[3], ior);
+                M.b = make_float4(r[4], r[5], r[6], static_cast<float>(ks / (kd + ks)));
             } else {
-                M.a = make_float4(alpha, ior, r[3], 0.0f);
-            }
-        } else if (M.type == kMatPlastic) {
-            // plastic.cc:112-122 and PlasticBRDF's specular sampling weight (plastic.cc:26)
-            const double kd = 0.2126 * r[1] + 0.7152 * r[2] + 0.0722 * r[3];
-            const double ks = 0.2126 * r[4] + 0.7152 * r[5] + 0.0722 * r[6];
-            const float ior = static_cast<float>(gray1(r[7]));
-            if (!(ior > 0.0f) || !(kd + ks > 0.0)) {
-                setError("spgpu_upload_scene: plastic needs ior > 0 and a non-black Kd + Ks");
+                setError("spgpu_upload_scene: unknown material type");
                 return SPGPU_EINVAL;
             }
-            M.a = make_float4(r[1], r[2], r[3], ior);
-            M.b = make_float4(r[4], r[5], r[6], static_cast<float>(ks / (kd + ks)));
-        } else {
-            setError("spgpu_upload_scene: unknown material type");
-            return SPGPU_EINVAL;
         }
-    }
-    // area lights: one per emitting triangle, in triangle order (sceneparser.cc:173-179)
-    std::vector<LightRecord> lights;
-    std::vector<int> triLight(ntri, -1);
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int i = 0; i < ntri; i++) {
-        const float *v = verts + 9 * static_cast<int64_t>(i);
-        for (int k = 0; k < 3; k++)
-            for (int a = 0; a < 3; a++) {
-                lo[a] = std::min(lo[a], static_cast<double>(v[3 * k + a]));
-                hi[a] = std::max(hi[a], static_cast<double>(v[3 * k + a]));
+        // area lights: one per emitting triangle, in triangle order (sceneparser.cc:173-179)
+        std::vector<LightRecord> lights;
+        std::vector<int> triLight(ntri, -1);
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int i = 0; i < ntri; i++) {
+            const float *v = verts + 9 * static_cast<int64_t>(i);
+            for (int k = 0; k < 3; k++)
+                for (int a = 0; a < 3; a++) {
+                    lo[a] = std::min(lo[a], static_cast<double>(v[3 * k + a]));
+                    hi[a] = std::max(hi[a], static_cast<double>(v[3 * k + a]));
+                }
+            if (!tri_emit) continue;
+            const float *e = tri_emit + 3 * static_cast<int64_t>(i);
+            if (e[0] == 0.0f && e[1] == 0.0f && e[2] == 0.0f) continue;
+            const double e1[3] = {static_cast<double>(v[3]) - v[0], static_cast<double>(v[4]) - v[1],
+                                  static_cast<double>(v[5]) - v[2]};
+            const double e2[3] = {static_cast<double>(v[6]) - v[0], static_cast<double>(v[7]) - v[1],
+                                  static_cast<double>(v[8]) - v[2]};
+            const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                 e1[0] * e2[1] - e1[1] * e2[0]};
+            const double len = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+            if (!(len > 0.0)) {
+                setError("spgpu_upload_scene: degenerate emitting triangle");
+                return SPGPU_EINVAL;
             }
-        if (!tri_emit) continue;
-        const float *e = tri_emit + 3 * static_cast<int64_t>(i);
-        if (e[0] == 0.0f && e[1] == 0.0f && e[2] == 0.0f) continue;
-        const double e1[3] = {static_cast<double>(v[3]) - v[0], static_cast<double>(v[4]) - v[1],
-                              static_cast<double>(v[5]) - v[2]};
-        const double e2[3] = {static_cast<double>(v[6]) - v[0], static_cast<double>(v[7]) - v[1],
-                              static_cast<double>(v[8]) - v[2]};
-        const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
-                             e1[0] * e2[1] - e1[1] * e2[0]};
-        const double len = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-        if (!(len > 0.0)) {
-            setError("spgpu_upload_scene: degenerate emitting triangle");
-            return SPGPU_EINVAL;
+            LightRecord L;
+            L.p0 = make_float4(v[0], v[1], v[2], static_cast<float>(0.5 * len));
+            L.e1 = make_float4(v[3] - v[0], v[4] - v[1], v[5] - v[2], 0.0f);
+            L.e2 = make_float4(v[6] - v[0], v[7] - v[1], v[8] - v[2], 0.0f);
+            L.n = make_float4(static_cast<float>(c[0] / len), static_cast<float>(c[1] / len),
+                              static_cast<float>(c[2] / len), 0.0f);
+            L.L = make_float4(e[0], e[1], e[2], 0.0f);
+            triLight[i] = static_cast<int>(lights.size());
+            lights.push_back(L);
         }
-        LightRecord L;
-        L.p0 = make_float4(v[0], v[1], v[2], static_cast<float>(0.5 * len));
-        L.e1 = make_float4(v[3] - v[0], v[4] - v[1], v[5] - v[2], 0.0f);
-        L.e2 = make_float4(v[6] - v[0], v[7] - v[1], v[8] - v[2], 0.0f);
-        L.n = make_float4(static_cast<float>(c[0] / len), static_cast<float>(c[1] / len), static_cast<float>(c[2] / len), 0.0f);
-        L.L = make_float4(e[0], e[1], e[2], 0.0f);
-        triLight[i] = static_cast<int>(lights.size());
-        lights.push_back(L);
-    }
-    int rc = 0;
-    if ((rc = upload(&C.verts, verts, static_cast<size_t>(ntri) * 9, C.stream))) return rc;
-    if ((rc = upload(&C.triMat, reinterpret_cast<const int *>(tri_mat), static_cast<size_t>(ntri), C.stream))) return rc;
-    if ((rc = upload(&C.triLight, triLight.data(), triLight.size(), C.stream))) return rc;
-    if ((rc = upload(&C.mats, mats.data(), mats.size(), C.stream))) return rc;
-    if (!lights.empty() && (rc = upload(&C.lights, lights.data(), lights.size(), C.stream))) return rc;
-    C.ntri = ntri;
-    C.nmat = nmat;
-    C.nArea = static_cast<int>(lights.size());
-    if (env) {
-        const double3 center = make_double3(0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2]));
-        const double d[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
-        const double radius = 0.5 * std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        if ((rc = uploadEnv(C, env_w, env_h, env, center, radius))) return rc;
-        C.hasEnv = true;
-    }
-    cudaError_t e = cudaStreamSynchronize(C.stream);
-    if (e != cudaSuccess) return cudaFail("spgpu_upload_scene", e);
-    C.sceneReady = true;
-    return 0;
+        int rc = 0;
+        if ((rc = upload(&C.verts, verts, static_cast<size_t>(ntri) * 9, C.stream))) return rc;
+        if ((rc = upload(&C.triMat, reinterpret_cast<const int *>(tri_mat), static_cast<size_t>(ntri), C.stream)))
+            return rc;
+        if ((rc = upload(&C.triLight, triLight.data(), triLight.size(), C.stream))) return rc;
+        if ((rc = upload(&C.mats, mats.data(), mats.size(), C.stream))) return rc;
+        if (!lights.empty() && (rc = upload(&C.lights, lights.data(), lights.size(), C.stream))) return rc;
+        C.ntri = ntri;
+        C.nmat = nmat;
+        C.nArea = static_cast<int>(lights.size());
+        if (env) {
+            const double3 center = make_double3(0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2]));
+            const double d[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+            const double radius = 0.5 * std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if ((rc = uploadEnv(C, env_w, env_h, env, center, radius))) return rc;
+            C.hasEnv = true;
+        }
+        cudaError_t e = cudaStreamSynchronize(C.stream);
+        if (e != cudaSuccess) return cudaFail("spgpu_upload_scene", e);
+        C.sceneReady = true;
+        return 0;
+    });
 }
 
 int spgpu_build_bvh(spgpu_ctx *h) {
-    NvtxRange nvtxRange("spgpu_build_bvh");
-    if (!h) return SPGPU_EINVAL;
-    Ctx &C = h->c;
-    if (!C.sceneReady) {
-        setError("spgpu_build_bvh: no scene uploaded");
-        return SPGPU_ESTATE;
-    }
-    cudaSetDevice(C.device);
-    C.bvhReady = false;
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    cudaEventRecord(a, C.stream);
-    char err[256] = {0};
-    const int rc = buildWideBVH(C.verts, C.ntri, C.triMat, C.triLight, &C.bvh, C.stream, err, sizeof(err));
-    cudaEventRecord(b, C.stream);
-    cudaEventSynchronize(b);
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, a, b);
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    if (rc != 0) {
-        setError(err);
-        return SPGPU_EBUILD;
-    }
-    C.buildMs = ms;
-    C.bvhReady = true;
-    freeRenderQueues(&C.rq);   // cached graphs refer to the old tree
-    for (int k = 0; k < Ctx::kPassLanes - 1; k++) freeRenderQueues(&C.rqLane[k]);
-    return 0;
+    return guarded("spgpu_build_bvh", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_build_bvh");
+        if (!h) return SPGPU_EINVAL;
+        Ctx &C = h->c;
+        if (!C.sceneReady) {
+            setError("spgpu_build_bvh: no scene uploaded");
+            return SPGPU_ESTATE;
+        }
+        cudaSetDevice(C.device);
+        C.bvhReady = false;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, C.stream);
+        char err[256] = {0};
+        const int rc = buildWideBVH(C.verts, C.ntri, C.triMat, C.triLight, &C.bvh, C.stream, err, sizeof(err));
+        cudaEventRecord(b, C.stream);
+        cudaEventSynchronize(b);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (rc != 0) {
+            setError(err);
+            return SPGPU_EBUILD;
+        }
+        C.buildMs = ms;
+        C.bvhReady = true;
+        freeRenderQueues(&C.rq);   // cached graphs refer to the old tree
+        for (int k = 0; k < Ctx::kPassLanes - 1; k++) freeRenderQueues(&C.rqLane[k]);
+        return 0;
+    });
 }
 
 int spgpu_bvh_stats(spgpu_ctx *h, spgpu_bvh_info *out) {
@@ -720,36 +747,38 @@ int spgpu_trace_stats(spgpu_ctx *h, int any_hit, const float *org_tmin, const fl
 }
 
 int spgpu_trace_host(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out) {
-    NvtxRange nvtxRange("spgpu_trace_host");
-    if (!h) return SPGPU_EINVAL;
-    Ctx &C = h->c;
-    if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
-        setError("spgpu_trace_host: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    if (n == 0) return 0;
-    cudaSetDevice(C.device);
-    const size_t rayBytes = static_cast<size_t>(n) * 16;
-    const size_t outBytes = static_cast<size_t>(n) * (any_hit ? 4 : 16);
-    float *dO = nullptr, *dD = nullptr;
-    void *dOut = nullptr;
-    cudaError_t e = cudaMallocAsync(&dO, rayBytes, C.stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&dD, rayBytes, C.stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&dOut, (outBytes + 15) & ~size_t(15), C.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dO, org_tmin, rayBytes, cudaMemcpyHostToDevice, C.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dir_tmax, rayBytes, cudaMemcpyHostToDevice, C.stream);
-    int rc = 0;
-    if (e != cudaSuccess) rc = cudaFail("spgpu_trace_host", e);
-    if (rc == 0) rc = launchTrace(C, any_hit, dO, dD, n, dOut, C.stream, false);
-    if (rc == 0) {
-        e = cudaMemcpyAsync(out, dOut, outBytes, cudaMemcpyDeviceToHost, C.stream);
+    return guarded("spgpu_trace_host", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_trace_host");
+        if (!h) return SPGPU_EINVAL;
+        Ctx &C = h->c;
+        if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
+            setError("spgpu_trace_host: invalid arguments");
+            return SPGPU_EINVAL;
+        }
+        if (n == 0) return 0;
+        cudaSetDevice(C.device);
+        const size_t rayBytes = static_cast<size_t>(n) * 16;
+        const size_t outBytes = static_cast<size_t>(n) * (any_hit ? 4 : 16);
+        float *dO = nullptr, *dD = nullptr;
+        void *dOut = nullptr;
+        cudaError_t e = cudaMallocAsync(&dO, rayBytes, C.stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(&dD, rayBytes, C.stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(&dOut, (outBytes + 15) & ~size_t(15), C.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dO, org_tmin, rayBytes, cudaMemcpyHostToDevice, C.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dir_tmax, rayBytes, cudaMemcpyHostToDevice, C.stream);
+        int rc = 0;
         if (e != cudaSuccess) rc = cudaFail("spgpu_trace_host", e);
-    }
-    cudaFreeAsync(dO, C.stream);
-    cudaFreeAsync(dD, C.stream);
-    cudaFreeAsync(dOut, C.stream);
-    if (rc == 0) rc = checkKernelError(C, C.stream);
-    return rc;
+        if (rc == 0) rc = launchTrace(C, any_hit, dO, dD, n, dOut, C.stream, false);
+        if (rc == 0) {
+            e = cudaMemcpyAsync(out, dOut, outBytes, cudaMemcpyDeviceToHost, C.stream);
+            if (e != cudaSuccess) rc = cudaFail("spgpu_trace_host", e);
+        }
+        cudaFreeAsync(dO, C.stream);
+        cudaFreeAsync(dD, C.stream);
+        cudaFreeAsync(dOut, C.stream);
+        if (rc == 0) rc = checkKernelError(C, C.stream);
+        return rc;
+    });
 }
 
 int spgpu_trace_host_noalloc(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
@@ -886,13 +915,15 @@ int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
 
 int spgpu_batch_prepare(spgpu_ctx *h, int32_t count, const spgpu_batch_item *items, int32_t autotune,
                         spgpu_batch_tuning *tuning) {
-    NvtxRange nvtxRange("spgpu_batch_prepare");
-    if (!h || count <= 0 || !items) {
-        setError("spgpu_batch_prepare: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    cudaSetDevice(h->c.device);
-    return batchPrepare(h, &h->c.batch, count, items, autotune, tuning);
+    return guarded("spgpu_batch_prepare", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_batch_prepare");
+        if (!h || count <= 0 || !items) {
+            setError("spgpu_batch_prepare: invalid arguments");
+            return SPGPU_EINVAL;
+        }
+        cudaSetDevice(h->c.device);
+        return batchPrepare(h, &h->c.batch, count, items, autotune, tuning);
+    });
 }
 
 int64_t spgpu_batch_film_pixels(spgpu_ctx *h) { return h && h->c.batch ? batchPixels(*h->c.batch) : -1; }
@@ -927,13 +958,15 @@ int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_
 }
 
 int spgpu_guiding_init(spgpu_ctx *h, const spgpu_guiding_config *cfg) {
-    NvtxRange nvtxRange("spgpu_guiding_init");
-    if (!h || !cfg) {
-        setError("spgpu_guiding_init: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    cudaSetDevice(h->c.device);
-    return guideInit(h->c, &h->c.guide, cfg);
+    return guarded("spgpu_guiding_init", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_guiding_init");
+        if (!h || !cfg) {
+            setError("spgpu_guiding_init: invalid arguments");
+            return SPGPU_EINVAL;
+        }
+        cudaSetDevice(h->c.device);
+        return guideInit(h->c, &h->c.guide, cfg);
+    });
 }
 
 int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, int32_t flags,
@@ -1036,50 +1069,56 @@ int spgpu_film_resolve(spgpu_ctx *h, const float *film, int32_t width, int32_t h
 }
 
 int spgpu_write_hdr(const char *path, const uint8_t *rgbe, int32_t width, int32_t height) {
-    if (!path || !rgbe || width <= 0 || height <= 0 || width > 0x7FFF) {
-        setError("spgpu_write_hdr: invalid arguments (scanline width < 32768)");
-        return SPGPU_EINVAL;
-    }
-    return writeHdr(path, rgbe, width, height);
+    return guarded("spgpu_write_hdr", [&]() -> int {
+        if (!path || !rgbe || width <= 0 || height <= 0 || width > 0x7FFF) {
+            setError("spgpu_write_hdr: invalid arguments (scanline width < 32768)");
+            return SPGPU_EINVAL;
+        }
+        return writeHdr(path, rgbe, width, height);
+    });
 }
 
 int spgpu_write_png(const char *path, const uint8_t *rgb, int32_t width, int32_t height) {
-    if (!path || !rgb || width <= 0 || height <= 0) {
-        setError("spgpu_write_png: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    return writePng(path, rgb, width, height);
+    return guarded("spgpu_write_png", [&]() -> int {
+        if (!path || !rgb || width <= 0 || height <= 0) {
+            setError("spgpu_write_png: invalid arguments");
+            return SPGPU_EINVAL;
+        }
+        return writePng(path, rgb, width, height);
+    });
 }
 
 int spgpu_render_host(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_render_stats *stats) {
-    NvtxRange nvtxRange("spgpu_render_host");
-    if (!h || !d || !film) {
-        setError("spgpu_render_host: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    Ctx &C = h->c;
-    if (d->width <= 0 || d->height <= 0) {
-        setError("spgpu_render_host: invalid resolution");
-        return SPGPU_EINVAL;
-    }
-    cudaSetDevice(C.device);
-    const size_t bytes = static_cast<size_t>(d->width) * d->height * 16;
-    float *dFilm = nullptr;
-    cudaError_t e = cudaMallocAsync(&dFilm, bytes, C.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dFilm, film, bytes, cudaMemcpyHostToDevice, C.stream);
-    if (e != cudaSuccess) {
+    return guarded("spgpu_render_host", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_render_host");
+        if (!h || !d || !film) {
+            setError("spgpu_render_host: invalid arguments");
+            return SPGPU_EINVAL;
+        }
+        Ctx &C = h->c;
+        if (d->width <= 0 || d->height <= 0) {
+            setError("spgpu_render_host: invalid resolution");
+            return SPGPU_EINVAL;
+        }
+        cudaSetDevice(C.device);
+        const size_t bytes = static_cast<size_t>(d->width) * d->height * 16;
+        float *dFilm = nullptr;
+        cudaError_t e = cudaMallocAsync(&dFilm, bytes, C.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dFilm, film, bytes, cudaMemcpyHostToDevice, C.stream);
+        if (e != cudaSuccess) {
+            cudaFreeAsync(dFilm, C.stream);
+            return cudaFail("spgpu_render_host", e);
+        }
+        int rc = spgpu_render(h, d, dFilm, stats, C.stream);
+        if (rc == 0) {
+            e = cudaMemcpyAsync(film, dFilm, bytes, cudaMemcpyDeviceToHost, C.stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(C.stream);
+            if (e != cudaSuccess) rc = cudaFail("spgpu_render_host", e);
+        }
         cudaFreeAsync(dFilm, C.stream);
-        return cudaFail("spgpu_render_host", e);
-    }
-    int rc = spgpu_render(h, d, dFilm, stats, C.stream);
-    if (rc == 0) {
-        e = cudaMemcpyAsync(film, dFilm, bytes, cudaMemcpyDeviceToHost, C.stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(C.stream);
-        if (e != cudaSuccess) rc = cudaFail("spgpu_render_host", e);
-    }
-    cudaFreeAsync(dFilm, C.stream);
-    cudaStreamSynchronize(C.stream);
-    return rc;
+        cudaStreamSynchronize(C.stream);
+        return rc;
+    });
 }
 
 }  // extern "C"
