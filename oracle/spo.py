@@ -169,7 +169,6 @@ class Oracle:
         self.lib.spo_film_reinhard(film.ctypes.data, W, H, alpha, out.ctypes.data)
         return out
 
-
     def film_drago(self, film, p):
         film, W, H = self._film(film)
         out = np.zeros((H, W, 3), np.float64)

@@ -105,4 +105,11 @@ def durand(film, target_contrast, sigma_space=0.02, sigma_color=0.4):
     cf = np.log(target_contrast) / (log_base.max() - log_base.min())
     log_abs = cf * log_base.max()
     m = 10.0 ** (_gray_rep(log_base) * cf + _gray_rep(log_detail) - log_abs)
-    return np.clip(tmp * m[..., None], 0.0, 1.0)
+    return _clamp01(tmp * m[..., None])
+
+
+def _clamp01(c):
+    """Spectrum::clamp(c, 0, 1) = maximum(lo, minimum(c, hi)) with std::max / std::min per
+    channel (core/spectrum.cc:697-713): a NaN channel becomes 0."""
+    t = np.where(1.0 < c, 1.0, c)
+    return np.where(0.0 < t, t, 0.0)

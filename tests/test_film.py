@@ -7,6 +7,7 @@ import struct
 import zlib
 
 import numpy as np
+import pytest
 
 from conftest import GOLDEN
 
@@ -99,3 +100,19 @@ def test_tone_mapping_restatement_matches_reference():
     np.testing.assert_allclose(durand, g["durand"], rtol=1e-13, atol=1e-15)
     inside = (g["durand"] > 0) & (g["durand"] < 1)
     assert inside.mean() > 0.5   # the image is mostly not clipped: the comparison means something
+
+
+@pytest.mark.parametrize("H, W", [(1, 1), (1, 9), (7, 1), (48, 64)])
+def test_tone_mapping_restatement_on_random_films(ref, H, W):
+    """The numpy restatement against the compiled reference's operators on seeded films,
+    including single-row and single-column images (the bilateral filter's scans have
+    nothing to do along a unit dimension) and black pixels."""
+    from oracle import tmo_oracle
+    rng = np.random.default_rng(H * 1000 + W)
+    film = np.empty((H, W, 4), np.float32)
+    film[..., :3] = rng.lognormal(0.0, 2.0, (H, W, 3)).astype(np.float32)
+    film[..., 3] = rng.integers(1, 64, (H, W)).astype(np.float32)
+    film[rng.random((H, W)) < 0.1] = 0.0
+    np.testing.assert_allclose(tmo_oracle.reinhard(film, 0.3), ref.film_reinhard(film, 0.3), rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(tmo_oracle.drago(film, 0.7), ref.film_drago(film, 0.7), rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(tmo_oracle.durand(film, 4.0), ref.film_durand(film, 4.0), rtol=1e-12, atol=1e-15)
