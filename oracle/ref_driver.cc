@@ -208,6 +208,27 @@ spo_scene *spo_scene_create(int ntri, const double *verts, const int32_t *tri_ma
 
 void spo_scene_destroy(spo_scene *s) { delete s; }
 
+double spo_triangle_area(const double *v) {
+    const Triangle tri(Point3d(v[0], v[1], v[2]), Point3d(v[3], v[4], v[5]), Point3d(v[6], v[7], v[8]),
+                       Transform());
+    return tri.area();
+}
+
+int spo_box_intersect(const double *lo, const double *hi, const double *org, const double *dir, double tmax,
+                      double *tnear, double *tfar) {
+    const Bounds3d b(Point3d(lo[0], lo[1], lo[2]), Point3d(hi[0], hi[1], hi[2]));
+    return b.intersect(Ray(Point3d(org[0], org[1], org[2]), Vector3d(dir[0], dir[1], dir[2]), tmax), tnear, tfar)
+               ? 1
+               : 0;
+}
+
+void spo_ray_invdir(const double *org, const double *dir, double *inv) {
+    const Ray r(Point3d(org[0], org[1], org[2]), Vector3d(dir[0], dir[1], dir[2]));
+    inv[0] = r.invdir().x();
+    inv[1] = r.invdir().y();
+    inv[2] = r.invdir().z();
+}
+
 int spo_scene_num_lights(const spo_scene *s) { return static_cast<int>(s->lights.size()); }
 
 int spo_trace(spo_scene *s, int any, int64_t n, const double *org, const double *dir,

@@ -312,7 +312,7 @@ struct Box {
         if (df.y >= df.z) return 1;
         return 2;
     }
-    bool hit(const Ray &r) const {   // bounds3d_detail.h:64
+    bool hit(const Ray &r, double *tNear = nullptr, double *tFar = nullptr) const {   // bounds3d_detail.h:64
         double t0 = 0.0, t1 = r.maxDist;
         for (int i = 0; i < 3; i++) {
             double a = (lo[i] - r.o[i]) * r.inv[i];
@@ -322,6 +322,8 @@ struct Box {
             t1 = std::min(t1, b);
             if (t0 > t1) return false;
         }
+        if (tNear) *tNear = t0;
+        if (tFar) *tFar = t1;
         return true;
     }
 };
@@ -1540,6 +1542,27 @@ spo_scene *spo_scene_create(int ntri, const double *verts, const int32_t *tri_ma
     }
     s->bvh.build(s->tris);
     return s;
+}
+
+double spo_triangle_area(const double *v) {
+    Tri T;
+    for (int k = 0; k < 3; k++) T.p[k] = V3(v[3 * k], v[3 * k + 1], v[3 * k + 2]);
+    return triArea(T);
+}
+
+int spo_box_intersect(const double *lo, const double *hi, const double *org, const double *dir, double tmax,
+                      double *tnear, double *tfar) {
+    Box b;
+    b.lo = V3(lo[0], lo[1], lo[2]);
+    b.hi = V3(hi[0], hi[1], hi[2]);
+    return b.hit(Ray(V3(org[0], org[1], org[2]), V3(dir[0], dir[1], dir[2]), tmax), tnear, tfar) ? 1 : 0;
+}
+
+void spo_ray_invdir(const double *org, const double *dir, double *inv) {
+    const Ray r(V3(org[0], org[1], org[2]), V3(dir[0], dir[1], dir[2]));
+    inv[0] = r.inv.x;
+    inv[1] = r.inv.y;
+    inv[2] = r.inv.z;
 }
 
 void spo_scene_destroy(spo_scene *s) { delete s; }

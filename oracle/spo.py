@@ -169,6 +169,28 @@ class Oracle:
         self.lib.spo_film_reinhard(film.ctypes.data, W, H, alpha, out.ctypes.data)
         return out
 
+    def triangle_area(self, v):
+        v = np.ascontiguousarray(v, np.float64).reshape(9)
+        self.lib.spo_triangle_area.restype = C.c_double
+        self.lib.spo_triangle_area.argtypes = [C.c_void_p]
+        return self.lib.spo_triangle_area(v.ctypes.data)
+
+    def box_intersect(self, lo, hi, org, d, tmax=np.inf):
+        """(hit, tnear, tfar) of Bounds3d::intersect."""
+        a = [np.ascontiguousarray(x, np.float64).reshape(3) for x in (lo, hi, org, d)]
+        tn, tf = C.c_double(np.nan), C.c_double(np.nan)
+        self.lib.spo_box_intersect.argtypes = [C.c_void_p] * 4 + [C.c_double, C.c_void_p, C.c_void_p]
+        h = self.lib.spo_box_intersect(*[x.ctypes.data for x in a], float(tmax), C.byref(tn), C.byref(tf))
+        return bool(h), tn.value, tf.value
+
+    def ray_invdir(self, org, d):
+        o = np.ascontiguousarray(org, np.float64).reshape(3)
+        dd = np.ascontiguousarray(d, np.float64).reshape(3)
+        inv = np.zeros(3, np.float64)
+        self.lib.spo_ray_invdir.argtypes = [C.c_void_p] * 3
+        self.lib.spo_ray_invdir(o.ctypes.data, dd.ctypes.data, inv.ctypes.data)
+        return inv
+
     def film_drago(self, film, p):
         film, W, H = self._film(film)
         out = np.zeros((H, W, 3), np.float64)

@@ -73,6 +73,17 @@ int spo_bsdf_eval(const double *mat, int64_t n, const double *wo, const double *
 int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double *u,
                     double *wi, double *f, double *pdf, int32_t *type);
 
+/* Known-answer probes of the geometry primitives, the objects of the reference's own
+ * unit tests: Triangle::area (core/triangle.cc; tests/test_geometry.cc:79-84) of the
+ * triangle v[0..8]; Bounds3d::intersect (core/bounds3d_detail.h:64-79;
+ * tests/test_geometry.cc:119-125) of the box [lo, hi] and the ray (org, dir, tmax),
+ * returning 1 on a hit with the entry and exit distances; Ray's inverse direction with
+ * INFTY for zero components (core/ray.cc:43-47; tests/test_ray.cc:14-21). */
+double spo_triangle_area(const double *v);
+int spo_box_intersect(const double *lo, const double *hi, const double *org, const double *dir, double tmax,
+                      double *tnear, double *tfar);
+void spo_ray_invdir(const double *org, const double *dir, double *inv);
+
 const char *spo_name(void);
 
 /* Film output through the reference (compiled reference only): a W x H film of float4

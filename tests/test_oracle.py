@@ -150,3 +150,45 @@ def test_port_qbvh_variant_of_reference_agrees(ref):
     pa, _ = ref.scene(sph).trace(org.astype(float), d.astype(float))
     pb, _ = ref.scene(sph, use_simd=True).trace(org.astype(float), d.astype(float))
     assert (pa == pb).mean() > 0.999
+
+
+def _geometry_kats(o):
+    """The reference's own unit-test values: tests/test_geometry.cc:79-84 (area 0.5),
+    :119-125 (slab entry 1, exit 2), tests/test_ray.cc:14-21 (INFTY for zero components)."""
+    assert o.triangle_area([1, 0, 0, 0, 0, 0, 0, 1, 0]) == 0.5
+    hit, tn, tf = o.box_intersect([0, 0, 0], [1, 1, 1], [0.5, 0.5, -1.0], [0, 0, 1])
+    assert hit and tn == 1.0 and tf == 2.0
+    inv = o.ray_invdir([1, 2, 3], [1, 0, 0])
+    assert list(inv) == [1.0, 1.0e32, 1.0e32]   # INFTY is 1e32 (core/common.h:54)
+
+
+def test_geometry_kats_port(port):
+    _geometry_kats(port)
+
+
+def test_geometry_kats_reference(ref):
+    _geometry_kats(ref)
+
+
+def test_geometry_probes_port_matches_reference(port, ref):
+    """Seeded triangles, boxes and rays (axis-aligned directions included): the
+    restatement's area, slab distances and inverse directions are bit-identical to the
+    reference's."""
+    rng = np.random.default_rng(17)
+    hits = 0
+    for k in range(300):
+        v = rng.normal(size=9) * rng.lognormal(0, 2)
+        assert port.triangle_area(v) == ref.triangle_area(v)
+        lo = rng.normal(size=3)
+        hi = lo + rng.random(3) * 2
+        org = rng.normal(size=3) * 3
+        d = rng.normal(size=3) if k % 4 == 0 else lo + rng.random(3) * (hi - lo) - org   # mostly aimed at the box
+        if k % 3 == 0:
+            d[rng.integers(0, 3)] = 0.0
+        tmax = np.inf if k % 2 else rng.random() * 5
+        hp, tnp, tfp = port.box_intersect(lo, hi, org, d, tmax)
+        hr, tnr, tfr = ref.box_intersect(lo, hi, org, d, tmax)
+        assert hp == hr and (not hp or (tnp, tfp) == (tnr, tfr))
+        hits += hp
+        np.testing.assert_array_equal(port.ray_invdir(org, d), ref.ray_invdir(org, d))
+    assert 20 < hits < 280
