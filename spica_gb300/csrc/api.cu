@@ -667,7 +667,10 @@ int spgpu_upload_scene(spgpu_ctx *h, int32_t ntri, const float *verts, const int
 int spgpu_build_bvh(spgpu_ctx *h) {
     return guarded("spgpu_build_bvh", [&]() -> int {
         NvtxRange nvtxRange("spgpu_build_bvh");
-        if (!h) return SPGPU_EINVAL;
+        if (!h) {
+            setError("spgpu_build_bvh: null context");
+            return SPGPU_EINVAL;
+        }
         Ctx &C = h->c;
         if (!C.sceneReady) {
             setError("spgpu_build_bvh: no scene uploaded");
@@ -700,7 +703,10 @@ int spgpu_build_bvh(spgpu_ctx *h) {
 }
 
 int spgpu_bvh_stats(spgpu_ctx *h, spgpu_bvh_info *out) {
-    if (!h || !out) return SPGPU_EINVAL;
+    if (!h || !out) {
+        setError("spgpu_bvh_stats: invalid arguments");
+        return SPGPU_EINVAL;
+    }
     Ctx &C = h->c;
     std::memset(out, 0, sizeof(*out));
     out->triangles = C.ntri;
@@ -720,7 +726,10 @@ int spgpu_bvh_stats(spgpu_ctx *h, spgpu_bvh_info *out) {
 int spgpu_trace(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out,
                 void *stream) {
     NvtxRange nvtxRange("spgpu_trace");
-    if (!h) return SPGPU_EINVAL;
+    if (!h) {
+        setError("spgpu_trace: null context");
+        return SPGPU_EINVAL;
+    }
     Ctx &C = h->c;
     cudaSetDevice(C.device);
     return launchTrace(C, any_hit, org_tmin, dir_tmax, n, out, static_cast<cudaStream_t>(stream), false);
@@ -729,7 +738,10 @@ int spgpu_trace(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *d
 int spgpu_trace_stats(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out,
                       spgpu_trace_counters *counters) {
     NvtxRange nvtxRange("spgpu_trace_stats");
-    if (!h || !counters) return SPGPU_EINVAL;
+    if (!h || !counters) {
+        setError("spgpu_trace_stats: invalid arguments");
+        return SPGPU_EINVAL;
+    }
     Ctx &C = h->c;
     cudaSetDevice(C.device);
     cudaError_t e = cudaMemsetAsync(C.traceStats, 0, 4 * sizeof(unsigned long long), C.stream);
@@ -749,7 +761,10 @@ int spgpu_trace_stats(spgpu_ctx *h, int any_hit, const float *org_tmin, const fl
 int spgpu_trace_host(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out) {
     return guarded("spgpu_trace_host", [&]() -> int {
         NvtxRange nvtxRange("spgpu_trace_host");
-        if (!h) return SPGPU_EINVAL;
+        if (!h) {
+            setError("spgpu_trace_host: null context");
+            return SPGPU_EINVAL;
+        }
         Ctx &C = h->c;
         if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
             setError("spgpu_trace_host: invalid arguments");
@@ -784,7 +799,10 @@ int spgpu_trace_host(spgpu_ctx *h, int any_hit, const float *org_tmin, const flo
 int spgpu_trace_host_noalloc(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
                              void *out) {
     NvtxRange nvtxRange("spgpu_trace_host_noalloc");
-    if (!h) return SPGPU_EINVAL;
+    if (!h) {
+        setError("spgpu_trace_host_noalloc: null context");
+        return SPGPU_EINVAL;
+    }
     Ctx &C = h->c;
     if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
         setError("spgpu_trace_host_noalloc: invalid arguments");
@@ -1003,7 +1021,10 @@ int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
 
 int spgpu_guiding_train(spgpu_ctx *h, int32_t steps, double *mean_loss) {
     NvtxRange nvtxRange("spgpu_guiding_train");
-    if (!h || steps < 0) return SPGPU_EINVAL;
+    if (!h || steps < 0) {
+        setError("spgpu_guiding_train: invalid arguments");
+        return SPGPU_EINVAL;
+    }
     if (!h->c.guide) {
         setError("spgpu_guiding_train: call spgpu_guiding_init first");
         return SPGPU_ESTATE;

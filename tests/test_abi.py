@@ -51,6 +51,56 @@ def test_create_rejects_invalid_pass_lanes():
         assert b"pass_lanes" in lib.spgpu_last_error()
 
 
+# every entry point with a null context or null buffers: (name, arguments)
+_NULL_CALLS = [
+    ("spgpu_create", (None, None)),
+    ("spgpu_upload_scene", (None, 0, None, None, 0, None, None, 0, 0, None)),
+    ("spgpu_build_bvh", (None,)),
+    ("spgpu_bvh_stats", (None, None)),
+    ("spgpu_trace", (None, 0, None, None, 0, None, None)),
+    ("spgpu_trace_stats", (None, 0, None, None, 0, None, None)),
+    ("spgpu_trace_host", (None, 0, None, None, 0, None)),
+    ("spgpu_trace_host_noalloc", (None, 0, None, None, 0, None)),
+    ("spgpu_render", (None, None, None, None, None)),
+    ("spgpu_render_host", (None, None, None, None)),
+    ("spgpu_render_profile", (None, None, None, None, None)),
+    ("spgpu_batch_prepare", (None, 0, None, 0, None)),
+    ("spgpu_batch_run", (None, None, None, None, None)),
+    ("spgpu_guiding_init", (None, None)),
+    ("spgpu_guiding_render", (None, None, None, 0, None, None)),
+    ("spgpu_guiding_train", (None, 0, None)),
+    ("spgpu_guiding_ring", (None, None, 0, None)),
+    ("spgpu_guiding_params", (None, None, 0)),
+    ("spgpu_guiding_mlp", (None, None, 0, None, None)),
+    ("spgpu_guiding_grad", (None, None, 0, None, None, None)),
+    ("spgpu_film_resolve", (None, None, 0, 0, 0, 0.0, None, None)),
+    ("spgpu_write_hdr", (None, None, 0, 0)),
+    ("spgpu_write_png", (None, None, 0, 0)),
+    ("spgpu_scene_load", (None, None)),
+    ("spgpu_load_hdr", (None, None, 0, None, None)),
+]
+
+
+def test_invalid_arguments_return_a_status_and_a_message():
+    """Every entry point refuses a null context or null buffers with a negative status,
+    before any device call (so this runs without a GPU), and leaves a message that names
+    it in spgpu_last_error; spgpu_destroy and spgpu_scene_free accept NULL."""
+    from spica_gb300 import gpu
+    lib = gpu.load_library()
+    names = {n for n, _ in _NULL_CALLS}
+    counters = ("spgpu_batch_film_pixels", "spgpu_guiding_samples")   # -1 without the state they count
+    assert names == {n for n in _declared() if n not in (
+        "spgpu_destroy", "spgpu_scene_free", "spgpu_last_error", "spgpu_version") + counters}
+    for name in counters:
+        assert getattr(lib, name)(None) == -1, name
+    for name, args in _NULL_CALLS:
+        rc = getattr(lib, name)(*args)
+        assert rc < 0, name
+        assert lib.spgpu_last_error().decode().startswith(name), (name, lib.spgpu_last_error())
+    lib.spgpu_destroy(None)
+    lib.spgpu_scene_free(None)
+
+
 def test_loader_fails_loudly_without_library(tmp_path):
     import pytest
     from spica_gb300 import gpu
