@@ -132,3 +132,51 @@ def test_reference_side_plugins_compile_and_export():
         so = os.path.join(d, "_build", name + ".so")
         syms = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
         assert " createInstance" in syms and " getDescription" in syms, name
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/spica_gpu.h compiles as strict C99 (the language of a cgo / JNI / N-API
+    binding), and a C program links against the library and calls the host-only entry
+    points: the version, a scene file through spgpu_scene_load, and an .hdr write."""
+    import subprocess
+    import pytest
+    from spica_gb300 import build
+    lib = build.build()
+    (tmp_path / "t.ply").write_bytes(
+        b"ply\nformat binary_little_endian 1.0\nelement vertex 3\nproperty float x\nproperty float y\n"
+        b"property float z\nelement face 1\nproperty list uchar int vertex_indices\nend_header\n"
+        + bytes.fromhex("00000000" * 3 + "0000803f" + "00000000" * 2 + "00000000" + "0000803f" + "00000000")
+        + b"\x03" + bytes.fromhex("00000000" "01000000" "02000000"))
+    (tmp_path / "s.xml").write_text(
+        '<scene version="0.5.0"><integrator type="path"/><sensor type="perspective">'
+        '<float name="fov" value="40"/><transform name="toWorld"><lookAt origin="0 0 5" target="0 0 0" up="0 1 0"/>'
+        '</transform><sampler type="independent"><integer name="sampleCount" value="4"/></sampler>'
+        '<film type="hdrfilm"><integer name="width" value="8"/><integer name="height" value="6"/></film></sensor>'
+        '<shape type="ply"><string name="filename" value="t.ply"/></shape></scene>')
+    src = tmp_path / "main.c"
+    src.write_text(r'''
+#include "spica_gpu.h"
+#include <stdio.h>
+#include <string.h>
+int main(int argc, char **argv) {
+    spgpu_scene_file *sf = NULL;
+    uint8_t px[4 * 2 * 1] = {128, 64, 32, 129, 0, 0, 0, 0};
+    if (argc < 3 || strstr(spgpu_version(), "sm_103a") == NULL) return 2;
+    if (spgpu_scene_load(argv[1], &sf) != 0) { fprintf(stderr, "%s\n", spgpu_last_error()); return 3; }
+    printf("%d %d %d %d %d\n", sf->ntri, sf->nmat, sf->desc.width, sf->desc.height, sf->desc.spp);
+    spgpu_scene_free(sf);
+    if (spgpu_scene_load("missing.xml", &sf) != SPGPU_EINVAL || sf != NULL) return 4;
+    return spgpu_write_hdr(argv[2], px, 2, 1) == 0 ? 0 : 5;
+}
+''')
+    exe = tmp_path / "main"
+    inc = os.path.join(ROOT, "include")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", inc, str(src), lib,
+                        "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)], capture_output=True, text=True)
+    if r.returncode != 0 and "cannot find" in r.stderr:
+        pytest.skip("no C toolchain that links against the library")
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), str(tmp_path / "s.xml"), str(tmp_path / "o.hdr")], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    assert r.stdout.split() == ["1", "1", "8", "6", "4"]
+    assert (tmp_path / "o.hdr").read_bytes().startswith(b"#?RADIANCE")
