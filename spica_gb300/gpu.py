@@ -235,7 +235,8 @@ def load_library(path: Optional[str] = None):
 
 def _check(rc: int, what: str):
     if rc != 0:
-        msg = _lib.spgpu_last_error().decode() if _lib is not None else ""
+        # the message may quote bytes of a malformed input file
+        msg = _lib.spgpu_last_error().decode("utf-8", "replace") if _lib is not None else ""
         raise SpgpuError(f"{what} failed ({rc}): {msg}")
 
 

@@ -291,3 +291,50 @@ def test_headers_that_overstate_the_data_are_refused(tmp_path):
     (tmp_path / "huge.hdr").write_bytes(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 2000000000 +X 30000\n")
     with pytest.raises(SpgpuError, match="too large"):
         load_hdr(tmp_path / "huge.hdr")
+
+
+def _mutate(data, rng):
+    b = bytearray(data)
+    for _ in range(int(rng.integers(1, 7))):
+        op, i = rng.random(), int(rng.integers(0, len(b) + 1))
+        if op < 0.4 and b:
+            b[min(i, len(b) - 1)] = int(rng.integers(0, 256))
+        elif op < 0.6:
+            b[i:i] = bytes([int(rng.integers(0, 256))])
+        elif op < 0.8 and b:
+            del b[min(i, len(b) - 1)]
+        else:
+            del b[i:]
+    return bytes(b)
+
+
+def test_malformed_files_are_refused_not_crashed(tmp_path):
+    """Seeded byte-level mutations of a scene file, a PLY mesh and an .hdr map: every
+    load either succeeds or raises SpgpuError with a message (the message may quote
+    bytes of the file).  Nothing reads out of bounds or aborts the process."""
+    rng = np.random.default_rng(2024)
+    write_ply(tmp_path / "base.ply", rng.random((30, 3)), [[i, (i + 1) % 30, (i + 2) % 30] for i in range(30)])
+    write_hdr(tmp_path / "base.hdr", rng.integers(0, 255, (5, 9, 4)).astype(np.uint8))
+    xml = _minimal('<shape type="ply"><string name="filename" value="base.ply"/>'
+                   '<emitter type="area"><rgb name="radiance" value="1 2 3"/></emitter></shape>')
+    ply, hdr = (tmp_path / "base.ply").read_bytes(), (tmp_path / "base.hdr").read_bytes()
+    outcomes = {"loaded": 0, "refused": 0}
+    for k in range(450):
+        kind = k % 3
+        if kind == 0:
+            (tmp_path / "m.xml").write_bytes(_mutate(xml.encode(), rng))
+            call = lambda: load_scene(tmp_path / "m.xml")   # noqa: E731
+        elif kind == 1:
+            (tmp_path / "m.ply").write_bytes(_mutate(ply, rng))
+            (tmp_path / "m.xml").write_text(_minimal('<shape type="ply"><string name="filename" value="m.ply"/></shape>'))
+            call = lambda: load_scene(tmp_path / "m.xml")   # noqa: E731
+        else:
+            (tmp_path / "m.hdr").write_bytes(_mutate(hdr, rng))
+            call = lambda: load_hdr(tmp_path / "m.hdr")   # noqa: E731
+        try:
+            call()
+            outcomes["loaded"] += 1
+        except SpgpuError as e:
+            assert str(e), k
+            outcomes["refused"] += 1
+    assert outcomes["loaded"] > 20 and outcomes["refused"] > 20, outcomes
