@@ -10,8 +10,8 @@ The compute path is libspica_gpu.so (CUDA C++, C ABI in include/spica_gpu.h); th
 package is its host-side mirror of the reference's Accelerator/Integrator plugins.
 """
 from . import scenes  # noqa: F401
-from .gpu import (BVHInfo, Context, GpuBatch, GpuBVHAccel, GpuGuide, GpuPathIntegrator,  # noqa: F401
-                  RenderStats, SpgpuError, TraceCounters, load_library)
+from .gpu import (BVHInfo, Context, GpuBatch, GpuBVHAccel, GpuDirectLightingIntegrator, GpuGuide,  # noqa: F401
+                  GpuPathIntegrator, RenderStats, SpgpuError, TraceCounters, load_library, load_scene)
 
-__all__ = ["scenes", "Context", "GpuBatch", "GpuBVHAccel", "GpuGuide", "GpuPathIntegrator", "SpgpuError", "load_library", "BVHInfo",
-           "RenderStats", "TraceCounters"]
+__all__ = ["scenes", "Context", "GpuBatch", "GpuBVHAccel", "GpuDirectLightingIntegrator", "GpuGuide",
+           "GpuPathIntegrator", "SpgpuError", "load_library", "load_scene", "BVHInfo", "RenderStats", "TraceCounters"]
