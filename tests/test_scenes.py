@@ -59,3 +59,34 @@ def test_batch_variants_and_guiding_room():
     gr = scenes.guiding_room()
     assert gr.room_tris == 18 and gr.ntri == 18 + 200 * 12
     assert gr.env is not None and gr.env.max() >= 1.0e4
+
+
+def test_mid_scale_workload():
+    """The 2M-triangle benchmark scene: exact and deterministic triangle count, the
+    40 / 40 / 20 material mix and its parameter ranges, four one-sided quad lights facing
+    the ground, and the 1024 x 512 sky whose sun carries radiance 1e4 over a 0.5 degree
+    disk."""
+    sc = scenes.mid_scale()
+    again = scenes.mid_scale()
+    assert sc.ntri == 2_033_674
+    assert np.array_equal(sc.verts, again.verts) and np.array_equal(sc.tri_mat, again.tri_mat)
+    assert (_areas(sc.verts) > 1e-9).all()
+    m = sc.materials[1:-1]   # the 500 instances (ground first, the lights' black material last)
+    kinds = m[:, 0].astype(int)
+    frac = np.array([(kinds == k).mean() for k in (scenes.MAT_LAMBERT, scenes.MAT_CONDUCTOR, scenes.MAT_DIELECTRIC)])
+    assert len(m) == 500 and np.allclose(frac, [0.4, 0.4, 0.2], atol=0.06), frac
+    lam = m[kinds == scenes.MAT_LAMBERT][:, 1:4]
+    assert lam.min() >= 0.1 and lam.max() <= 0.9
+    emit = sc.tri_emit[:, 0] > 0
+    assert emit.sum() == 8 and sc.num_lights == 9   # one area light per triangle, plus the sky
+    L = sc.verts[emit].astype(np.float64)
+    n = np.cross(L[:, 3:6] - L[:, 0:3], L[:, 6:9] - L[:, 0:3])
+    assert (n[:, 2] < 0).all()
+    assert sc.env.shape == (512, 1024, 3)
+    # sun: the texels above the sky's own maximum hold 1e4 times the solid angle they cover
+    H, W = sc.env.shape[:2]
+    th = (np.arange(H) + 0.5) / H * np.pi
+    texel_sr = (np.pi / H) * (2 * np.pi / W) * np.sin(th)[:, None] * np.ones((1, W))
+    excess = np.clip(sc.env[..., 0].astype(np.float64) - 1.0, 0.0, None)
+    disk_sr = 2 * np.pi * (1 - np.cos(np.radians(0.25)))
+    assert abs((excess * texel_sr).sum() / 1.0e4 - disk_sr) < 0.1 * disk_sr
