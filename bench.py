@@ -220,6 +220,18 @@ def run_reference(args):
         sc.render(scene.camera, W, H, 1, scene.max_depth, seed=200 + k, window=(0, y, W, rows), nthreads=threads)
     dt = time.perf_counter() - t0
     value = args.steps * rows * W / dt
+    qbvh = None
+    if kind == "reference":
+        # the reference's second traversal, BVHAccel with useSIMD (its 4-wide QBVH, bvh.cc:389),
+        # on the same film rows
+        sq = o.scene(scene, use_simd=True)
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            y = int(ys[args.warmup + k])
+            sq.render(scene.camera, W, H, 1, scene.max_depth, seed=200 + k, window=(0, y, W, rows),
+                      nthreads=threads)
+        qbvh = {"value": args.steps * rows * W / (time.perf_counter() - t0), "unit": UNIT,
+                "variant": "BVHAccel useSIMD=true (QBVH)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -227,6 +239,8 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
                              "sample": f"{args.steps} steps of {rows} rows x {W} px", "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if qbvh:
+        line["qbvh"] = qbvh
     print(json.dumps(line), flush=True)
     return 0
 
