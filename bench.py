@@ -50,7 +50,12 @@ CONFIG = {"workload": "mid-scale plain render: 500 instances, ~2.03M triangles, 
 
 
 E2E_SPP = 16   # samples per pixel per host-API render call in the end-to-end measurement
-EXTEND_DRAM_BYTES_PER_LAUNCH = 28.68e6   # measured with ncu on the 1920x1080 workload
+PASS_LANES = 8   # sample passes in flight (spgpu_config.pass_lanes 0 = 8)
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one sample pass's 17 extend
+# launches on the 1920x1080 workload, averaged per launch.  A constant: it is measured
+# by the ncu command in profiles/ and must be re-measured whenever the tree, the
+# traversal or the queue layout changes.
+EXTEND_DRAM_BYTES_PER_LAUNCH = 28.68e6
 
 
 def max_over_ranks(torch, x: float, ws: int, device: str = "cuda") -> float:
@@ -388,27 +393,6 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=1280, H=720, budget_spp=1024, re
             "training_roofline": train_roof}
 
 
-def guided_passes(torch, GpuBVHAccel, scenes, W=640, H=360):
-    """Profiling case for the guided wavefront: brief online training, then one plain and
-    one guided 8-spp render of the guiding room inside the NVTX range 'profiled'."""
-    from spica_gb300.gpu import GUIDE_COLLECT, GUIDE_GUIDED, GpuGuide
-    sc = scenes.guiding_room(width=W, height=H)
-    acc = GpuBVHAccel(sc).construct()
-    g = GpuGuide(acc, seed=2)
-    p = {"width": W, "height": H, "maxDepth": sc.max_depth}
-    f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
-    for k in range(8):
-        g.render(sc.camera, dict(p, sampleCount=2), f, GUIDE_GUIDED | GUIDE_COLLECT, seed=1, sample_offset=2 * k)
-        g.train(32)
-    torch.cuda.synchronize()
-    torch.cuda.nvtx.range_push("profiled")
-    sp = g.render(sc.camera, dict(p, sampleCount=8), f, 0, seed=2)
-    sg = g.render(sc.camera, dict(p, sampleCount=8), f, GUIDE_GUIDED, seed=2)
-    torch.cuda.nvtx.range_pop()
-    torch.cuda.synchronize()
-    return {"width": W, "height": H, "spp": 8, "plain_ms": sp.ms, "guided_ms": sg.ms}
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -421,19 +405,6 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-API measurement")
     ap.add_argument("--no-guiding", action="store_true", help="skip the learned-guiding comparison")
     ap.add_argument("--no-profile", action="store_true", help="skip the per-kernel profile (roofline)")
-    ap.add_argument("--width", type=int, default=1920, help="film width (profiling cases only)")
-    ap.add_argument("--height", type=int, default=1080, help="film height (profiling cases only)")
-    ap.add_argument("--batch-only", type=int, default=0, metavar="RENDERS",
-                    help="only the batched-renders measurement on the first RENDERS variants, default launch "
-                         "shape (profiling cases)")
-    ap.add_argument("--guiding-only", action="store_true",
-                    help="only the learned-guiding comparison, on a small case (320x180, profiling)")
-    ap.add_argument("--guided-passes", action="store_true",
-                    help="profiling case: the guiding room at 640x360, 8 collection passes of 2 spp with 32 Adam "
-                         "steps each, then one plain and one guided render of 8 spp inside the NVTX range "
-                         "'profiled'")
-    ap.add_argument("--micro-only", type=int, default=0, metavar="RAYS",
-                    help="only the intersection microbench, on RAYS rays (profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -447,21 +418,7 @@ def main():
     from spica_gb300 import GpuBatch, GpuBVHAccel, GpuPathIntegrator, scenes
     from spica_gb300.gpu import KERNEL_CLASSES
 
-    if args.micro_only:
-        print(json.dumps({"microbench": microbench(torch, GpuBVHAccel, scenes, rays=args.micro_only)}), flush=True)
-        return 0
-    if args.batch_only:
-        print(json.dumps({"batch": batch_bench(torch, GpuBatch, scenes, reps=1, count=args.batch_only,
-                                               autotune=False)}), flush=True)
-        return 0
-    if args.guiding_only:
-        print(json.dumps({"guiding": guiding_bench(torch, GpuBVHAccel, scenes, W=320, H=180, budget_spp=64,
-                                                   ref_spp=512)}), flush=True)
-        return 0
-    if args.guided_passes:
-        print(json.dumps({"guided_passes": guided_passes(torch, GpuBVHAccel, scenes)}), flush=True)
-        return 0
-    scene = scenes.mid_scale(width=args.width, height=args.height)
+    scene = scenes.mid_scale()
     W, H, md = scene.width, scene.height, scene.max_depth
     npix = W * H
     acc = GpuBVHAccel(scene, device=local).construct()
@@ -470,8 +427,10 @@ def main():
     params = {"width": W, "height": H, "maxDepth": md}
     film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
-    # warm-up (graph capture happens in the first call)
-    integ.render_device(scene.camera, acc, dict(params, sampleCount=max(args.warmup, 1)), film, stream=stream)
+    # warm-up: every pass lane allocates its queues and captures its graph on its first
+    # pass, so the warm-up renders W passes on each of the PASS_LANES lanes
+    warm = max(args.warmup, 1) * PASS_LANES
+    integ.render_device(scene.camera, acc, dict(params, sampleCount=warm), film, stream=stream)
     torch.cuda.synchronize()
 
     def barrier():
@@ -484,7 +443,7 @@ def main():
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
     st = integ.render_device(scene.camera, acc, dict(params, sampleCount=args.steps), film,
-                             sample_offset=max(args.warmup, 1), stream=stream)
+                             sample_offset=warm, stream=stream)
     ev1.record()
     barrier()
     clk = clocks.stop()
@@ -537,8 +496,6 @@ def main():
                 "ms_per_launch": ext_ms_per_launch, "nodes_per_ray": pr.closest_nodes_per_ray,
                 "tris_per_ray": pr.closest_tris_per_ray}
     if (W, H) == (1920, 1080):
-        # ncu dram__bytes_read.sum + dram__bytes_write.sum of the 17 extend launches of a
-        # full-size pass, averaged per launch (profiles/extend_traffic_midscale_1080p.md)
         roofline["traffic"] = EXTEND_DRAM_BYTES_PER_LAUNCH
 
     pb = path_bytes(pr)

@@ -7,7 +7,8 @@
  * core/common.h:69-115; a C++ plugin wrapper turns a negative status into FatalError).
  *
  * One context = one device + one scene + its BVH.  A context is used by one host
- * thread at a time.  "device pointer" arguments are CUDA device memory (for example
+ * thread at a time, except spgpu_trace_host, which any number of host threads may call
+ * on one context at once (the calls are serialised inside).  "device pointer" arguments are CUDA device memory (for example
  * a torch tensor's data_ptr); "host" entry points take host memory and copy both
  * ways themselves.  `stream` is a cudaStream_t passed as void*; NULL is CUDA's
  * legacy default stream (the one torch uses unless told otherwise).
@@ -144,11 +145,16 @@ int spgpu_bvh_stats(spgpu_ctx *ctx, spgpu_bvh_info *out);
  * uint32 (1 = occluded). */
 int spgpu_trace(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n, void *out,
                 void *stream);                                                       /* device pointers */
+/* host pointers; blocking.  Safe to call from several host threads on one context, as
+ * the reference calls Accelerator::intersect from every render thread
+ * (core/integrator.cc:77): the calls queue on a per-context lock.  Rays and hits are
+ * staged in a per-context device buffer, allocated on the first call and regrown only
+ * when a larger batch arrives. */
 int spgpu_trace_host(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
-                     void *out);                                                     /* host pointers   */
+                     void *out);
 /* spgpu_trace_host without any device allocation (no counterpart in the reference).
- * spgpu_trace_host allocates its device ray and hit buffers per call from the
- * stream-ordered pool; this variant stages them instead in a static device array
+ * spgpu_trace_host allocates its device staging buffer on a context's first call and
+ * again whenever a larger batch arrives; this variant stages rays and hits instead in a static device array
  * reserved with the library on each device (3 MiB + 256 bytes), so it suits callers whose
  * device memory is fully held by their own allocator or arena, or that must not grow
  * or trim a memory pool in a latency-critical loop.
@@ -162,6 +168,39 @@ int spgpu_trace_host_noalloc(spgpu_ctx *ctx, int any_hit, const float *org_tmin,
 /* same as spgpu_trace on device pointers, counting node and triangle visits */
 int spgpu_trace_stats(spgpu_ctx *ctx, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
                       void *out, spgpu_trace_counters *counters);
+
+/* ---- BSDFs and the sampler, one function at a time ------------------------------
+ * The device functions that shade every hit of spgpu_render, evaluated on caller-given
+ * directions and random numbers.  Host pointers; blocking; the context supplies the
+ * device and stream only (no scene needed).
+ *
+ * replaces: BSDF::f, BSDF::pdf and BSDF::sample (core/bsdf.cc:49-136) of one material
+ * (an 8-float SPGPU_MAT_* record, as in spgpu_upload_scene), with directions in the
+ * shading frame: z = shading normal (the reference's BSDF with normal z, tangent x,
+ * binormal y, where world and local directions coincide).
+ * eval:   wo, wi: n x 3  ->  f: n x 3, pdf: n.  For the smooth dielectric, pdf is
+ *         FresnelSpecular::pdf (core/bxdf.cc:236: F or 1 - F within the 1e-4 cones about
+ *         the mirror and refracted directions).
+ * sample: wo: n x 3, u: n x 3 -- u[0], u[1] the 2D sample of BSDF::sample and u[2] the
+ *         draw the reference takes from its BxDFs' own generator (core/bxdf.cc:18 for the
+ *         rough dielectric's reflect-or-refract choice, bsdfs/plastic.cc:18 for the
+ *         plastic's specular-or-diffuse choice; unused by the other materials)
+ *         ->  wi: n x 3, f: n x 3, pdf: n, type: n (BxDFType bits of the sample:
+ *         1 reflection, 2 transmission, 4 diffuse, 8 glossy, 16 specular; 0 and pdf 0
+ *         when BSDF::sample finds none, wi then undefined). */
+int spgpu_bsdf_eval(spgpu_ctx *ctx, const float *material, int64_t n, const float *wo, const float *wi, float *f,
+                    float *pdf);
+int spgpu_bsdf_sample(spgpu_ctx *ctx, const float *material, int64_t n, const float *wo, const float *u, float *wi,
+                      float *f, float *pdf, int32_t *type);
+/* replaces: the random-number stream behind Sampler::get1D / get2D (core/sampler.h:28-36;
+ * samplers/independent.cc:6-23 over core/random.cc's MT19937).  The renderer draws its
+ * numbers from Philox4x32-10 (Salmon, Moraes, Dror and Shaw, SC 2011) instead, keyed by
+ * (seed, film pixel index) and counted by (sample index, bounce -- 0xFFFF for the camera
+ * ray --, stream, 0x5350); each block gives four uniforms in [0, 1) from the top 24 bits
+ * of each word.  This entry point runs that generator on the device for n arbitrary
+ * counters (n x 4 words) and keys (n x 2 words): raw: n x 4 words, u: n x 4 uniforms. */
+int spgpu_sampler_generate(spgpu_ctx *ctx, int64_t n, const uint32_t *counter, const uint32_t *key, uint32_t *raw,
+                           float *u);
 
 /* ---- rendering -------------------------------------------------------------------
  * replaces: Integrator::render(camera, scene, params) of the path integrator plugin

@@ -987,6 +987,15 @@ inline Sampler &hiddenPlasticRandom() {
     static thread_local Sampler r(0u);
     return r;
 }
+// A hidden draw, for spo_bsdf_sample_uc: with g_ucIn set, the draw is *g_ucIn instead of
+// the generator's next number; either way it is recorded in g_ucLast.
+thread_local const double *g_ucIn = nullptr;
+thread_local double g_ucLast = 0.0;
+inline double hiddenDraw(Sampler &r) {
+    const double v = g_ucIn ? *g_ucIn : r.get1D();
+    g_ucLast = v;
+    return v;
+}
 
 inline double frDiffuseReflectance(double eta) {   // fresnel.cc:87
     if (eta >= 1.0) return -1.4399 / (eta * eta) + 0.7099 / eta + 0.6681 + 0.0636 * eta;
@@ -1178,7 +1187,7 @@ struct BSDF {
             const double cO = dot(wo, wh.z > 0.0 ? wh : -wh);
             const double F = frDielectric(cO, 1.0, ior);
             bool ok = true;
-            if (hiddenBxdfRandom().get1D() < F) {
+            if (hiddenDraw(hiddenBxdfRandom()) < F) {
                 wi = reflectV(wo, wh);
                 if (!sameHemi(wo, wi)) ok = false;
                 else st = kReflection | kGlossy;
@@ -1197,7 +1206,7 @@ struct BSDF {
         } else if (kind == SPO_MAT_PLASTIC) {   // PlasticBRDF::sample, plastic.cc:44
             const double Fo = frDielectric(cosT(wo), 1.0, ior);
             const double ps = plasticProbSpecular(wo);
-            if (hiddenPlasticRandom().get1D() < ps) {
+            if (hiddenDraw(hiddenPlasticRandom()) < ps) {
                 wi = V3(-wo.x, -wo.y, wo.z);
                 *pdf = ps;
                 ret = Ks * Fo / std::abs(cosT(wi));
@@ -1667,6 +1676,37 @@ int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double
             double p = 0.0;
             int st = 0;
             const RGB v = b.sample(o, &d, P2{u[2 * i], u[2 * i + 1]}, &p, kAll, &st);
+            wi[3 * i] = d.x;
+            wi[3 * i + 1] = d.y;
+            wi[3 * i + 2] = d.z;
+            f[3 * i] = v.r;
+            f[3 * i + 1] = v.g;
+            f[3 * i + 2] = v.b;
+            pdf[i] = p;
+            type[i] = st;
+        }
+    });
+    th.join();
+    return 0;
+}
+
+// spo_bsdf_sample with the hidden draws made visible: ucIn == NULL draws them from the
+// hidden generators (fresh thread, as spo_bsdf_sample) and reports each row's draw in
+// ucOut (NaN for a row that took none); otherwise row i's draw is ucIn[i].
+int spo_bsdf_sample_uc(const double *mat, int64_t n, const double *wo, const double *u, const double *ucIn,
+                       double *wi, double *f, double *pdf, int32_t *type, double *ucOut) {
+    const BSDF b = makeBSDF(mat, normalizeDiv(cross(V3(1, 0, 0), V3(0, 1, 0))), V3(1, 0, 0), V3(0, 1, 0));
+    std::thread th([&]() {
+        for (int64_t i = 0; i < n; i++) {
+            const V3 o(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+            V3 d(0, 0, 0);
+            double p = 0.0;
+            int st = 0;
+            g_ucIn = ucIn ? ucIn + i : nullptr;
+            g_ucLast = std::numeric_limits<double>::quiet_NaN();
+            const RGB v = b.sample(o, &d, P2{u[2 * i], u[2 * i + 1]}, &p, kAll, &st);
+            g_ucIn = nullptr;
+            if (ucOut) ucOut[i] = g_ucLast;
             wi[3 * i] = d.x;
             wi[3 * i + 1] = d.y;
             wi[3 * i + 2] = d.z;

@@ -16,7 +16,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = os.environ.get("SPICA_REFERENCE_SOURCES", "/root/reference/sources")
+# the reference checkout beside this repository (override with SPICA_REFERENCE_SOURCES)
+REF_TREE = os.environ.get("SPICA_REFERENCE_SOURCES",
+                          os.path.normpath(os.path.join(HERE, "..", "..", "reference", "sources")))
 LIBS = {
     "ref": os.path.join(HERE, "_ref", "libspica_ref.so"),
     "port": os.path.join(HERE, "_port", "libspica_oracle.so"),
@@ -104,6 +106,26 @@ class Oracle:
         typ = np.zeros(n, np.int32)
         self.lib.spo_bsdf_sample(mat, n, wo, u, wi, f, pdf, typ)
         return wi, f, pdf, typ
+
+    def bsdf_sample_uc(self, mat, wo, u, uc=None):
+        """bsdf_sample with the BxDFs' hidden draws visible (the restatement only): with
+        uc None the draws come from the hidden generators and are returned per row (NaN
+        where a row took none); otherwise row i uses uc[i].  Returns (wi, f, pdf, type,
+        uc)."""
+        if not hasattr(self.lib, "spo_bsdf_sample_uc"):
+            raise NotImplementedError("spo_bsdf_sample_uc is provided by the restatement only")
+        fn = self.lib.spo_bsdf_sample_uc
+        fn.argtypes = [_dp, C.c_int64, _dp, _dp, C.c_void_p, _dp, _dp, _dp, _ip, _dp]
+        mat = np.ascontiguousarray(mat, np.float64)
+        wo = np.ascontiguousarray(wo, np.float64).reshape(-1, 3)
+        u = np.ascontiguousarray(u, np.float64).reshape(-1, 2)
+        n = wo.shape[0]
+        wi, f, pdf = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+        typ = np.zeros(n, np.int32)
+        uc_in = None if uc is None else np.ascontiguousarray(uc, np.float64).reshape(n)
+        uc_out = np.zeros(n)
+        fn(mat, n, wo, u, uc_in.ctypes.data if uc_in is not None else None, wi, f, pdf, typ, uc_out)
+        return wi, f, pdf, typ, uc_out
 
     def probe_material(self, mat):
         """The drop-in plugin's material translation on the reference's BSDF for a

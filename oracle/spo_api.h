@@ -72,6 +72,13 @@ int spo_bsdf_eval(const double *mat, int64_t n, const double *wo, const double *
                   double *f, double *pdf);
 int spo_bsdf_sample(const double *mat, int64_t n, const double *wo, const double *u,
                     double *wi, double *f, double *pdf, int32_t *type);
+/* The restatement only: spo_bsdf_sample with the draws of the BxDFs' hidden generators
+ * (core/bxdf.cc:18, bsdfs/plastic.cc:18) made visible.  uc_in == NULL: drawn as in
+ * spo_bsdf_sample, row i's draw reported in uc_out[i] (NaN if none); else row i uses
+ * uc_in[i]. */
+int spo_bsdf_sample_uc(const double *mat, int64_t n, const double *wo, const double *u,
+                       const double *uc_in, double *wi, double *f, double *pdf, int32_t *type,
+                       double *uc_out);
 
 /* Known-answer probes of the geometry primitives, the objects of the reference's own
  * unit tests: Triangle::area (core/triangle.cc; tests/test_geometry.cc:79-84) of the

@@ -10,8 +10,9 @@ The compute path is libspica_gpu.so (CUDA C++, C ABI in include/spica_gpu.h); th
 package is its host-side mirror of the reference's Accelerator/Integrator plugins.
 """
 from . import scenes  # noqa: F401
-from .gpu import (BVHInfo, Context, GpuBatch, GpuBVHAccel, GpuDirectLightingIntegrator, GpuGuide,  # noqa: F401
-                  GpuPathIntegrator, RenderStats, SpgpuError, TraceCounters, load_library, load_scene)
+from .gpu import (BVHInfo, Context, GpuBatch, GpuBSDF, GpuBVHAccel, GpuDirectLightingIntegrator,  # noqa: F401
+                  GpuGuide, GpuPathIntegrator, GpuSampler, RenderStats, SpgpuError, TraceCounters, load_library,
+                  load_scene, philox)
 
-__all__ = ["scenes", "Context", "GpuBatch", "GpuBVHAccel", "GpuDirectLightingIntegrator", "GpuGuide",
+__all__ = ["scenes", "Context", "GpuBatch", "GpuBSDF", "GpuSampler", "philox", "GpuBVHAccel", "GpuDirectLightingIntegrator", "GpuGuide",
            "GpuPathIntegrator", "SpgpuError", "load_library", "load_scene", "BVHInfo", "RenderStats", "TraceCounters"]

@@ -337,20 +337,60 @@ int noallocScratch(int device, unsigned char **base) {
 
 void setError(const std::string &msg) { g_lastError = msg; }
 
-// Runs the body of a C entry point so that no C++ exception crosses the C ABI: a failed
-// host allocation becomes SPGPU_ENOMEM, any other exception SPGPU_EINVAL, each with a
-// message.
-template <class F>
-int guarded(const char *name, F &&body) noexcept {
-    try {
-        return body();
-    } catch (const std::bad_alloc &) {
-        setError(std::string(name) + ": out of host memory");
-        return SPGPU_ENOMEM;
-    } catch (const std::exception &e) {
-        setError(std::string(name) + ": " + e.what());
-        return SPGPU_EINVAL;
+// The C ABI's 8-float material records (SPGPU_MAT_*) as device records.  The plugins
+// read alpha and IOR through Spectrum::gray() of a constant texture
+// (roughconductor.cc:48, dielectric.cc:33); the same value is kept here.
+int materialRecords(const char *who, const float *materials, int nmat, std::vector<MaterialRecord> *out) {
+    out->assign(nmat, MaterialRecord{});
+    auto gray1 = [](double v) { return 0.2126 * v + 0.7152 * v + 0.0722 * v; };
+    for (int m = 0; m < nmat; m++) {
+        const float *r = materials + 8 * m;
+        MaterialRecord &M = (*out)[m];
+        std::memset(&M, 0, sizeof(M));
+        M.type = static_cast<int>(r[0]);
+        const bool beckmannConductor = M.type == SPGPU_MAT_CONDUCTOR_BECKMANN;
+        if (beckmannConductor) M.type = kMatConductor;
+        if (M.type == kMatLambert) {
+            M.a = make_float4(fmaxf(r[1], 0.0f), fmaxf(r[2], 0.0f), fmaxf(r[3], 0.0f), 0.0f);
+        } else if (M.type == kMatConductor) {
+            M.a = make_float4(r[2], r[3], r[4], static_cast<float>(gray1(r[1])));
+            M.b = make_float4(r[5], r[6], r[7], beckmannConductor ? 1.0f : 0.0f);   // b.w: distribution
+            if (!(M.a.w > 0.0f)) {
+                setError(std::string(who) + ": conductor roughness must be positive (smooth conductors are not "
+                         "supported)");
+                return SPGPU_EINVAL;
+            }
+        } else if (M.type == kMatDielectric) {
+            M.a = make_float4(0.0f, 0.0f, 0.0f, static_cast<float>(gray1(r[1])));
+        } else if (M.type == kMatRoughDielectric) {
+            // roughdielectric.cc:41-84: zero roughness is the smooth dielectric's FresnelSpecular
+            const float alpha = static_cast<float>(gray1(r[1])), ior = static_cast<float>(gray1(r[2]));
+            if (alpha == 0.0f) {
+                M.type = kMatDielectric;
+                M.a = make_float4(0.0f, 0.0f, 0.0f, ior);
+            } else if (!(alpha > 0.0f) || !(ior > 0.0f) || (r[3] != 0.0f && r[3] != 1.0f)) {
+                setError(std::string(who) + ": rough dielectric needs alpha >= 0, ior > 0, distribution 0 or 1");
+                return SPGPU_EINVAL;
+            } else {
+                M.a = make_float4(alpha, ior, r[3], 0.0f);
+            }
+        } else if (M.type == kMatPlastic) {
+            // plastic.cc:112-122 and PlasticBRDF's specular sampling weight (plastic.cc:26)
+            const double kd = 0.2126 * r[1] + 0.7152 * r[2] + 0.0722 * r[3];
+            const double ks = 0.2126 * r[4] + 0.7152 * r[5] + 0.0722 * r[6];
+            const float ior = static_cast<float>(gray1(r[7]));
+            if (!(ior > 0.0f) || !(kd + ks > 0.0)) {
+                setError(std::string(who) + ": plastic needs ior > 0 and a non-black Kd + Ks");
+                return SPGPU_EINVAL;
+            }
+            M.a = make_float4(r[1], r[2], r[3], ior);
+            M.b = make_float4(r[4], r[5], r[6], static_cast<float>(ks / (kd + ks)));
+        } else {
+            setError(std::string(who) + ": unknown material type");
+            return SPGPU_EINVAL;
+        }
     }
+    return 0;
 }
 
 int cudaFail(const char *what, cudaError_t e) {
@@ -533,6 +573,7 @@ void spgpu_destroy(spgpu_ctx *h) {
     C.guide = nullptr;
     cudaFree(C.traceErr);
     cudaFree(C.traceStats);
+    cudaFree(C.hostStage);
     if (C.stream) cudaStreamDestroy(C.stream);
     delete h;
 }
@@ -554,57 +595,8 @@ int spgpu_upload_scene(spgpu_ctx *h, int32_t ntri, const float *verts, const int
                 return SPGPU_EINVAL;
             }
         }
-        // materials: the plugins read alpha and IOR through Spectrum::gray() of a constant
-        // texture (roughconductor.cc:48, dielectric.cc:33), kept here for the same value
-        auto gray1 = [](double v) { return 0.2126 * v + 0.7152 * v + 0.0722 * v; };
-        std::vector<MaterialRecord> mats(nmat);
-        for (int m = 0; m < nmat; m++) {
-            const float *r = materials + 8 * m;
-            MaterialRecord &M = mats[m];
-            std::memset(&M, 0, sizeof(M));
-            M.type = static_cast<int>(r[0]);
-            const bool beckmannConductor = M.type == SPGPU_MAT_CONDUCTOR_BECKMANN;
-            if (beckmannConductor) M.type = kMatConductor;
-            if (M.type == kMatLambert) {
-                M.a = make_float4(fmaxf(r[1], 0.0f), fmaxf(r[2], 0.0f), fmaxf(r[3], 0.0f), 0.0f);
-            } else if (M.type == kMatConductor) {
-                M.a = make_float4(r[2], r[3], r[4], static_cast<float>(gray1(r[1])));
-                M.b = make_float4(r[5], r[6], r[7], beckmannConductor ? 1.0f : 0.0f);   // b.w: distribution
-                if (!(M.a.w > 0.0f)) {
-                    setError("spgpu_upload_scene: conductor roughness must be positive (smooth conductors are not "
-                             "supported)");
-                    return SPGPU_EINVAL;
-                }
-            } else if (M.type == kMatDielectric) {
-                M.a = make_float4(0.0f, 0.0f, 0.0f, static_cast<float>(gray1(r[1])));
-            } else if (M.type == kMatRoughDielectric) {
-                // roughdielectric.cc:41-84: zero roughness is the smooth dielectric's FresnelSpecular
-                const float alpha = static_cast<float>(gray1(r[1])), ior = static_cast<float>(gray1(r[2]));
-                if (alpha == 0.0f) {
-                    M.type = kMatDielectric;
-                    M.a = make_float4(0.0f, 0.0f, 0.0f, ior);
-                } else if (!(alpha > 0.0f) || !(ior > 0.0f) || (r[3] != 0.0f && r[3] != 1.0f)) {
-                    setError("spgpu_upload_scene: rough dielectric needs alpha >= 0, ior > 0, distribution 0 or 1");
-                    return SPGPU_EINVAL;
-                } else {
-                    M.a = make_float4(alpha, ior, r[3], 0.0f);
-                }
-            } else if (M.type == kMatPlastic) {
-                // plastic.cc:112-122 and PlasticBRDF's specular sampling weight (plastic.cc:26)
-                const double kd = 0.2126 * r[1] + 0.7152 * r[2] + 0.0722 * r[3];
-                const double ks = 0.2126 * r[4] + 0.7152 * r[5] + 0.0722 * r[6];
-                const float ior = static_cast<float>(gray1(r[7]));
-                if (!(ior > 0.0f) || !(kd + ks > 0.0)) {
-                    setError("spgpu_upload_scene: plastic needs ior > 0 and a non-black Kd + Ks");
-                    return SPGPU_EINVAL;
-                }
-                M.a = make_float4(r[1], r[2], r[3], ior);
-                M.b = make_float4(r[4], r[5], r[6], static_cast<float>(ks / (kd + ks)));
-            } else {
-                setError("spgpu_upload_scene: unknown material type");
-                return SPGPU_EINVAL;
-            }
-        }
+        std::vector<MaterialRecord> mats;
+        if (int rc = materialRecords("spgpu_upload_scene", materials, nmat, &mats)) return rc;
         // area lights: one per emitting triangle, in triangle order (sceneparser.cc:173-179)
         std::vector<LightRecord> lights;
         std::vector<int> triLight(ntri, -1);
@@ -771,91 +763,109 @@ int spgpu_trace_host(spgpu_ctx *h, int any_hit, const float *org_tmin, const flo
             return SPGPU_EINVAL;
         }
         if (n == 0) return 0;
-        cudaSetDevice(C.device);
+        if (n > (int64_t(1) << 30)) {
+            setError("spgpu_trace_host: at most 2^30 rays per call");
+            return SPGPU_EINVAL;
+        }
+        // one call at a time per context: the calls share the control words and the
+        // staging buffer (concurrent callers on one context queue here)
+        std::lock_guard<std::mutex> lock(C.hostTraceMu);
+        cudaError_t e = cudaSetDevice(C.device);
+        if (e != cudaSuccess) return cudaFail("spgpu_trace_host: cudaSetDevice", e);
         const size_t rayBytes = static_cast<size_t>(n) * 16;
         const size_t outBytes = static_cast<size_t>(n) * (any_hit ? 4 : 16);
-        float *dO = nullptr, *dD = nullptr;
-        void *dOut = nullptr;
-        cudaError_t e = cudaMallocAsync(&dO, rayBytes, C.stream);
-        if (e == cudaSuccess) e = cudaMallocAsync(&dD, rayBytes, C.stream);
-        if (e == cudaSuccess) e = cudaMallocAsync(&dOut, (outBytes + 15) & ~size_t(15), C.stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dO, org_tmin, rayBytes, cudaMemcpyHostToDevice, C.stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dir_tmax, rayBytes, cudaMemcpyHostToDevice, C.stream);
-        int rc = 0;
-        if (e != cudaSuccess) rc = cudaFail("spgpu_trace_host", e);
-        if (rc == 0) rc = launchTrace(C, any_hit, dO, dD, n, dOut, C.stream, false);
-        if (rc == 0) {
-            e = cudaMemcpyAsync(out, dOut, outBytes, cudaMemcpyDeviceToHost, C.stream);
-            if (e != cudaSuccess) rc = cudaFail("spgpu_trace_host", e);
+        const size_t need = 2 * rayBytes + ((outBytes + 255) & ~size_t(255));
+        if (need > C.hostStageBytes) {
+            // grow geometrically so that a stream of single-ray calls allocates once
+            const size_t grow = std::max(need, std::max<size_t>(2 * C.hostStageBytes, size_t(1) << 16));
+            if (C.hostStage) {
+                e = cudaStreamSynchronize(C.stream);
+                if (e != cudaSuccess) return cudaFail("spgpu_trace_host", e);
+                cudaFree(C.hostStage);
+                C.hostStage = nullptr;
+                C.hostStageBytes = 0;
+            }
+            e = cudaMalloc(&C.hostStage, grow);
+            if (e != cudaSuccess) return cudaFail("spgpu_trace_host: staging buffer", e);
+            C.hostStageBytes = grow;
         }
-        cudaFreeAsync(dO, C.stream);
-        cudaFreeAsync(dD, C.stream);
-        cudaFreeAsync(dOut, C.stream);
-        if (rc == 0) rc = checkKernelError(C, C.stream);
-        return rc;
+        float *dO = reinterpret_cast<float *>(C.hostStage);
+        float *dD = reinterpret_cast<float *>(C.hostStage + rayBytes);
+        void *dOut = C.hostStage + 2 * rayBytes;
+        e = cudaMemcpyAsync(dO, org_tmin, rayBytes, cudaMemcpyHostToDevice, C.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dir_tmax, rayBytes, cudaMemcpyHostToDevice, C.stream);
+        if (e != cudaSuccess) return cudaFail("spgpu_trace_host", e);
+        int rc = launchTrace(C, any_hit, dO, dD, n, dOut, C.stream, false);
+        if (rc) return rc;
+        e = cudaMemcpyAsync(out, dOut, outBytes, cudaMemcpyDeviceToHost, C.stream);
+        if (e != cudaSuccess) return cudaFail("spgpu_trace_host", e);
+        return checkKernelError(C, C.stream);
     });
 }
 
 int spgpu_trace_host_noalloc(spgpu_ctx *h, int any_hit, const float *org_tmin, const float *dir_tmax, int64_t n,
                              void *out) {
-    NvtxRange nvtxRange("spgpu_trace_host_noalloc");
-    if (!h) {
-        setError("spgpu_trace_host_noalloc: null context");
-        return SPGPU_EINVAL;
-    }
-    Ctx &C = h->c;
-    if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
-        setError("spgpu_trace_host_noalloc: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    if (n > kNoAllocMaxRays) {
-        setError("spgpu_trace_host_noalloc: " + std::to_string(n) + " rays exceed the static scratch limit of " +
-                 std::to_string(kNoAllocMaxRays) + " rays per call (split the batch or use spgpu_trace_host)");
-        return SPGPU_EINVAL;
-    }
-    if (!C.bvhReady) {
-        setError("spgpu_trace_host_noalloc: no BVH (call spgpu_upload_scene and spgpu_build_bvh first)");
-        return SPGPU_ESTATE;
-    }
-    if (n == 0) return 0;
-    cudaSetDevice(C.device);
-    unsigned char *base = nullptr;
-    int rc = noallocScratch(C.device, &base);
-    if (rc) return rc;
-    int *ctl = reinterpret_cast<int *>(base);
-    float4 *dO = reinterpret_cast<float4 *>(base + kNoAllocCtlBytes);
-    float4 *dD = reinterpret_cast<float4 *>(base + kNoAllocCtlBytes + kNoAllocRayBytes);
-    unsigned char *dOut = base + kNoAllocCtlBytes + 2 * kNoAllocRayBytes;
-    const size_t rayBytes = static_cast<size_t>(n) * 16;
-    const size_t outBytes = static_cast<size_t>(n) * (any_hit ? 4 : 16);
-    cudaStream_t s = C.stream;
-    // the error flag and the ray counter start at zero
-    cudaError_t e = cudaMemsetAsync(ctl, 0, 2 * sizeof(int), s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dO, org_tmin, rayBytes, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dir_tmax, rayBytes, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc", e);
-    const int64_t blocksNeeded = (n + kTraceBlock - 1) / kTraceBlock;
-    const int grid = static_cast<int>(std::min<int64_t>(blocksNeeded, static_cast<int64_t>(residentTraceBlocks(C.device))));
-    const uint32_t NN = static_cast<uint32_t>(C.bvh.n_nodes), NT = static_cast<uint32_t>(C.bvh.ntri);
-    if (any_hit)
-        k_trace<true, false><<<grid, kTraceBlock, 0, s>>>(dO, dD, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN, NT,
-                                                          nullptr, reinterpret_cast<uint32_t *>(dOut), ctl, nullptr);
-    else
-        k_trace<false, false><<<grid, kTraceBlock, 0, s>>>(dO, dD, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN,
-                                                           NT, reinterpret_cast<spgpu_hit *>(dOut), nullptr, ctl,
-                                                           nullptr);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc: launch", e);
-    int flag = 0;
-    e = cudaMemcpyAsync(out, dOut, outBytes, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, ctl, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc", e);
-    if (flag) {
-        setError("spgpu_trace_host_noalloc: traversal stack overflow or malformed tree");
-        return SPGPU_EKERNEL;
-    }
-    return 0;
+    return guarded("spgpu_trace_host_noalloc", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_trace_host_noalloc");
+        if (!h) {
+            setError("spgpu_trace_host_noalloc: null context");
+            return SPGPU_EINVAL;
+        }
+        Ctx &C = h->c;
+        if (n < 0 || (n > 0 && (!org_tmin || !dir_tmax || !out))) {
+            setError("spgpu_trace_host_noalloc: invalid arguments");
+            return SPGPU_EINVAL;
+        }
+        if (n > kNoAllocMaxRays) {
+            setError("spgpu_trace_host_noalloc: " + std::to_string(n) + " rays exceed the static scratch limit of " +
+                     std::to_string(kNoAllocMaxRays) + " rays per call (split the batch or use spgpu_trace_host)");
+            return SPGPU_EINVAL;
+        }
+        if (!C.bvhReady) {
+            setError("spgpu_trace_host_noalloc: no BVH (call spgpu_upload_scene and spgpu_build_bvh first)");
+            return SPGPU_ESTATE;
+        }
+        if (n == 0) return 0;
+        cudaError_t e = cudaSetDevice(C.device);
+        if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc: cudaSetDevice", e);
+        unsigned char *base = nullptr;
+        int rc = noallocScratch(C.device, &base);
+        if (rc) return rc;
+        int *ctl = reinterpret_cast<int *>(base);
+        float4 *dO = reinterpret_cast<float4 *>(base + kNoAllocCtlBytes);
+        float4 *dD = reinterpret_cast<float4 *>(base + kNoAllocCtlBytes + kNoAllocRayBytes);
+        unsigned char *dOut = base + kNoAllocCtlBytes + 2 * kNoAllocRayBytes;
+        const size_t rayBytes = static_cast<size_t>(n) * 16;
+        const size_t outBytes = static_cast<size_t>(n) * (any_hit ? 4 : 16);
+        cudaStream_t s = C.stream;
+        // the error flag and the ray counter start at zero
+        e = cudaMemsetAsync(ctl, 0, 2 * sizeof(int), s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dO, org_tmin, rayBytes, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dir_tmax, rayBytes, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc", e);
+        const int64_t blocksNeeded = (n + kTraceBlock - 1) / kTraceBlock;
+        const int grid = static_cast<int>(std::min<int64_t>(blocksNeeded, static_cast<int64_t>(residentTraceBlocks(C.device))));
+        const uint32_t NN = static_cast<uint32_t>(C.bvh.n_nodes), NT = static_cast<uint32_t>(C.bvh.ntri);
+        if (any_hit)
+            k_trace<true, false><<<grid, kTraceBlock, 0, s>>>(dO, dD, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN, NT,
+                                                              nullptr, reinterpret_cast<uint32_t *>(dOut), ctl, nullptr);
+        else
+            k_trace<false, false><<<grid, kTraceBlock, 0, s>>>(dO, dD, static_cast<int>(n), C.bvh.nodes, C.bvh.tris, NN,
+                                                               NT, reinterpret_cast<spgpu_hit *>(dOut), nullptr, ctl,
+                                                               nullptr);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc: launch", e);
+        int flag = 0;
+        e = cudaMemcpyAsync(out, dOut, outBytes, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, ctl, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cudaFail("spgpu_trace_host_noalloc", e);
+        if (flag) {
+            setError("spgpu_trace_host_noalloc: traversal stack overflow or malformed tree");
+            return SPGPU_EKERNEL;
+        }
+        return 0;
+    });
 }
 
 int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_render_stats *stats, void *stream) {

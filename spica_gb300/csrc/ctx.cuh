@@ -3,6 +3,9 @@
 #pragma once
 
 #include <cstdint>
+#include <exception>
+#include <mutex>
+#include <new>
 #include <string>
 
 #include <nvtx3/nvToolsExt.h>
@@ -108,6 +111,12 @@ struct Ctx {
     // ray-batch scratch
     int *traceErr = nullptr;
     unsigned long long *traceStats = nullptr;
+    // spgpu_trace_host: calls on one context from several host threads (the reference
+    // calls Accelerator::intersect from every render thread) take this lock, because they
+    // share traceErr, the ray counter behind it and the staging buffer below
+    std::mutex hostTraceMu;
+    unsigned char *hostStage = nullptr;   // rays in, hits out; grown on demand, kept
+    size_t hostStageBytes = 0;
     // renderer
     // Render pass lanes: consecutive sample passes alternate between kPassLanes queue
     // sets (each with its own pass graph), lane k > 0 on laneStream[k - 1], so one
@@ -152,6 +161,26 @@ struct NvtxRange {
 
 void setError(const std::string &msg);
 int cudaFail(const char *what, cudaError_t e);
+
+// Runs the body of a C entry point so that no C++ exception crosses the C ABI: a failed
+// host allocation becomes SPGPU_ENOMEM, any other exception SPGPU_EINVAL, each with a
+// message.
+template <class F>
+int guarded(const char *name, F &&body) noexcept {
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        setError(std::string(name) + ": out of host memory");
+        return SPGPU_ENOMEM;
+    } catch (const std::exception &e) {
+        setError(std::string(name) + ": " + e.what());
+        return SPGPU_EINVAL;
+    }
+}
+
+// C-ABI material records (SPGPU_MAT_*, 8 floats each) as device records; `who` names
+// the entry point in error messages
+int materialRecords(const char *who, const float *materials, int nmat, std::vector<MaterialRecord> *out);
 void freeRenderQueues(RenderQueues *q);
 
 // camera matrices of the reference's PerspectiveCamera, computed in double on the

@@ -175,7 +175,8 @@ EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version",
            "spgpu_render", "spgpu_render_host", "spgpu_render_profile", "spgpu_batch_prepare",
            "spgpu_batch_film_pixels", "spgpu_batch_run", "spgpu_guiding_init", "spgpu_guiding_render",
            "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_ring", "spgpu_guiding_params", "spgpu_guiding_mlp",
-           "spgpu_guiding_grad", "spgpu_scene_load", "spgpu_scene_free", "spgpu_load_hdr"]
+           "spgpu_guiding_grad", "spgpu_scene_load", "spgpu_scene_free", "spgpu_load_hdr", "spgpu_bsdf_eval",
+           "spgpu_bsdf_sample", "spgpu_sampler_generate"]
 
 _lib = None
 
@@ -223,6 +224,9 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_guiding_params.argtypes = [vp, vp, i32]
     lib.spgpu_guiding_mlp.argtypes = [vp, vp, i32, vp, vp]
     lib.spgpu_guiding_grad.argtypes = [vp, vp, i32, vp, C.POINTER(C.c_double), vp]
+    lib.spgpu_bsdf_eval.argtypes = [vp, vp, i64, vp, vp, vp, vp]
+    lib.spgpu_bsdf_sample.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp]
+    lib.spgpu_sampler_generate.argtypes = [vp, i64, vp, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("spgpu_destroy", "spgpu_last_error", "spgpu_version"):
             getattr(lib, name).restype = C.c_int
@@ -364,6 +368,129 @@ def _pack_rays(org, dir, tmax=None, tmin=None):
     dt[:, :3] = dir
     dt[:, 3] = 1.0e32 if tmax is None else tmax
     return ot, dt
+
+
+class GpuBSDF:
+    """One material's BSDF on the device, function by function (spgpu_bsdf_eval /
+    spgpu_bsdf_sample): BSDF::f, BSDF::pdf and BSDF::sample (core/bsdf.cc:49-136) in
+    the shading frame (z = shading normal).  material: 8-float SPGPU_MAT_* record."""
+
+    def __init__(self, material, ctx: Optional[Context] = None, device: int = 0):
+        self.ctx = ctx or Context(device)
+        self.material = np.ascontiguousarray(material, np.float32).reshape(8)
+
+    def f_pdf(self, wo, wi):
+        """(f (n, 3), pdf (n,)) for directions wo, wi (n, 3)."""
+        wo = np.ascontiguousarray(wo, np.float32).reshape(-1, 3)
+        wi = np.ascontiguousarray(wi, np.float32).reshape(-1, 3)
+        n = wo.shape[0]
+        f = np.zeros((n, 3), np.float32)
+        pdf = np.zeros(n, np.float32)
+        _check(self.ctx.lib.spgpu_bsdf_eval(self.ctx.h, self.material.ctypes.data, n, wo.ctypes.data, wi.ctypes.data,
+                                            f.ctypes.data, pdf.ctypes.data), "spgpu_bsdf_eval")
+        return f, pdf
+
+    def sample(self, wo, u):
+        """BSDF::sample for directions wo (n, 3) and numbers u (n, 3): the 2D sample and
+        the draw the reference's rough dielectric and plastic take from their own
+        generator.  Returns (wi, f, pdf, type)."""
+        wo = np.ascontiguousarray(wo, np.float32).reshape(-1, 3)
+        u = np.ascontiguousarray(u, np.float32).reshape(-1, 3)
+        n = wo.shape[0]
+        wi = np.zeros((n, 3), np.float32)
+        f = np.zeros((n, 3), np.float32)
+        pdf = np.zeros(n, np.float32)
+        t = np.zeros(n, np.int32)
+        _check(self.ctx.lib.spgpu_bsdf_sample(self.ctx.h, self.material.ctypes.data, n, wo.ctypes.data, u.ctypes.data,
+                                              wi.ctypes.data, f.ctypes.data, pdf.ctypes.data, t.ctypes.data),
+               "spgpu_bsdf_sample")
+        return wi, f, pdf, t
+
+
+def philox(counter, key, ctx: Optional[Context] = None):
+    """Philox4x32-10 on the device (spgpu_sampler_generate): counter (n, 4) and key (n, 2)
+    uint32 -> (raw words (n, 4) uint32, uniforms (n, 4) float32 in [0, 1))."""
+    ctx = ctx or Context()
+    c = np.ascontiguousarray(counter, np.uint32).reshape(-1, 4)
+    k = np.ascontiguousarray(key, np.uint32).reshape(-1, 2)
+    if c.shape[0] != k.shape[0]:
+        raise ValueError("counter and key need the same number of rows")
+    raw = np.zeros_like(c)
+    u = np.zeros(c.shape, np.float32)
+    _check(ctx.lib.spgpu_sampler_generate(ctx.h, c.shape[0], c.ctypes.data, k.ctypes.data, raw.ctypes.data,
+                                          u.ctypes.data), "spgpu_sampler_generate")
+    return raw, u
+
+
+CAMERA_BOUNCE = 0xFFFF   # the bounce word of the camera ray's counter
+STREAM_TAG = 0x5350      # the fourth counter word of every renderer draw
+
+
+class GpuSampler:
+    """The renderer's random numbers behind the reference's Sampler interface
+    (core/sampler.h:24-37: startPixel, startNextSample, get1D, get2D, clone).  The
+    reference's Independent sampler (samplers/independent.cc:6-23) reads one MT19937
+    stream per thread; here every (seed, film pixel, sample index) has its own
+    Philox4x32-10 stream, so a pixel's numbers do not depend on which thread draws them.
+    Dimensions run in the renderer's order: dimensions 0-3 are the camera block
+    (bounce word 0xFFFF, stream 0: film x, film y, then two unused lens numbers), and
+    dimension 4 + k is lane k % 4 of stream (k // 4) % 4 at bounce k // 16."""
+
+    BLOCKS = 16   # counter blocks fetched per device call
+
+    def __init__(self, seed: int = 0, ctx: Optional[Context] = None, width: Optional[int] = None):
+        self.seed = int(seed) & 0xFFFFFFFF
+        self.ctx = ctx
+        self.width = width
+        self.pixel = 0
+        self.sample = -1
+        self.dim = 0
+        self._cache = {}
+
+    def clone(self, seed: int) -> "GpuSampler":
+        return GpuSampler(seed, ctx=self.ctx, width=self.width)
+
+    def startPixel(self, x: int, y: int = 0):
+        """Select the film pixel (x, y) of a film `width` wide (the key is the film's pixel
+        index y * width + x); with no width, x is the film pixel index itself."""
+        self.pixel = int(y) * int(self.width) + int(x) if self.width else int(x)
+        self.sample = -1
+        self.dim = 0
+        self._cache = {}
+
+    def startNextSample(self):
+        self.sample += 1
+        self.dim = 0
+        self._cache = {}
+
+    @staticmethod
+    def block_of(dim: int):
+        """(bounce word, stream, lane) of a dimension."""
+        if dim < 4:
+            return CAMERA_BOUNCE, 0, dim
+        k = dim - 4
+        return k // 16, (k // 4) % 4, k % 4
+
+    def _block(self, b: int):
+        if b not in self._cache:
+            if self.ctx is None:
+                self.ctx = Context()
+            blocks = range(b, b + self.BLOCKS)
+            ctr = np.array([[max(self.sample, 0), *self.block_of(4 * j)[:2], STREAM_TAG] for j in blocks], np.uint32)
+            key = np.tile(np.array([self.seed, self.pixel], np.uint32), (len(blocks), 1))
+            _, u = philox(ctr, key, self.ctx)
+            for j, row in zip(blocks, u):
+                self._cache[j] = row
+        return self._cache[b]
+
+    def get1D(self) -> float:
+        v = float(self._block(self.dim // 4)[self.dim % 4])
+        self.dim += 1
+        return v
+
+    def get2D(self):
+        a = self.get1D()
+        return a, self.get1D()
 
 
 class GpuPathIntegrator:

@@ -7,7 +7,10 @@
 // hands it to BVHAccel.  Single-ray intersect() calls go through the host entry point
 // one ray at a time and then let the owning primitive rebuild the SurfaceInteraction
 // in double, so callers see the same interaction object as with BVHAccel; batched
-// callers should use spgpu_trace on device buffers instead.
+// callers should use spgpu_trace on device buffers instead.  The reference calls
+// intersect() from every parallel_for thread (core/integrator.cc:77); spgpu_trace_host
+// serialises those calls on the context (they share its control words and staging
+// buffer), so the plugin is safe under that caller.
 #include "core/cobject.h"
 #undef SPICA_EXPORT_PLUGIN
 #define SPICA_EXPORT_PLUGIN(name, descr)

@@ -116,3 +116,48 @@ def zscores(mean_a, var_a, mean_b, var_b):
     z[(v == 0) & (mean_a == mean_b)] = 0.0
     z[(v == 0) & (mean_a != mean_b)] = np.inf
     return z
+
+
+# ---------------------------------------------------------------- BSDFs, function by function
+BSDF_REL_TOL = 1e-4     # f and pdf, relative to the oracle
+WI_ABS_TOL = 1e-5       # sampled unit directions, per component
+BSDF_ABS_FLOOR = 1e-7   # values below this fraction of the table's largest are compared absolutely
+ULP_STEPS = 4           # input perturbation of the conditioning test, in float32 ulps
+
+
+def bsdf_mismatch(f, pdf, fr, pr, rel=BSDF_REL_TOL):
+    """Rows where f (n, 3) or pdf (n,) differ from the oracle's fr, pr by more than rel
+    relative (with an absolute floor of BSDF_ABS_FLOOR times the largest oracle value)."""
+    f, pdf, fr, pr = (np.asarray(a, np.float64) for a in (f, pdf, fr, pr))
+    fa = BSDF_ABS_FLOOR * max(float(np.abs(fr).max(initial=0.0)), 1e-30)
+    pa = BSDF_ABS_FLOOR * max(float(np.abs(pr).max(initial=0.0)), 1e-30)
+    bad_f = (np.abs(f - fr) > rel * np.abs(fr) + fa).any(axis=1)
+    bad_p = np.abs(pdf - pr) > rel * np.abs(pr) + pa
+    return bad_f | bad_p
+
+
+def bsdf_conditioning(oracle, inputs, rows, fr, pr, wr=None, sr=None, trials=8, seed=0):
+    """Stated FP32 ties among the flagged rows: the oracle's output (f, pdf and, for
+    sampling, the direction and type) moves beyond the contract's tolerance when every
+    input component moves by up to ULP_STEPS float32 ulps.  oracle(*inputs) returns
+    (f, pdf) or (f, pdf, wi, type)."""
+    idx = np.nonzero(rows)[0]
+    tie = np.zeros(rows.shape[0], bool)
+    if idx.size == 0:
+        return tie
+    rng = np.random.default_rng(seed)
+    sub = [np.asarray(x, np.float64)[idx] for x in inputs]
+    base_f, base_p = fr[idx], pr[idx]
+    for _ in range(trials):
+        pert = []
+        for x in sub:
+            ulp = np.spacing(np.abs(x).astype(np.float32)).astype(np.float64)
+            pert.append(x + ULP_STEPS * ulp * rng.choice([-1.0, 1.0], size=x.shape))
+        out = oracle(*pert)
+        moved = bsdf_mismatch(out[0], out[1], base_f, base_p)
+        if wr is not None:
+            both = (out[1] > 0) & (base_p > 0)
+            moved |= both & (np.abs(out[2] - wr[idx]).max(axis=1) > WI_ABS_TOL)
+            moved |= out[3] != sr[idx]
+        tie[idx[moved]] = True
+    return tie

@@ -78,6 +78,9 @@ _NULL_CALLS = [
     ("spgpu_write_png", (None, None, 0, 0)),
     ("spgpu_scene_load", (None, None)),
     ("spgpu_load_hdr", (None, None, 0, None, None)),
+    ("spgpu_bsdf_eval", (None, None, 0, None, None, None, None)),
+    ("spgpu_bsdf_sample", (None, None, 0, None, None, None, None, None, None)),
+    ("spgpu_sampler_generate", (None, 0, None, None, None, None)),
 ]
 
 

@@ -1,0 +1,151 @@
+"""Parity on the benchmark workloads themselves, against the oracle (the restatement that
+tests/test_oracle.py pins bit for bit to the compiled reference):
+
+  * the 2.03M-triangle mid-scale scene at 1920 x 1080, max depth 16 (the bench's
+    workload): the GPU's full frame against oracle renders of four film windows,
+    PathIntegrator::Li (integrators/path/path.cc:42-125) with the environment map
+    (lights/envmap.cc:17-134) and the area lights;
+  * the whole ray-intersection workload: 1,048,576 triangles, 8M coherent and 8M
+    incoherent rays, closest and any hit (BVHAccel::intersect, accelerators/bvh.cc:
+    315-388);
+  * batched renders: three seeded box-room variants rendered by the persistent batch
+    launch (spgpu_batch_run), each against the oracle's render of the same variant;
+  * a scene file: the box room written in the reference's XML format and loaded by
+    spgpu_scene_load, against the compiled reference's own render of the box room
+    (tests/golden/render_boxroom.npz).
+
+Image rule (tests/parity.py): per pixel and channel the means agree within 3 sigma for
+all but 1 % of the values, sigma from independent batch means on both sides; the
+window means agree within 3 standard errors.  Trace rule: primitive ids identical
+except stated FP32 ties, t within 1e-5 relative.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from parity import classify_any, classify_closest, zscores
+from spica_gb300 import GpuBatch, GpuBVHAccel, GpuPathIntegrator, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _assert_images_agree(mg, vg, mr, vr, what):
+    z = zscores(mg, vg, mr, vr)
+    frac = float((np.abs(z) > 3).mean())
+    worst = np.unravel_index(np.argmax(np.abs(z)), z.shape)
+    assert frac < 0.01, (what, frac, float(np.abs(z).max()), float(z.mean()), worst, float(mg[worst]), float(mr[worst]))
+    se = np.sqrt(vg.sum() + vr.sum()) / z.size
+    assert abs(mg.mean() - mr.mean()) < 3 * se + 1e-6, (what, mg.mean(), mr.mean(), se)
+
+
+def _moments(batch_means):
+    m = np.stack(batch_means)
+    return m.mean(0), m.var(0, ddof=1) / m.shape[0]
+
+
+# film windows (x0, y0, w, h) of the mid-scale frame: ground, instances, horizon, sky
+MID_WINDOWS = [(472, 700, 16, 16), (952, 532, 16, 16), (1400, 600, 16, 16), (240, 300, 16, 16)]
+
+
+def test_midscale_frame_vs_oracle_windows(gpulib, port):
+    sc = scenes.mid_scale()
+    W, H, md = sc.width, sc.height, sc.max_depth
+    batches, spp = 32, 64
+    acc = GpuBVHAccel(sc).construct()
+    integ = GpuPathIntegrator(seed=77)
+    film = np.zeros((H, W, 4), np.float32)
+    gpu = {w: [] for w in MID_WINDOWS}
+    for k in range(batches):
+        film[:] = 0
+        integ.render(sc.camera, acc, {"width": W, "height": H, "maxDepth": md, "sampleCount": spp}, film=film,
+                     sample_offset=k * spp)
+        assert np.all(film[..., 3] == spp)
+        for (x0, y0, w, h) in MID_WINDOWS:
+            gpu[(x0, y0, w, h)].append(film[y0:y0 + h, x0:x0 + w, :3] / spp)
+    o = port.scene(sc)
+    for win in MID_WINDOWS:
+        ref = [o.render(sc.camera, W, H, spp, md, seed=5000 + k, window=win)[0] / spp for k in range(batches)]
+        mg, vg = _moments(gpu[win])
+        mr, vr = _moments(ref)
+        assert mr.max() > 0
+        _assert_images_agree(mg, vg, mr, vr, ("mid-scale window", win))
+
+
+def test_full_microbench_ray_set_vs_oracle(gpulib, port):
+    """All 16,777,216 rays of the intersection microbench (8M pinhole rays at 4096 x 2048
+    and 8M rays from U(box) in U(S^2) directions) on the 1,048,576-triangle displaced
+    sphere: closest hit and any hit (tmax U[0, 2r])."""
+    sph = scenes.displaced_sphere(levels=9, seed=0)
+    assert sph.ntri == 1 << 20
+    org, d, tmax = scenes.microbench_rays(sph, 1 << 23, 1 << 23, 4096, 2048, seed=0)
+    assert org.shape[0] == 1 << 24
+    acc = GpuBVHAccel(sph).construct()
+    prim, t, _, _ = acc.intersect(org, d)
+    o = port.scene(sph)
+    o64, d64 = org.astype(np.float64), d.astype(np.float64)
+    pr, tr = o.trace(o64, d64)
+    r = classify_closest(sph.verts, org, d, prim, t, pr, tr)
+    assert r["fail"] == 0 and r["t_fail"] == 0, r
+    assert r["equal"] >= 0.999 * r["total"], r
+    assert (pr >= 0).mean() > 0.3
+    h = acc.intersect_any(org, d, tmax)
+    hr = o.trace(o64, d64, tmax.astype(np.float64), any_hit=True)
+    ra = classify_any(sph.verts, org, d, tmax, h, hr, pr, tr, prim, t)
+    assert ra["fail"] == 0, ra
+    assert ra["mismatch"] <= 1e-4 * ra["total"], ra
+
+
+def test_batched_variants_vs_oracle(gpulib, port):
+    """Three seeded box-room variants (their own wall albedos and light offsets, films of
+    32 x 32 to 64 x 64) through the persistent batch launch, 16 independent batches of
+    32 samples per pixel, against the oracle's renders of each variant."""
+    import torch
+    vs = scenes.batch_variants(3, seed=12)
+    for k, v in enumerate(vs):
+        v.width = v.height = 32 + 16 * k
+        v.spp = 32
+    batches = 16
+    per = [[] for _ in vs]
+    for s in range(batches):
+        b = GpuBatch(vs, seed=300 + s, autotune=False)
+        films = torch.zeros((b.pixels, 4), dtype=torch.float32, device="cuda")
+        b.run(films)
+        torch.cuda.synchronize()
+        host = films.cpu().numpy()
+        for i, v in enumerate(vs):
+            f = b.film(host, i)
+            assert np.all(f[..., 3] == v.spp)
+            per[i].append(f[..., :3] / v.spp)
+    for i, v in enumerate(vs):
+        o = port.scene(v)
+        ref = [o.render(v.camera, v.width, v.height, v.spp, v.max_depth, seed=900 + s)[0] / v.spp
+               for s in range(batches)]
+        mg, vg = _moments(per[i])
+        mr, vr = _moments(ref)
+        _assert_images_agree(mg, vg, mr, vr, ("batch variant", i))
+
+
+def test_scene_file_box_room_vs_reference_render(gpulib, tmp_path):
+    """The box room as an XML scene file with PLY meshes, loaded by spgpu_scene_load and
+    rendered on the GPU, against the compiled reference's render of the box room."""
+    from spica_gb300.gpu import load_scene
+    from test_render_gpu import ref_moments
+    from test_scene_file import scene_to_files
+    g = np.load(os.path.join(GOLDEN, "render_boxroom.npz"))
+    W, H, md = int(g["W"]), int(g["H"]), int(g["max_depth"])
+    sc = scenes.box_room(width=W, height=H, max_depth=md)
+    got, integ = load_scene(scene_to_files(sc, tmp_path / "box"))
+    assert integ == "path" and (got.width, got.height, got.max_depth) == (W, H, md)
+    np.testing.assert_allclose(np.asarray(got.camera, np.float64), g["camera"], rtol=1e-6, atol=1e-6)
+    acc = GpuBVHAccel(got).construct()
+    gi = GpuPathIntegrator(seed=31)
+    means = []
+    for k in range(16):
+        f = gi.render(got.camera, acc, {"width": W, "height": H, "maxDepth": md, "sampleCount": 512},
+                      sample_offset=512 * k)
+        means.append(f[..., :3] / 512)
+    mg, vg = _moments(means)
+    mr, vr = ref_moments(g)
+    _assert_images_agree(mg, vg, mr, vr, "scene-file box room")

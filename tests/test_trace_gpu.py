@@ -140,3 +140,46 @@ def test_invalid_arguments_raise(gpulib):
     bad.tri_mat = np.array([5], np.int32)
     with pytest.raises(SpgpuError):
         ctx.upload_scene(bad)    # material index out of range
+
+
+def test_host_trace_from_many_threads(gpulib):
+    """spgpu_trace_host called on one context from eight host threads at once, as the
+    reference calls Accelerator::intersect from every render thread
+    (core/integrator.cc:77): batches of 1 to 4096 rays, closest and any hit, each
+    result identical to the same call made alone."""
+    import threading
+    sph = scenes.displaced_sphere(levels=6, seed=2)
+    org, d, tmax = scenes.microbench_rays(sph, 20000, 20000, 256, 128, seed=4)
+    acc = GpuBVHAccel(sph).construct()
+    rng = np.random.default_rng(8)
+    jobs = []
+    i = 0
+    while i < org.shape[0]:
+        n = int(rng.choice([1, 1, 1, 7, 64, 4096]))
+        jobs.append((i, min(i + n, org.shape[0]), bool(rng.integers(0, 2))))
+        i += n
+    alone = {}
+    for a, b, anyh in jobs:
+        alone[a] = acc.intersect_any(org[a:b], d[a:b], tmax[a:b]) if anyh else acc.intersect(org[a:b], d[a:b])[:2]
+    got, errors = {}, []
+
+    def worker(my):
+        try:
+            for a, b, anyh in my:
+                got[a] = (acc.intersect_any(org[a:b], d[a:b], tmax[a:b]) if anyh
+                          else acc.intersect(org[a:b], d[a:b])[:2])
+        except Exception as e:   # noqa: BLE001 -- reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(jobs[k::8],)) for k in range(8)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    assert len(got) == len(jobs)
+    for a, b, anyh in jobs:
+        if anyh:
+            assert np.array_equal(got[a], alone[a])
+        else:
+            assert np.array_equal(got[a][0], alone[a][0]) and np.array_equal(got[a][1], alone[a][1])
