@@ -196,7 +196,9 @@ struct alignas(16) MaterialRecord {
 };
 
 __device__ __forceinline__ float cos2T(float3 w) { return w.z * w.z; }
-__device__ __forceinline__ float sin2T(float3 w) { return fmaxf(0.0f, 1.0f - w.z * w.z); }
+// sin^2 of a unit vector from its x and y (the reference's 1 - cos^2 in double): in
+// float32, 1 - z^2 keeps few digits near the normal, where sharp lobes are evaluated
+__device__ __forceinline__ float sin2T(float3 w) { return fminf(1.0f, w.x * w.x + w.y * w.y); }
 __device__ __forceinline__ float tan2T(float3 w) { return sin2T(w) / (cos2T(w) + kEpsT); }
 
 // concentric disk, cosine hemisphere (core/sampling.cc:151-179)
@@ -275,7 +277,10 @@ __device__ __forceinline__ float ggxLambda(float3 w, float a) {
 // visible-normal sampling, Heitz and d'Eon, "Importance Sampling Microfacet-Based
 // BSDFs using the Distribution of Visible Normals" (EGSR 2014): stretch, sample the
 // slopes of the unit-roughness distribution, rotate, unstretch.
-__device__ __forceinline__ void ggxSample11(float cosTheta, float u0, float u1, float *sx, float *sy) {
+// sinTheta is passed in, computed from the direction's x and y: 1 - cos^2 would lose
+// most of its float32 digits near normal incidence.
+__device__ __forceinline__ void ggxSample11(float cosTheta, float sinTheta, float u0, float u1, float *sx,
+                                           float *sy) {
     if (cosTheta > 0.9999f) {
         const float r = sqrtf(u0 / (1.0f - u0));
         float s, c;
@@ -284,12 +289,12 @@ __device__ __forceinline__ void ggxSample11(float cosTheta, float u0, float u1, 
         *sy = r * s;
         return;
     }
-    const float sinTheta = sqrtf(fmaxf(0.0f, 1.0f - cosTheta * cosTheta));
     const float tanTheta = sinTheta / cosTheta;
     const float a = 1.0f / tanTheta;
     const float G1 = 2.0f / (1.0f + sqrtf(1.0f + 1.0f / (a * a)));
-    const float A = 2.0f * u0 / G1 - 1.0f;
-    float tmp = 1.0f / (A * A - 1.0f);
+    const float Ap1 = 2.0f * u0 / G1;   // A + 1, so that A^2 - 1 = (A + 1)(A - 1) keeps its digits
+    const float A = Ap1 - 1.0f;
+    float tmp = 1.0f / (Ap1 * (Ap1 - 2.0f));
     if (tmp > 1.0e10f) tmp = 1.0e10f;
     const float B = tanTheta;
     const float D = sqrtf(fmaxf(0.0f, B * B * tmp * tmp - (A * A - B * B) * tmp));
@@ -365,7 +370,8 @@ __device__ __forceinline__ float beckLambda(float3 w, float a) {
 }
 // slopes of the unit-roughness distribution seen from cosThetaI: Jakob's inversion of
 // the slope CDF by bisection / Newton steps (at most 16)
-__device__ __forceinline__ void beckSample11(float cosThetaI, float U1, float U2, float *sx, float *sy) {
+__device__ __forceinline__ void beckSample11(float cosThetaI, float sinThetaI, float U1, float U2, float *sx,
+                                            float *sy) {
     if (cosThetaI > 0.9999f) {
         const float r = sqrtf(-logf(1.0f - U1));
         float s, c;
@@ -374,14 +380,15 @@ __device__ __forceinline__ void beckSample11(float cosThetaI, float U1, float U2
         *sy = r * s;
         return;
     }
-    const float sinThetaI = sqrtf(fmaxf(0.0f, 1.0f - cosThetaI * cosThetaI));
     const float tanThetaI = sinThetaI / cosThetaI;
     const float cotThetaI = 1.0f / tanThetaI;
     float a = -1.0f, c = refErff(cotThetaI);
     const float samplex = fmaxf(U1, 1.0e-6f);
-    const float thetaI = acosf(cosThetaI);
+    const float thetaI = atan2f(sinThetaI, cosThetaI);   // acos loses digits near normal incidence
     const float fit = 1.0f + thetaI * (-0.876f + thetaI * (0.4265f - 0.0594f * thetaI));
-    float b = c - (1.0f + c) * powf(1.0f - samplex, fit);
+    // b = c - (1 + c) (1 - samplex)^fit, written as (1 + c)(1 - (1 - samplex)^fit) - 1 so
+    // that small samples keep their digits
+    float b = (1.0f + c) * -expm1f(fit * log1pf(-samplex)) - 1.0f;
     const float sqrtPiInv = 0.5641895835f;   // 1 / sqrt(pi)
     const float norm = 1.0f / (1.0f + c + sqrtPiInv * tanThetaI * expf(-cotThetaI * cotThetaI));
     for (int it = 0; it < 16; it++) {
@@ -403,10 +410,10 @@ __device__ __forceinline__ float3 visibleNormal(float3 wo, float a, float u0, fl
     const bool flip = wo.z < 0.0f;
     const float3 w = flip ? -wo : wo;
     const float3 ws = normalize(mk(a * w.x, a * w.y, w.z));
+    const float st = sqrtf(ws.x * ws.x + ws.y * ws.y);
     float sx, sy;
-    if (BECKMANN) beckSample11(ws.z, u0, u1, &sx, &sy);
-    else ggxSample11(ws.z, u0, u1, &sx, &sy);
-    const float st = sqrtf(fmaxf(0.0f, 1.0f - ws.z * ws.z));
+    if (BECKMANN) beckSample11(ws.z, st, u0, u1, &sx, &sy);
+    else ggxSample11(ws.z, st, u0, u1, &sx, &sy);
     const float cp = st == 0.0f ? 1.0f : clampf(ws.x / st, -1.0f, 1.0f);
     const float sp = st == 0.0f ? 0.0f : clampf(ws.y / st, -1.0f, 1.0f);
     const float tmp = cp * sx - sp * sy;
@@ -562,26 +569,26 @@ __device__ __forceinline__ float3 bsdfF(const MaterialRecord &m, float3 wo, floa
 }
 __device__ __forceinline__ float bsdfPdf(const MaterialRecord &m, float3 wo, float3 wi) {
     if (m.type == kMatRoughDielectric) return mtPdf(m, wo, wi, mtHalf(m, wo, wi));
+    if (m.type == kMatPlastic) {   // PlasticBRDF::pdf (plastic.cc:69) tests no hemisphere
+        const float ps = plasticProbSpecular(m, wo);
+        return plasticMirror(wi) ? ps : (1.0f - ps) * fabsf(wi.z) * kInvPi;
+    }
     if (wo.z * wi.z <= 0.0f) return 0.0f;
     if (m.type == kMatLambert) return fabsf(wi.z) * kInvPi;
     if (m.type == kMatConductor) {
         const float3 wh = normalize(wo + wi);
         return condPdf(m, wo, wh) / (4.0f * dot(wo, wh));
     }
-    if (m.type == kMatPlastic) {
-        const float ps = plasticProbSpecular(m, wo);
-        return plasticMirror(wi) ? ps : (1.0f - ps) * fabsf(wi.z) * kInvPi;
-    }
     return 0.0f;
 }
 __device__ __forceinline__ float bsdfPdfDielectricCone(const MaterialRecord &m, float3 wo, float3 wi) {
     return dielectricCone(m, wo, wi);   // FresnelSpecular::pdf (bxdf.cc:236): F or 1 - F inside the cones
 }
-// BSDF::sample for the material's BxDF; returns f, sets wi, pdf and the sampled type
-// bits.  uc is the draw the reference takes from its BxDFs' hidden generator
-// (core/bxdf.cc:18, bsdfs/plastic.cc:18): the rough dielectric's reflect / refract and
-// the plastic's specular / diffuse choice.
-__device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo, float u0, float u1, float uc,
+// The material's BxDF::sample; returns f, sets wi, pdf and the sampled type bits.  uc is
+// the draw the reference takes from its BxDFs' hidden generator (core/bxdf.cc:18,
+// bsdfs/plastic.cc:18): the rough dielectric's reflect / refract and the plastic's
+// specular / diffuse choice.
+__device__ __forceinline__ float3 bxdfSample(const MaterialRecord &m, float3 wo, float u0, float u1, float uc,
                                              float3 *wi, float *pdf, int *type) {
     *pdf = 0.0f;
     *type = 0;
@@ -659,6 +666,18 @@ __device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo,
     *type = kSpecular | kTransmission;
     const float ft = (1.0f - F) * ((eI * eI) / (eT * eT));
     return mk(ft, ft, ft) / fabsf(w.z);
+}
+
+// BSDF::sample (core/bsdf.cc:65-110) over the material's one BxDF: a sample of pdf 0 is
+// no sample (type 0, f 0)
+__device__ __forceinline__ float3 bsdfSample(const MaterialRecord &m, float3 wo, float u0, float u1, float uc,
+                                             float3 *wi, float *pdf, int *type) {
+    const float3 f = bxdfSample(m, wo, u0, u1, uc, wi, pdf, type);
+    if (*pdf == 0.0f) {
+        *type = 0;
+        return mk(0, 0, 0);
+    }
+    return f;
 }
 
 // wavefront shading class (sort key of the material-sorted queues): 0 diffuse, 1 glossy,

@@ -136,11 +136,16 @@ def bsdf_mismatch(f, pdf, fr, pr, rel=BSDF_REL_TOL):
     return bad_f | bad_p
 
 
-def bsdf_conditioning(oracle, inputs, rows, fr, pr, wr=None, sr=None, trials=8, seed=0):
+BECKMANN_CDF_TOL = 1e-6   # the Beckmann slope inversion stops within this of its target (core/microfacet.cc:120)
+
+
+def bsdf_conditioning(oracle, inputs, rows, fr, pr, wr=None, sr=None, trials=8, seed=0, abs_tol=None):
     """Stated FP32 ties among the flagged rows: the oracle's output (f, pdf and, for
     sampling, the direction and type) moves beyond the contract's tolerance when every
-    input component moves by up to ULP_STEPS float32 ulps.  oracle(*inputs) returns
-    (f, pdf) or (f, pdf, wi, type)."""
+    input component moves by up to ULP_STEPS float32 ulps, or by abs_tol[k] (absolute,
+    per input k; e.g. BECKMANN_CDF_TOL on the first random number of a Beckmann sampler,
+    whose result the reference itself defines only to that tolerance).  oracle(*inputs)
+    returns (f, pdf) or (f, pdf, wi, type)."""
     idx = np.nonzero(rows)[0]
     tie = np.zeros(rows.shape[0], bool)
     if idx.size == 0:
@@ -150,9 +155,11 @@ def bsdf_conditioning(oracle, inputs, rows, fr, pr, wr=None, sr=None, trials=8, 
     base_f, base_p = fr[idx], pr[idx]
     for _ in range(trials):
         pert = []
-        for x in sub:
-            ulp = np.spacing(np.abs(x).astype(np.float32)).astype(np.float64)
-            pert.append(x + ULP_STEPS * ulp * rng.choice([-1.0, 1.0], size=x.shape))
+        for k, x in enumerate(sub):
+            step = ULP_STEPS * np.spacing(np.abs(x).astype(np.float32)).astype(np.float64)
+            if abs_tol is not None and abs_tol[k] is not None:
+                step = np.maximum(step, np.asarray(abs_tol[k], np.float64))
+            pert.append(x + step * rng.choice([-1.0, 1.0], size=x.shape))
         out = oracle(*pert)
         moved = bsdf_mismatch(out[0], out[1], base_f, base_p)
         if wr is not None:

@@ -10,7 +10,9 @@ same numbers within 1e-5; the sampled type identical.  The oracle is evaluated o
 FP32-rounded inputs the GPU receives, with the draws of the reference's hidden BxDF
 generators passed in explicitly (the rough dielectric's and the plastic's third
 number).  A row that misses the contract is a stated FP32 tie only if the oracle's own
-output moves beyond the tolerance when its inputs move by 4 float32 ulps
+output moves beyond the tolerance when its inputs move by 4 float32 ulps, or, for the
+Beckmann samplers, when the first random number moves by 1e-6, the tolerance to which
+the reference's own slope inversion converges (core/microfacet.cc:120)
 (tests/parity.py, bsdf_conditioning); such rows may be at most 1 % of a table.
 """
 import os
@@ -19,7 +21,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import WI_ABS_TOL, bsdf_conditioning, bsdf_mismatch
+from parity import BECKMANN_CDF_TOL, WI_ABS_TOL, bsdf_conditioning, bsdf_mismatch
 
 pytestmark = pytest.mark.gpu
 
@@ -28,6 +30,15 @@ TABLES = ["bsdf_tables.npz", "bsdf_tables_conductor.npz", "bsdf_tables_more.npz"
 
 def _f32(a):
     return np.asarray(a, np.float32).astype(np.float64)
+
+
+def _rows(table, k, fails, **cols):
+    """A readable dump of the first failing rows."""
+    lines = [f"{table} material {k}: {fails.size} rows fail, first {fails[:8].tolist()}"]
+    for i in fails[:8]:
+        lines.append(f"  row {i}: " + "; ".join(f"{n}={np.array2string(np.asarray(v[i]), precision=9)}"
+                                                for n, v in cols.items()))
+    return "\n".join(lines)
 
 
 @pytest.fixture(scope="module")
@@ -47,7 +58,7 @@ def test_bsdf_eval_vs_oracle(ctx, port, table):
         bad = bsdf_mismatch(f, pdf, fr, pr)
         ties = bsdf_conditioning(lambda a, b: port.bsdf_eval(m, a, b), [wo, wi], bad, fr, pr) if bad.any() else bad
         fails = np.nonzero(bad & ~ties)[0]
-        assert fails.size == 0, (table, k, fails[:10], f[fails[:3]], fr[fails[:3]], pdf[fails[:3]], pr[fails[:3]])
+        assert fails.size == 0, _rows(table, k, fails, wo=wo, wi=wi, f=f, fr=fr, pdf=pdf, pr=pr)
         assert ties.sum() <= 0.01 * len(wo), (table, k, int(ties.sum()))
         # and against the reference's own table where the FP32 rounding of the inputs is
         # immaterial (the oracle's values at the rounded and the exact inputs agree)
@@ -77,10 +88,14 @@ def test_bsdf_sample_vs_oracle(ctx, port, table):
         bad = bsdf_mismatch(f, pdf, fr, pr) | (st != sr)
         both = (pdf > 0) & (pr > 0)
         bad |= both & (np.abs(wi - wr).max(1) > WI_ABS_TOL)
-        ties = bsdf_conditioning(oracle, [wo, u, uc], bad, fr, pr, wr, sr) if bad.any() else bad
+        # a Beckmann sampler (rough conductor type 5, rough dielectric distribution 0)
+        # inverts its slope CDF only to BECKMANN_CDF_TOL in the first number
+        beck = m[0] == 5 or (m[0] == 3 and m[3] == 0)
+        tol = [None, np.array([BECKMANN_CDF_TOL, 0.0]) if beck else None, None]
+        ties = bsdf_conditioning(oracle, [wo, u, uc], bad, fr, pr, wr, sr, abs_tol=tol) if bad.any() else bad
         fails = np.nonzero(bad & ~ties)[0]
-        assert fails.size == 0, (table, k, fails[:10], wi[fails[:3]], wr[fails[:3]], st[fails[:3]], sr[fails[:3]],
-                                 pdf[fails[:3]], pr[fails[:3]])
+        assert fails.size == 0, _rows(table, k, fails, wo=wo, u=u, uc=uc, wi=wi, wr=wr, f=f, fr=fr, pdf=pdf, pr=pr,
+                                      st=st, sr=sr)
         assert ties.sum() <= 0.01 * len(wo), (table, k, int(ties.sum()))
         assert (pdf > 0).mean() > 0.2
 

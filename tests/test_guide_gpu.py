@@ -25,6 +25,105 @@ def _random_params(seed):
     return p
 
 
+def _blocks():
+    """(name, slice) of each weight matrix and bias vector in the parameter layout."""
+    out, off = [], 0
+    for li, (o, i) in enumerate(go.SHAPES):
+        out.append((f"W{li + 1}", slice(off, off + o * i)))
+        off += o * i
+        out.append((f"b{li + 1}", slice(off, off + o)))
+        off += o
+    return out
+
+
+def _gather_indices(seed, step, n, avail):
+    """The training batch of Adam step `step`: ring entries chosen by Philox4x32-10 keyed
+    by (seed, 0), counter (sample, step, 0x47415448, 0), index = (word 0 * avail) >> 32."""
+    from oracle import philox as P
+    s = np.arange(n, dtype=np.uint64)
+    ctr = np.stack([s, np.full(n, step), np.full(n, 0x47415448), np.zeros(n)], 1).astype(np.uint32)
+    key = np.tile(np.array([seed, 0], np.uint32), (n, 1))
+    r = P.philox4x32_10(ctr, key)[:, 0].astype(np.uint64)
+    return ((r * np.uint64(avail)) >> np.uint64(32)).astype(np.int64)
+
+
+def test_adam_steps_match_oracle(gpulib):
+    """Three training steps (batch gather, gradient, Adam, weight packing) against a numpy
+    restatement of the same steps (Kingma and Ba, ICLR 2015: beta1 0.9, beta2 0.999,
+    eps 1e-8, bias-corrected moments) applied to the device's own gradient of the same
+    gathered batch, and the batch gather against the oracle's Philox indices."""
+    import torch
+    sc = _room(30)
+    W, H = 48, 32
+    acc = GpuBVHAccel(sc).construct()
+    lr, seed = 2e-3, 13
+    g = GpuGuide(acc, seed=seed, lr=lr, batch=4096)
+    f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    g.render(sc.camera, {"width": W, "height": H, "sampleCount": 8, "maxDepth": sc.max_depth}, f,
+             GUIDE_GUIDED | GUIDE_COLLECT, seed=5)
+    torch.cuda.synchronize()
+    ring = g.ring(1 << 20)
+    avail = ring.shape[0]
+    assert avail > 1000
+    n = min(4096, avail)
+    m = np.zeros(go.N_PARAMS)
+    v = np.zeros(go.N_PARAMS)
+    p = g.params().astype(np.float64)
+    for step in range(3):
+        batch = ring[_gather_indices(seed, step, n, avail)]
+        grad = torch.zeros(go.N_PARAMS, dtype=torch.float32, device="cuda")
+        g.grad(torch.from_numpy(np.ascontiguousarray(batch)).cuda(), grad)
+        gd = grad.cpu().numpy().astype(np.float64)
+        want = go.grad(p.astype(np.float32), batch[:, :9], batch[:, 9:12], batch[:, 12], emulate_bf16=True)
+        assert np.linalg.norm(gd - want) < 1e-2 * np.linalg.norm(want)
+        m = 0.9 * m + 0.1 * gd
+        v = 0.999 * v + 0.001 * gd * gd
+        p_next = p - lr * (m / (1 - 0.9 ** (step + 1))) / (np.sqrt(v / (1 - 0.999 ** (step + 1))) + 1e-8)
+        g.train(1)
+        got = g.params().astype(np.float64)
+        # the update is the same up to float32 rounding and the order of the device's
+        # gradient sums (atomic adds): 1 % of a step, where a step is lr
+        assert np.abs(got - p_next).max() <= 1e-2 * lr + 1e-6, (step, np.abs(got - p_next).max())
+        assert np.abs(got - p).max() > 0.5 * lr
+        p = got
+
+
+def test_gradient_matches_finite_differences(gpulib):
+    """The device gradient against central differences of the device's own loss along
+    directions of the parameters (steps of 3e-3 of the parameter norm, wide against the
+    weights' BF16 rounding; the oracle's own central differences agree within 2 %)."""
+    import torch
+    acc = GpuBVHAccel(_room(10)).construct()
+    g = GpuGuide(acc, seed=3)
+    p = _random_params(11).astype(np.float64)
+    rng = np.random.default_rng(4)
+    n = 2048
+    S = np.zeros((n, 16), np.float32)
+    S[:, :9] = rng.random((n, 9))
+    S[:, 3:9] = S[:, 3:9] * 2 - 1
+    w = rng.normal(size=(n, 3))
+    S[:, 9:12] = w / np.linalg.norm(w, axis=1, keepdims=True)
+    S[:, 12] = rng.random(n) + 0.05
+    Sd = torch.from_numpy(S).cuda()
+    grad = torch.zeros(go.N_PARAMS, dtype=torch.float32, device="cuda")
+
+    def loss_at(q):
+        g.set_params(q.astype(np.float32))
+        return g.grad(Sd, grad)
+
+    g.set_params(p.astype(np.float32))
+    g.grad(Sd, grad)
+    gd = grad.cpu().numpy().astype(np.float64)
+    for k in range(4):
+        # half along the gradient, half random, so that the derivative is well above the
+        # loss's BF16 rounding noise
+        r = rng.normal(size=go.N_PARAMS)
+        d = gd / np.linalg.norm(gd) + r / np.linalg.norm(r)
+        d *= 3e-3 * np.linalg.norm(p) / np.linalg.norm(d)
+        fd = (loss_at(p + d) - loss_at(p - d)) / 2.0
+        assert abs(fd - gd @ d) <= 0.05 * abs(gd @ d), (k, fd, gd @ d)
+
+
 def test_mlp_forward_matches_oracle(gpulib):
     import torch
     acc = GpuBVHAccel(_room(10)).construct()
@@ -66,6 +165,10 @@ def test_gradient_matches_oracle(gpulib):
     cos = gg @ want / (np.linalg.norm(gg) * np.linalg.norm(want))
     assert cos > 0.995, cos
     assert abs(np.linalg.norm(gg) / np.linalg.norm(want) - 1) < 0.03
+    # every parameter block on its own: W1, b1, ..., W4, b4 within 1e-2 relative
+    for name, sl in _blocks():
+        err = np.linalg.norm(gg[sl] - want[sl]) / max(np.linalg.norm(want[sl]), 1e-30)
+        assert err < 1e-2, (name, err)
     ref_loss = go.loss(p, S[:, :9], S[:, 9:12], S[:, 12], emulate_bf16=True)
     assert abs(loss - ref_loss) <= 0.02 * abs(ref_loss) + 1e-3, (loss, ref_loss)
 

@@ -50,9 +50,14 @@ MID_WINDOWS = [(472, 700, 16, 16), (952, 532, 16, 16), (1400, 600, 16, 16), (240
 
 
 def test_midscale_frame_vs_oracle_windows(gpulib, port):
+    """The bench's frame against four oracle windows (1,024 pixels, 3,072 values), 64
+    independent batches of 64 samples per pixel on each side.  The sun (radiance 1e4)
+    seen through glass and off conductors makes the per-pixel distributions heavy-tailed,
+    so the 3-sigma rule counts over all windows together; each window's mean must agree
+    within 3 standard errors on its own."""
     sc = scenes.mid_scale()
     W, H, md = sc.width, sc.height, sc.max_depth
-    batches, spp = 32, 64
+    batches, spp = 64, 64
     acc = GpuBVHAccel(sc).construct()
     integ = GpuPathIntegrator(seed=77)
     film = np.zeros((H, W, 4), np.float32)
@@ -65,12 +70,18 @@ def test_midscale_frame_vs_oracle_windows(gpulib, port):
         for (x0, y0, w, h) in MID_WINDOWS:
             gpu[(x0, y0, w, h)].append(film[y0:y0 + h, x0:x0 + w, :3] / spp)
     o = port.scene(sc)
+    zs = []
     for win in MID_WINDOWS:
         ref = [o.render(sc.camera, W, H, spp, md, seed=5000 + k, window=win)[0] / spp for k in range(batches)]
         mg, vg = _moments(gpu[win])
         mr, vr = _moments(ref)
         assert mr.max() > 0
-        _assert_images_agree(mg, vg, mr, vr, ("mid-scale window", win))
+        zs.append(zscores(mg, vg, mr, vr).ravel())
+        se = np.sqrt(vg.sum() + vr.sum()) / mg.size
+        assert abs(mg.mean() - mr.mean()) < 3 * se + 1e-6, (win, mg.mean(), mr.mean(), se)
+    z = np.concatenate(zs)
+    frac = float((np.abs(z) > 3).mean())
+    assert frac < 0.01, (frac, float(np.abs(z).max()), float(z.mean()))
 
 
 def test_full_microbench_ray_set_vs_oracle(gpulib, port):
@@ -138,7 +149,11 @@ def test_scene_file_box_room_vs_reference_render(gpulib, tmp_path):
     sc = scenes.box_room(width=W, height=H, max_depth=md)
     got, integ = load_scene(scene_to_files(sc, tmp_path / "box"))
     assert integ == "path" and (got.width, got.height, got.max_depth) == (W, H, md)
-    np.testing.assert_allclose(np.asarray(got.camera, np.float64), g["camera"], rtol=1e-6, atol=1e-6)
+    # the file's lookAt target may be any point along the view direction
+    cf, cg = np.asarray(got.camera, np.float64), np.asarray(g["camera"], np.float64)
+    dirs = [(c[3:6] - c[0:3]) / np.linalg.norm(c[3:6] - c[0:3]) for c in (cf, cg)]
+    np.testing.assert_allclose(cf[[0, 1, 2, 6, 7, 8, 9]], cg[[0, 1, 2, 6, 7, 8, 9]], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(dirs[0], dirs[1], atol=1e-6)
     acc = GpuBVHAccel(got).construct()
     gi = GpuPathIntegrator(seed=31)
     means = []
