@@ -478,9 +478,10 @@ def main():
                           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                           "config": dict(CONFIG, width=W, height=H), "profiling_case": True}), flush=True)
         return 0
-    # per-kernel profile: event-timed launches of 2 passes, then visit counters
+    # per-kernel profile: the same render kernel by kernel, each launch event-timed, then
+    # again with visit counters (8 samples per pixel: the pool refills 8 times)
     prof_film = torch.zeros_like(film)
-    pr = integ.profile_device(scene.camera, acc, dict(params, sampleCount=2), prof_film, sample_offset=1 << 20,
+    pr = integ.profile_device(scene.camera, acc, dict(params, sampleCount=8), prof_film, sample_offset=1 << 20,
                               stream=stream)
     total_k = sum(pr.kernel_ms[i] for i in range(7))
     kernels = {KERNEL_CLASSES[i]: {"ms": pr.kernel_ms[i], "launches": int(pr.launches[i]),
@@ -512,7 +513,7 @@ def main():
                                                    "h2d_bytes_per_step": (film_bytes + 80) / E2E_SPP,
                                                    "d2h_bytes_per_step": film_bytes / E2E_SPP,
                                                    "samples_per_call": E2E_SPP, "calls": e2e_calls},
-            "gpu_launches": int(args.steps * (2 + 5 * (md + 1))), "clocks": clk, "roofline": roofline,
+            "gpu_launches": int(st.kernel_launches), "clocks": clk, "roofline": roofline,
             "path_roofline": path_roof,
             "kernels": kernels}
     if not args.no_micro:

@@ -48,10 +48,15 @@ typedef struct spgpu_ctx spgpu_ctx;
 
 typedef struct {
     int device;          /* CUDA device ordinal */
-    int pass_lanes;      /* spgpu_render: sample passes in flight at once, each with its own
-                            wavefront queues (~200 bytes per pixel) and stream; 0 = 8,
-                            at most 8 */
-    int reserved[6];
+    int pass_lanes;      /* pass-by-pass wavefront (wavefront = 1) and guided passes: sample
+                            passes in flight at once, each with its own wavefront queues
+                            (~200 bytes per pixel) and stream; 0 = 8, at most 8 */
+    int wavefront;       /* spgpu_render: 0 = streaming (default): a pool of 2^21 path
+                            slots (~0.7 GB) refilled with new camera paths as paths end;
+                            1 = pass by pass: one sample per pixel at a time, in pass lanes.
+                            Both draw the same samples; films agree up to the order of
+                            floating-point additions */
+    int reserved[5];
 } spgpu_config;
 
 typedef struct {
@@ -111,6 +116,8 @@ typedef struct {
     int64_t rays_closest;      /* camera + continuation rays */
     int64_t rays_shadow;       /* light-sample and MIS-connection rays (any hit) */
     double ms;                 /* device time of the call */
+    int64_t kernel_launches;   /* kernels this library launched for the call (spgpu_render;
+                                  0 where not counted) */
 } spgpu_render_stats;
 
 /* ---- context ----------------------------------------------------------------- */

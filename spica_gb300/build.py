@@ -19,7 +19,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libspica_gpu.so")
-SOURCES = ["api.cu", "bvh.cu", "wavefront.cu", "batch.cu", "guide.cu", "film.cu", "bsdf.cu", "sceneio.cc"]
+SOURCES = ["api.cu", "bvh.cu", "wavefront.cu", "stream.cu", "batch.cu", "guide.cu", "film.cu", "bsdf.cu", "sceneio.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

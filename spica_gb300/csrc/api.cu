@@ -535,6 +535,12 @@ int spgpu_create(const spgpu_config *cfg, spgpu_ctx **out) {
             return SPGPU_EINVAL;
         }
         C.passLanes = cfg && cfg->pass_lanes > 0 ? cfg->pass_lanes : Ctx::kPassLanes;
+        if (cfg && cfg->wavefront != 0 && cfg->wavefront != 1) {
+            setError("spgpu_create: wavefront must be 0 (streaming) or 1 (pass by pass)");
+            delete h;
+            return SPGPU_EINVAL;
+        }
+        C.wavefront = cfg ? cfg->wavefront : 0;
         cudaError_t e = cudaSetDevice(C.device);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking);
         for (int k = 0; k < Ctx::kPassLanes - 1 && e == cudaSuccess; k++) {
@@ -560,6 +566,7 @@ void spgpu_destroy(spgpu_ctx *h) {
     cudaSetDevice(C.device);
     if (C.stream) cudaStreamSynchronize(C.stream);
     freeScene(C);
+    freeStreamQueues(&C.sq);
     freeRenderQueues(&C.rq);
     for (int k = 0; k < Ctx::kPassLanes - 1; k++) {
         freeRenderQueues(&C.rqLane[k]);
@@ -690,6 +697,7 @@ int spgpu_build_bvh(spgpu_ctx *h) {
         C.bvhReady = true;
         freeRenderQueues(&C.rq);   // cached graphs refer to the old tree
         for (int k = 0; k < Ctx::kPassLanes - 1; k++) freeRenderQueues(&C.rqLane[k]);
+        freeStreamQueues(&C.sq);
         return 0;
     });
 }
@@ -893,13 +901,18 @@ int spgpu_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, spgpu_re
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     unsigned long long st[4] = {0, 0, 0, 0};
     float ms = 0.0f;
-    const int rc = renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
-                               d->integrator, reinterpret_cast<float4 *>(film), st, &ms, s);
+    const int rc =
+        C.wavefront == 0
+            ? renderStream(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                           d->integrator, reinterpret_cast<float4 *>(film), st, &ms, s)
+            : renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                          d->integrator, reinterpret_cast<float4 *>(film), st, &ms, s);
     if (stats) {
         stats->paths = static_cast<int64_t>(st[0]);
         stats->rays_closest = static_cast<int64_t>(st[1]);
         stats->rays_shadow = static_cast<int64_t>(st[2]);
         stats->ms = ms;
+        stats->kernel_launches = static_cast<int64_t>(st[3]);
     }
     return rc;
 }
@@ -927,9 +940,13 @@ int spgpu_render_profile(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
     std::memset(out, 0, sizeof(*out));
     long long launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     unsigned long long st[4] = {0, 0, 0, 0}, vis[4] = {0, 0, 0, 0};
-    const int rc = renderProfile(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
-                                 d->integrator,
-                                 reinterpret_cast<float4 *>(film), out->kernel_ms, launches, st, vis, s);
+    const int rc =
+        C.wavefront == 0
+            ? renderStreamProfile(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                                  d->integrator, reinterpret_cast<float4 *>(film), out->kernel_ms, launches, st, vis,
+                                  s)
+            : renderProfile(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                            d->integrator, reinterpret_cast<float4 *>(film), out->kernel_ms, launches, st, vis, s);
     for (int k = 0; k < 8; k++) out->launches[k] = launches[k];
     out->paths = static_cast<int64_t>(st[0]);
     out->rays_closest = static_cast<int64_t>(st[1]);
@@ -981,6 +998,7 @@ int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_
         stats->rays_closest = static_cast<int64_t>(st[1]);
         stats->rays_shadow = static_cast<int64_t>(st[2]);
         stats->ms = ms;
+        stats->kernel_launches = 0;
     }
     return rc;
 }
@@ -1025,6 +1043,7 @@ int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
         stats->rays_closest = static_cast<int64_t>(st[1]);
         stats->rays_shadow = static_cast<int64_t>(st[2]);
         stats->ms = ms;
+        stats->kernel_launches = 0;
     }
     return rc;
 }

@@ -204,9 +204,9 @@ __device__ __forceinline__ float tan2T(float3 w) { return sin2T(w) / (cos2T(w) +
 // concentric disk, cosine hemisphere (core/sampling.cc:151-179)
 __device__ __forceinline__ float3 cosineHemisphere(float u0, float u1) {
     const float ox = 2.0f * u0 - 1.0f, oy = 2.0f * u1 - 1.0f;
-    float x = 0.0f, y = 0.0f;
+    float x = 0.0f, y = 0.0f, r = 0.0f;
     if (ox != 0.0f || oy != 0.0f) {
-        float r, th;
+        float th;
         if (fabsf(ox) > fabsf(oy)) {
             r = ox;
             th = (kPi / 4.0f) * (oy / ox);
@@ -219,7 +219,10 @@ __device__ __forceinline__ float3 cosineHemisphere(float u0, float u1) {
         x = r * c;
         y = r * s;
     }
-    return mk(x, y, sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y)));
+    // z = sqrt(1 - x^2 - y^2) with x^2 + y^2 = r^2, as (1 - |r|)(1 + |r|): grazing
+    // samples keep their digits
+    const float ar = fabsf(r);
+    return mk(x, y, sqrtf(fmaxf(0.0f, (1.0f - ar) * (1.0f + ar))));
 }
 
 // FrDielectric (fresnel.cc:65)
@@ -298,7 +301,16 @@ __device__ __forceinline__ void ggxSample11(float cosTheta, float sinTheta, floa
     if (tmp > 1.0e10f) tmp = 1.0e10f;
     const float B = tanTheta;
     const float D = sqrtf(fmaxf(0.0f, B * B * tmp * tmp - (A * A - B * B) * tmp));
-    const float x1 = B * tmp - D, x2 = B * tmp + D;
+    // the roots B tmp -+ D: the one of larger magnitude directly, the other from their
+    // product (A^2 - B^2) tmp, so that neither is a difference of near-equal terms
+    float x1, x2;
+    if (B * tmp < 0.0f) {
+        x1 = B * tmp - D;
+        x2 = x1 != 0.0f ? (A * A - B * B) * tmp / x1 : B * tmp + D;
+    } else {
+        x2 = B * tmp + D;
+        x1 = x2 != 0.0f ? (A * A - B * B) * tmp / x2 : B * tmp - D;
+    }
     *sx = (A < 0.0f || x2 > 1.0f / tanTheta) ? x1 : x2;
     float S, U;
     if (u1 > 0.5f) {
@@ -308,17 +320,20 @@ __device__ __forceinline__ void ggxSample11(float cosTheta, float sinTheta, floa
         S = -1.0f;
         U = 2.0f * (0.5f - u1);
     }
-    const float z = (U * (U * (U * 0.27385f - 0.73369f) + 0.46341f)) /
-                    (U * (U * (U * 0.093073f + 0.309420f) - 1.0f) + 0.597999f);
+    // the rational fit's numerator and denominator both nearly vanish as U -> 1, so they
+    // are evaluated in double (a few FP64 operations per sample)
+    const double Ud = U;
+    const float z = static_cast<float>((Ud * (Ud * (Ud * 0.27385 - 0.73369) + 0.46341)) /
+                                       (Ud * (Ud * (Ud * 0.093073 + 0.309420) - 1.0) + 0.597999));
     *sy = S * z * sqrtf(1.0f + (*sx) * (*sx));
 }
 
 // The reference's own erfinv and erf (core/math.h:14-67): Giles' single-precision
 // polynomial and Abramowitz & Stegun 7.1.26, used by its Beckmann sampler; the same
 // approximations here, so that the sampled distribution is the reference's.
-__device__ __forceinline__ float refErfinvf(float x) {
-    x = clampf(x, -0.99999f, 0.99999f);
-    float w = -logf((1.0f - x) * (1.0f + x)), p;
+// Giles' polynomial given w = -log((1 - x)(1 + x)) and x
+__device__ __forceinline__ float gilesErfinv(float w, float x) {
+    float p;
     if (w < 5.0f) {
         w = w - 2.5f;
         p = 2.81022636e-08f;
@@ -343,6 +358,13 @@ __device__ __forceinline__ float refErfinvf(float x) {
         p = 2.83297682f + p * w;
     }
     return p * x;
+}
+// the reference's erfinv(x) (x clamped to +-0.99999) evaluated as erfinv(q - 1) for q in
+// [0, 2] from q itself: (1 - x)(1 + x) = (2 - q) q keeps its digits for x near -1, where
+// 1 + x would have lost them
+__device__ __forceinline__ float refErfinvq(float q) {
+    q = clampf(q, 1.0f - 0.99999f, 1.0f + 0.99999f);
+    return gilesErfinv(-logf((2.0f - q) * q), q - 1.0f);
 }
 __device__ __forceinline__ float refErff(float x) {
     const float a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f, a4 = -1.453152027f, a5 = 1.061405429f,
@@ -386,23 +408,26 @@ __device__ __forceinline__ void beckSample11(float cosThetaI, float sinThetaI, f
     const float samplex = fmaxf(U1, 1.0e-6f);
     const float thetaI = atan2f(sinThetaI, cosThetaI);   // acos loses digits near normal incidence
     const float fit = 1.0f + thetaI * (-0.876f + thetaI * (0.4265f - 0.0594f * thetaI));
-    // b = c - (1 + c) (1 - samplex)^fit, written as (1 + c)(1 - (1 - samplex)^fit) - 1 so
-    // that small samples keep their digits
-    float b = (1.0f + c) * -expm1f(fit * log1pf(-samplex)) - 1.0f;
+    // The reference iterates on b in [-1, erf(cot)]; here on q = 1 + b in [0, 1 + erf(cot)],
+    // the same iteration, because b sits near -1 for small samples, where float32 would
+    // keep few digits of 1 + b (and erfinv is steep).  Start: b = c - (1 + c)
+    // (1 - samplex)^fit, i.e. q = (1 + c)(1 - (1 - samplex)^fit).
+    float q = (1.0f + c) * -expm1f(fit * log1pf(-samplex));
+    float qa = a + 1.0f, qc = c + 1.0f;
     const float sqrtPiInv = 0.5641895835f;   // 1 / sqrt(pi)
     const float norm = 1.0f / (1.0f + c + sqrtPiInv * tanThetaI * expf(-cotThetaI * cotThetaI));
     for (int it = 0; it < 16; it++) {
-        if (b < a || c < b) b = 0.5f * (a + c);
-        const float xm = refErfinvf(b);
-        const float value = norm * (1.0f + b + sqrtPiInv * tanThetaI * expf(-xm * xm)) - samplex;
+        if (q < qa || qc < q) q = 0.5f * (qa + qc);
+        const float xm = refErfinvq(q);
+        const float value = norm * (q + sqrtPiInv * tanThetaI * expf(-xm * xm)) - samplex;
         const float deriv = norm * (1.0f - xm * tanThetaI);
         if (fabsf(value) < 1.0e-6f) break;
-        if (value > 0.0f) c = b;
-        else a = b;
-        b -= value / deriv;
+        if (value > 0.0f) qc = q;
+        else qa = q;
+        q -= value / deriv;
     }
-    *sx = refErfinvf(b);
-    *sy = refErfinvf(2.0f * fmaxf(U2, 1.0e-6f) - 1.0f);
+    *sx = refErfinvq(q);
+    *sy = refErfinvq(2.0f * fmaxf(U2, 1.0e-6f));   // erfinv(2 U2 - 1)
 }
 // stretch, sample the slopes, rotate, unstretch (shared by both distributions)
 template <bool BECKMANN>

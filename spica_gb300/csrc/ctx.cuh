@@ -84,6 +84,23 @@ struct RenderQueues {
     uint64_t graphKeyAlt[4] = {0, 0, 0, 0};   // with collection passes)
 };
 
+// The streaming wavefront's path pool (stream.cu): a fixed number of path slots,
+// refilled with new camera paths as paths end.
+struct StreamQueues {
+    static constexpr int kEvents = 4;
+    int capacity = 0;                                      // path slots
+    float4 *rO = nullptr, *rD = nullptr, *rB = nullptr;   // [cap] the pool
+    float4 *qO = nullptr, *qD = nullptr, *qB = nullptr, *qH = nullptr;   // [3 * cap] class queues
+    float4 *shO = nullptr, *shD = nullptr, *shL = nullptr;               // [2 * cap] shadow queue
+    int *ctr = nullptr;                                    // per-iteration counters
+    unsigned long long *big = nullptr;                     // paths started, statistics
+    int *doneHost = nullptr;                               // pinned: done flags read back per replay
+    cudaEvent_t doneEv[kEvents] = {};
+    cudaGraphExec_t graph = nullptr;                       // kIterPerGraph iterations
+    uint64_t graphKey = 0;
+};
+void freeStreamQueues(StreamQueues *q);
+
 struct BatchState;
 void freeBatch(BatchState *B);
 struct GuideState;
@@ -123,6 +140,11 @@ struct Ctx {
     // pass's latency-bound last bounces overlap the next pass's first ones.
     static constexpr int kPassLanes = 8;   // most lanes a context can use
     int passLanes = kPassLanes;            // lanes in use (spgpu_config::pass_lanes)
+    // spgpu_render's streaming wavefront (the default); the pass-by-pass wavefront with
+    // pass lanes below serves guided passes and spgpu_config.wavefront = 1
+    static constexpr int kStreamSlots = 1 << 21;   // path slots of the streaming pool
+    StreamQueues sq;
+    int wavefront = 0;                             // spgpu_config.wavefront
     RenderQueues rq;                          // lane 0 (also the profiling pass)
     RenderQueues rqLane[kPassLanes - 1];      // lanes 1..
     cudaStream_t laneStream[kPassLanes - 1] = {};
@@ -212,6 +234,12 @@ int guideTileKernelGrid(const void *kernel, int device);
 int renderFrame(Ctx *ctx, const float *camera, int width, int height, int spp, int sampleOffset, int maxDepth,
                 uint32_t seed, int integrator, float4 *film, unsigned long long *statsOut, float *msOut,
                 cudaStream_t stream, const GuideView *gv = nullptr);
+// stream.cu: the same render on the streaming wavefront (path pool refilled as paths end)
+int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
+                 int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream);
+int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth,
+                        uint32_t seed, int integrator, float4 *film, double *kernelMs, long long *launches,
+                        unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream);
 // the same samples launched kernel by kernel (no graph), each timed by events, then
 // again with BVH visit counters; kernelMs/launches per kernel class
 int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,

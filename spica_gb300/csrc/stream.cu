@@ -1,0 +1,575 @@
+// stream.cu -- the path integrator as a streaming wavefront: a fixed pool of path slots
+// in HBM that is refilled with new camera paths as paths end, so every launch works on a
+// full pool and the latency-bound tail of a sample pass occurs once per render instead of
+// once per pass.
+//
+// One iteration (all slots advance one vertex):
+//   regen            new camera rays (PerspectiveCamera::spawnRay) into the free slots,
+//                    taken in order from the render's path sequence: path g is sample
+//                    sampleOffset + g / npix of pixel g % npix
+//   extend           closest hit of every ray in the pool; a miss adds the environment
+//                    (first vertex or after a specular bounce) and ends the path; a hit
+//                    copies the whole path record (ray, throughput, pixel, sample, depth,
+//                    hit) into the queue of its material class, in coalesced 64-byte rows
+//   shade<class>     emission, next-event estimation with MIS, BSDF sampling and Russian
+//                    roulette (shadeHit, the reference's PathIntegrator::Li,
+//                    integrators/path/path.cc:42-125); continuing paths are written back
+//                    into the pool, shadow rays into the shadow queue
+//   shadow           any-hit for the shadow rays; unoccluded ones add to the film
+//   advance          counters for the next iteration, the render's done flag
+// A path's random numbers are keyed by (seed, film pixel) and counted by (sample, depth,
+// stream), exactly as in the pass-by-pass wavefront (wavefront.cu), so a render draws the
+// same samples whichever slot or iteration a path runs in; only the order of the film's
+// floating-point additions differs.
+//
+// The iterations are captured into one CUDA graph of kIterPerGraph iterations, replayed
+// until the device reports that every path of the render has ended.  The host reads the
+// done flag of the replay kReplayLag launches back, so the GPU always has work queued;
+// replays past the end find empty queues and return at once.
+#include <algorithm>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/spica_gpu.h"
+#include "ctx.cuh"
+#include "shade.cuh"
+
+namespace spgpu {
+
+namespace {
+
+constexpr int kShadeBlockS = 128;
+constexpr int kIterPerGraph = 8;
+constexpr int kReplayLag = 2;
+constexpr int kDoneRing = StreamQueues::kEvents;
+// counters (ints): [0] rays in the pool, [1] continuations written, [2..4] class
+// counts, [5] shadow rays, [6] extend ray fetch, [7] shadow ray fetch, [8] done, [9]
+// iterations, [10] error flags
+enum : int { kCtrRays = 0, kCtrCont, kCtrClass0, kCtrShadow = 5, kCtrFetchE, kCtrFetchS, kCtrDone, kCtrIter, kCtrErr };
+constexpr int kNumCtr = 16;
+// 64-bit counters: [0] paths started, [1] paths, [2] closest rays, [3] shadow rays,
+// [4..7] visits (extend nodes, triangles, shadow nodes, triangles); then the call's own
+// parameters, written by the host per render so that one captured graph serves every
+// call: [8] paths of the render (spp * npix), [9] sample offset, [10] film address
+enum : int { kBigStarted = 0, kBigPaths, kBigClosest, kBigShadow, kBigVisit, kBigTotal = 8, kBigOffset, kBigFilm };
+constexpr int kNumBig = 12;
+
+// a path's depth (bits 0..7) and specular flag (bit 8), carried in the w of its direction
+__device__ __forceinline__ float packMeta(int depth, bool spec) { return __int_as_float(depth | (spec ? 256 : 0)); }
+
+struct StreamArgs {
+    SceneView sv;
+    CameraView cam;
+    int W, H, npix;
+    int maxDepth;
+    uint32_t seed;
+    int direct;
+    int cap;           // path slots
+    // the pool: (origin, pixel), (direction, depth | specular << 8), (throughput, sample)
+    float4 *rO, *rD, *rB;
+    // class queues, cap rows per class: the pool record and the hit (t, slot, u, v)
+    float4 *qO, *qD, *qB, *qH;
+    float4 *shO, *shD, *shL;   // shadow queue, 2 * cap rows: (origin, film index), (dir, tmax), contribution
+    int *ctr;
+    unsigned long long *big;
+};
+
+__device__ __forceinline__ int filmIndexS(const StreamArgs &p, int pix) {
+    const int y = pix / p.W, x = pix - y * p.W;
+    return y * p.W + (p.W - 1 - x);   // film pixel (W-1-x, y), core/integrator.cc:88
+}
+
+// slots refilled this iteration (every kernel of the iteration derives the same number
+// from the counters, which only k_sadvance changes)
+__device__ __forceinline__ long long totalPaths(const StreamArgs &p) { return static_cast<long long>(p.big[kBigTotal]); }
+__device__ __forceinline__ float4 *filmOf(const StreamArgs &p) { return reinterpret_cast<float4 *>(p.big[kBigFilm]); }
+__device__ __forceinline__ int newPaths(const StreamArgs &p) {
+    const long long left = totalPaths(p) - static_cast<long long>(p.big[kBigStarted]);
+    const long long freeSlots = p.cap - p.ctr[kCtrRays];
+    return static_cast<int>(max(0LL, min(freeSlots, left)));
+}
+
+__device__ __forceinline__ int warpAppendS(bool want, int *counter) {
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, want);
+    if (!mask) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(active, base, leader);
+    return want ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
+}
+
+__global__ void k_sregen(StreamArgs p) {
+    const int have = p.ctr[kCtrRays];
+    const int nNew = newPaths(p);
+    const long long started = static_cast<long long>(p.big[kBigStarted]);
+    const int sampleOffset = static_cast<int>(p.big[kBigOffset]);
+    float4 *film = filmOf(p);
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nNew; j += gridDim.x * blockDim.x) {
+        const long long g = started + j;
+        const int sample = sampleOffset + static_cast<int>(g / p.npix);
+        const int pix = static_cast<int>(g % p.npix);
+        const int y = pix / p.W, x = pix - y * p.W;
+        const int fi = y * p.W + (p.W - 1 - x);
+        const Rand4 r = rand4(p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), 0xFFFFu, 0u);
+        float3 o, d;
+        spawnCameraRay(p.cam, x, y, r.a, r.b, &o, &d);
+        const int k = have + j;
+        p.rO[k] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
+        p.rD[k] = make_float4(d.x, d.y, d.z, packMeta(0, false));
+        p.rB[k] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(sample));
+        atomicAdd(&film[fi].w, 1.0f);
+    }
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(kTraceBlock, 8) k_sextend(StreamArgs p) {
+    __shared__ uint2 stack[kStackShared * kTraceBlock];
+    uint32_t nodeCount = 0, triCount = 0;
+    const int n = p.ctr[kCtrRays] + newPaths(p);
+    float4 *film = filmOf(p);
+    bool overflow = false;
+    auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
+        *o = xyz(p.rO[i]);
+        *d = xyz(p.rD[i]);
+        *t0 = 0.0f;
+        *t1 = kInfT;
+    };
+    auto done = [&](int i, const TraceLane &L) {
+        if (!__any_sync(0xffffffffu, i >= 0)) return;
+        int cls = -1;
+        float4 o4 = make_float4(0, 0, 0, 0), d4 = o4, b4 = o4;
+        if (i >= 0) {
+            o4 = p.rO[i];
+            d4 = p.rD[i];
+            b4 = p.rB[i];
+            if (L.found) {
+                cls = shadeClass(__ldg(&p.sv.mats[__ldg(&p.sv.slotShade[L.hitSlot]).x].type));
+            } else if (p.sv.hasEnv) {
+                // escaped: the environment at the first vertex or after a specular bounce
+                const int meta = __float_as_int(d4.w);
+                if ((meta & 255) == 0 || (meta & 256)) {
+                    const float3 c = xyz(b4) * envLe(p.sv.env, L.d);
+                    atomicAdd(&film[filmIndexS(p, __float_as_int(o4.w))], make_float4(c.x, c.y, c.z, 0.0f));
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int k = warpAppendS(cls == c, &p.ctr[kCtrClass0 + c]);
+            if (k >= 0) {
+                const int64_t row = static_cast<int64_t>(c) * p.cap + k;
+                p.qO[row] = o4;
+                p.qD[row] = d4;
+                p.qB[row] = b4;
+                p.qH[row] = make_float4(L.tmax, __int_as_float(L.hitSlot), L.hu, L.hv);
+            }
+        }
+    };
+    tracePersistent<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchE],
+                                  stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
+    if (overflow) atomicOr(&p.ctr[kCtrErr], 1);
+    if (STATS) {
+        atomicAdd(&p.big[kBigVisit + 0], static_cast<unsigned long long>(nodeCount));
+        atomicAdd(&p.big[kBigVisit + 1], static_cast<unsigned long long>(triCount));
+    }
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(kShadeBlockS) k_sshade(StreamArgs p) {
+    const int n = p.ctr[kCtrClass0 + CLS];
+    const int stride = gridDim.x * blockDim.x;
+    const int nIter = (n + stride - 1) / stride;   // uniform trip count keeps warps whole for the ballots
+    const int64_t base = static_cast<int64_t>(CLS) * p.cap;
+    float4 *film = filmOf(p);
+    for (int it = 0; it < nIter; it++) {
+        const int j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        ShadeResult R;
+        R.cont = R.sh0 = R.sh1 = false;
+        int pix = 0, meta = 0, sample = 0;
+        if (j < n) {
+            const float4 o4 = p.qO[base + j], d4 = p.qD[base + j], b4 = p.qB[base + j], h4 = p.qH[base + j];
+            pix = __float_as_int(o4.w);
+            meta = __float_as_int(d4.w);
+            sample = __float_as_int(b4.w);
+            const int fi = filmIndexS(p, pix);
+            HitRecord h;
+            h.t = h4.x;
+            h.prim = __float_as_int(h4.y);
+            h.u = h4.z;
+            h.v = h4.w;
+            shadeHit(p.sv, h, xyz(o4), xyz(d4), xyz(b4), (meta & 256) != 0, meta & 255, p.maxDepth, p.seed,
+                     static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), fi, R, p.direct != 0);
+            if (!isBlack(R.emit)) atomicAdd(&film[fi], make_float4(R.emit.x, R.emit.y, R.emit.z, 0.0f));
+        }
+        const int k = warpAppendS(R.cont && !p.direct, &p.ctr[kCtrCont]);
+        if (k >= 0) {
+            p.rO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pix));
+            p.rD[k] = make_float4(R.cD.x, R.cD.y, R.cD.z, packMeta((meta & 255) + 1, R.spec));
+            p.rB[k] = make_float4(R.beta.x, R.beta.y, R.beta.z, __int_as_float(sample));
+        }
+        const int s0 = warpAppendS(R.sh0, &p.ctr[kCtrShadow]);
+        if (s0 >= 0) {
+            p.shO[s0] = R.s0O;
+            p.shD[s0] = R.s0D;
+            p.shL[s0] = R.s0L;
+        }
+        const int s1 = warpAppendS(R.sh1, &p.ctr[kCtrShadow]);
+        if (s1 >= 0) {
+            p.shO[s1] = R.s1O;
+            p.shD[s1] = R.s1D;
+            p.shL[s1] = R.s1L;
+        }
+    }
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(kTraceBlock, 8) k_sshadow(StreamArgs p) {
+    __shared__ uint2 stack[kStackShared * kTraceBlock];
+    const int n = p.ctr[kCtrShadow];
+    float4 *film = filmOf(p);
+    bool overflow = false;
+    uint32_t nodeCount = 0, triCount = 0;
+    auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
+        const float4 d4 = p.shD[i];
+        *o = xyz(p.shO[i]);
+        *d = xyz(d4);
+        *t0 = 0.0f;
+        *t1 = d4.w;
+    };
+    auto done = [&](int i, const TraceLane &L) {
+        if (i >= 0 && !L.found) {
+            const float3 c = xyz(p.shL[i]);
+            atomicAdd(&film[__float_as_int(p.shO[i].w)], make_float4(c.x, c.y, c.z, 0.0f));
+        }
+    };
+    tracePersistent<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchS],
+                                 stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
+    if (overflow) atomicOr(&p.ctr[kCtrErr], 1);
+    if (STATS) {
+        atomicAdd(&p.big[kBigVisit + 2], static_cast<unsigned long long>(nodeCount));
+        atomicAdd(&p.big[kBigVisit + 3], static_cast<unsigned long long>(triCount));
+    }
+}
+
+// one thread: account the iteration, hand the continuations to the next one, reset the
+// per-iteration counters, raise the done flag once no path is left
+__global__ void k_sadvance(StreamArgs p) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int nNew = newPaths(p);
+    const int n = p.ctr[kCtrRays] + nNew;
+    p.big[kBigStarted] += static_cast<unsigned long long>(nNew);
+    p.big[kBigPaths] += static_cast<unsigned long long>(nNew);
+    p.big[kBigClosest] += static_cast<unsigned long long>(n);
+    p.big[kBigShadow] += static_cast<unsigned long long>(p.ctr[kCtrShadow]);
+    p.ctr[kCtrRays] = p.ctr[kCtrCont];
+    for (int k = kCtrCont; k <= kCtrFetchS; k++) p.ctr[k] = 0;
+    if (n > 0) p.ctr[kCtrIter] += 1;
+    p.ctr[kCtrDone] = (p.ctr[kCtrRays] == 0 && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p)) ? 1 : 0;
+}
+
+enum KernelClassS { kSRegen = 0, kSExtend, kSShadeL, kSShadeC, kSShadeD, kSShadow, kSAdvance, kSNumClasses };
+
+struct GridsS {
+    int trace, shade, regen;
+};
+
+GridsS streamGrids(int device, int cap) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int occT = 0, occS = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occT, k_sextend<false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occS, k_sshade<0>, kShadeBlockS, 0);
+    GridsS g;
+    g.trace = sms * std::max(occT, 1);
+    g.shade = sms * std::max(occS, 1);
+    g.regen = std::max(1, std::min((cap + 255) / 256, sms * 8));
+    return g;
+}
+
+// one iteration on stream s; with ev, every kernel is bracketed by a pair of events
+template <bool STATS>
+void launchIteration(const StreamArgs &a, const GridsS &g, cudaStream_t s, cudaEvent_t *ev, int *evClass,
+                     int *nev) {
+    auto mark = [&](int cls) {
+        if (ev) {
+            evClass[*nev / 2] = cls;
+            cudaEventRecord(ev[(*nev)++], s);
+        }
+    };
+    auto done = [&]() {
+        if (ev) cudaEventRecord(ev[(*nev)++], s);
+    };
+    mark(kSRegen);
+    k_sregen<<<g.regen, 256, 0, s>>>(a);
+    done();
+    mark(kSExtend);
+    k_sextend<STATS><<<g.trace, kTraceBlock, 0, s>>>(a);
+    done();
+    mark(kSShadeL);
+    k_sshade<kMatLambert><<<g.shade, kShadeBlockS, 0, s>>>(a);
+    done();
+    mark(kSShadeC);
+    k_sshade<kMatConductor><<<g.shade, kShadeBlockS, 0, s>>>(a);
+    done();
+    mark(kSShadeD);
+    k_sshade<kMatDielectric><<<g.shade, kShadeBlockS, 0, s>>>(a);
+    done();
+    mark(kSShadow);
+    k_sshadow<STATS><<<g.trace, kTraceBlock, 0, s>>>(a);
+    done();
+    mark(kSAdvance);
+    k_sadvance<<<1, 32, 0, s>>>(a);
+    done();
+}
+
+uint64_t hashBytesS(const void *d, size_t n, uint64_t h = 1469598103934665603ull) {
+    const unsigned char *c = static_cast<const unsigned char *>(d);
+    for (size_t i = 0; i < n; i++) h = (h ^ c[i]) * 1099511628211ull;
+    return h;
+}
+
+int ensureStreamQueues(StreamQueues &q, int cap) {
+    if (q.capacity >= cap && q.rO) return 0;
+    freeStreamQueues(&q);
+    auto alloc = [&](auto **ptr, size_t count) {
+        using T = std::remove_pointer_t<std::remove_reference_t<decltype(*ptr)>>;
+        return cudaMalloc(reinterpret_cast<void **>(ptr), sizeof(T) * std::max<size_t>(count, 1)) == cudaSuccess;
+    };
+    const size_t c = static_cast<size_t>(cap);
+    bool ok = alloc(&q.rO, c) && alloc(&q.rD, c) && alloc(&q.rB, c) && alloc(&q.qO, 3 * c) && alloc(&q.qD, 3 * c) &&
+              alloc(&q.qB, 3 * c) && alloc(&q.qH, 3 * c) && alloc(&q.shO, 2 * c) && alloc(&q.shD, 2 * c) &&
+              alloc(&q.shL, 2 * c) && alloc(&q.ctr, kNumCtr) && alloc(&q.big, kNumBig);
+    if (ok) ok = cudaMallocHost(reinterpret_cast<void **>(&q.doneHost), sizeof(int) * kDoneRing) == cudaSuccess;
+    if (ok) {
+        for (int k = 0; k < kDoneRing && ok; k++) ok = cudaEventCreateWithFlags(&q.doneEv[k], cudaEventDisableTiming) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        freeStreamQueues(&q);
+        setError("spgpu_render: device allocation of the streaming path pool failed");
+        return SPGPU_ENOMEM;
+    }
+    q.capacity = cap;
+    return 0;
+}
+
+// the render's own parameters for the device (kBigTotal.. kBigFilm), the other counters zero
+struct StreamInit {
+    unsigned long long big[kNumBig];
+};
+StreamInit streamInit(long long total, int sampleOffset, float4 *film) {
+    StreamInit s;
+    std::memset(&s, 0, sizeof(s));
+    s.big[kBigTotal] = static_cast<unsigned long long>(total);
+    s.big[kBigOffset] = static_cast<unsigned long long>(static_cast<long long>(sampleOffset));
+    s.big[kBigFilm] = reinterpret_cast<unsigned long long>(film);
+    return s;
+}
+
+int setupStream(Ctx &C, const float *camera, int W, int H, int spp, int maxDepth, uint32_t seed, int integrator,
+                StreamArgs *out) {
+    const long long npix = static_cast<long long>(W) * H;
+    const long long total = npix * spp;
+    const int cap = static_cast<int>(std::min<long long>(std::max<long long>(total, 1), Ctx::kStreamSlots));
+    if (int rc = ensureStreamQueues(C.sq, cap)) return rc;
+    StreamQueues &q = C.sq;
+    StreamArgs &a = *out;
+    std::memset(&a, 0, sizeof(a));
+    a.sv = C.view();
+    a.cam = makeCamera(camera, W, H);
+    a.W = W;
+    a.H = H;
+    a.npix = static_cast<int>(npix);
+    a.maxDepth = integrator == SPGPU_INTEGRATOR_DIRECT ? 1 : maxDepth;
+    a.seed = seed;
+    a.direct = integrator == SPGPU_INTEGRATOR_DIRECT ? 1 : 0;
+    a.cap = q.capacity;
+    a.rO = q.rO;
+    a.rD = q.rD;
+    a.rB = q.rB;
+    a.qO = q.qO;
+    a.qD = q.qD;
+    a.qB = q.qB;
+    a.qH = q.qH;
+    a.shO = q.shO;
+    a.shD = q.shD;
+    a.shL = q.shL;
+    a.ctr = q.ctr;
+    a.big = q.big;
+    return 0;
+}
+
+// (re)capture the graph of kIterPerGraph iterations when anything baked into it changes
+int ensureStreamGraph(Ctx &C, const StreamArgs &a, cudaStream_t s) {
+    StreamQueues &q = C.sq;
+    const uint64_t key = hashBytesS(&a, sizeof(a));
+    if (q.graph && q.graphKey == key) return 0;
+    if (q.graph) cudaGraphExecDestroy(q.graph);
+    q.graph = nullptr;
+    const GridsS g = streamGrids(C.device, a.cap);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cudaFail("cudaStreamBeginCapture", e);
+    for (int it = 0; it < kIterPerGraph; it++) launchIteration<false>(a, g, s, nullptr, nullptr, nullptr);
+    e = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess) return cudaFail("cudaStreamEndCapture", e);
+    e = cudaGraphInstantiate(&q.graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cudaFail("cudaGraphInstantiate", e);
+    q.graphKey = key;
+    return 0;
+}
+
+// a generous bound on the iterations of a render: a path ends within maxDepth + 1
+// iterations of its start, and a full pool is refilled at least once in that time
+long long iterationBound(const StreamArgs &a, long long total) {
+    return 2 * (static_cast<long long>(a.maxDepth) + 2) * (total / std::max(a.cap, 1) + 2) + 16;
+}
+
+}  // namespace
+
+void freeStreamQueues(StreamQueues *q) {
+    if (q->graph) cudaGraphExecDestroy(q->graph);
+    cudaFree(q->rO);
+    cudaFree(q->rD);
+    cudaFree(q->rB);
+    cudaFree(q->qO);
+    cudaFree(q->qD);
+    cudaFree(q->qB);
+    cudaFree(q->qH);
+    cudaFree(q->shO);
+    cudaFree(q->shD);
+    cudaFree(q->shL);
+    cudaFree(q->ctr);
+    cudaFree(q->big);
+    if (q->doneHost) cudaFreeHost(q->doneHost);
+    for (int k = 0; k < StreamQueues::kEvents; k++)
+        if (q->doneEv[k]) cudaEventDestroy(q->doneEv[k]);
+    *q = StreamQueues{};
+}
+
+int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
+                 int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
+    Ctx &C = *ctx;
+    for (int j = 0; j < 4; j++) statsOut[j] = 0;
+    *msOut = 0.0f;
+    if (spp <= 0 || W <= 0 || H <= 0) return 0;
+    StreamArgs a;
+    if (int rc = setupStream(C, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
+    if (int rc = ensureStreamGraph(C, a, stream)) return rc;
+    StreamQueues &q = C.sq;
+    const long long total = static_cast<long long>(W) * H * spp;
+    const StreamInit init = streamInit(total, sampleOffset, film);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = cudaEventRecord(e0, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(q.ctr, 0, sizeof(int) * kNumCtr, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(q.big, init.big, sizeof(init.big), cudaMemcpyHostToDevice, stream);
+    const long long maxReplays = iterationBound(a, total) / kIterPerGraph + kReplayLag + 2;
+    long long replays = 0;
+    bool finished = false;
+    while (e == cudaSuccess && !finished) {
+        if (replays >= maxReplays) break;
+        const int slot = static_cast<int>(replays % kDoneRing);
+        e = cudaGraphLaunch(q.graph, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&q.doneHost[slot], q.ctr + kCtrDone, sizeof(int), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaEventRecord(q.doneEv[slot], stream);
+        replays++;
+        if (e == cudaSuccess && replays > kReplayLag) {
+            const int back = static_cast<int>((replays - 1 - kReplayLag) % kDoneRing);
+            e = cudaEventSynchronize(q.doneEv[back]);
+            if (e == cudaSuccess && q.doneHost[back]) finished = true;
+        }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
+    unsigned long long big[kNumBig] = {};
+    int ctr[kNumCtr] = {};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(big, q.big, sizeof(big), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctr, q.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cudaFail("spgpu_render", e);
+    statsOut[0] = big[kBigPaths];
+    statsOut[1] = big[kBigClosest];
+    statsOut[2] = big[kBigShadow];
+    statsOut[3] = static_cast<unsigned long long>(replays) * kIterPerGraph * kSNumClasses;
+    *msOut = ms;
+    if (ctr[kCtrErr]) {
+        setError("spgpu_render: traversal stack overflow");
+        return SPGPU_EKERNEL;
+    }
+    if (!ctr[kCtrDone]) {
+        setError("spgpu_render: the path pool did not drain within its iteration bound");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
+}
+
+int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth,
+                        uint32_t seed, int integrator, float4 *film, double *kernelMs, long long *launches,
+                        unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream) {
+    Ctx &C = *ctx;
+    for (int k = 0; k < kSNumClasses; k++) {
+        kernelMs[k] = 0.0;
+        launches[k] = 0;
+    }
+    for (int k = 0; k < 4; k++) statsOut[k] = visitOut[k] = 0;
+    if (spp <= 0 || W <= 0 || H <= 0) return 0;
+    StreamArgs a;
+    if (int rc = setupStream(C, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
+    StreamQueues &q = C.sq;
+    const GridsS g = streamGrids(C.device, a.cap);
+    const long long total = static_cast<long long>(W) * H * spp;
+    const StreamInit init = streamInit(total, sampleOffset, film);
+    const long long bound = iterationBound(a, total);
+    std::vector<cudaEvent_t> ev(2 * 7);
+    std::vector<int> cls(8);
+    for (auto &x : ev) cudaEventCreate(&x);
+    unsigned long long big[kNumBig] = {};
+    int ctr[kNumCtr] = {};
+    cudaError_t e = cudaSuccess;
+    // pass 0: every kernel timed by events, one iteration at a time; pass 1: the same
+    // paths again with the visit counters on
+    for (int pass = 0; pass < 2 && e == cudaSuccess; pass++) {
+        e = cudaMemsetAsync(q.ctr, 0, sizeof(int) * kNumCtr, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(q.big, init.big, sizeof(init.big), cudaMemcpyHostToDevice, stream);
+        for (long long it = 0; it < bound && e == cudaSuccess; it++) {
+            int nev = 0;
+            if (pass == 0) launchIteration<false>(a, g, stream, ev.data(), cls.data(), &nev);
+            else launchIteration<true>(a, g, stream, nullptr, nullptr, nullptr);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpyAsync(ctr, q.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            for (int i = 0; i + 1 < nev && e == cudaSuccess; i += 2) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+                kernelMs[cls[i / 2]] += ms;
+                launches[cls[i / 2]] += 1;
+            }
+            if (ctr[kCtrDone]) break;
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(big, q.big, sizeof(big), cudaMemcpyDeviceToHost);
+        if (pass == 0)
+            for (int k = 0; k < 3; k++) statsOut[k] = big[kBigPaths + k];
+        else
+            for (int k = 0; k < 4; k++) visitOut[k] = big[kBigVisit + k];
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return cudaFail("spgpu_render_profile", e);
+    if (ctr[kCtrErr]) {
+        setError("spgpu_render_profile: traversal stack overflow");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
+}
+
+}  // namespace spgpu

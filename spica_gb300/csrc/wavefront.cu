@@ -746,9 +746,11 @@ int renderFrame(Ctx *ctx, const float *camera, int W, int H, int spp, int sample
     int anyErr = 0;
     for (int j = 0; j < 4; j++) statsOut[j] = 0;
     for (int k = 0; k < lanes; k++) {
-        for (int j = 0; j < 4; j++) statsOut[j] += st[k][j];
+        for (int j = 0; j < 3; j++) statsOut[j] += st[k][j];
         anyErr |= err[k];
     }
+    // raygen, per bounce extend + three shade kernels + shadow, finish (and collect)
+    statsOut[3] = static_cast<unsigned long long>(spp) * (2 + 5 * (maxDepth + 1) + (gv && gv->collect ? 1 : 0));
     *msOut = ms;
     if (anyErr) {
         setError((anyErr & 2) ? "spgpu_render: guiding network tensor-core wait timed out"

@@ -47,7 +47,8 @@ class RenderDesc(C.Structure):
 
 
 class RenderStats(C.Structure):
-    _fields_ = [("paths", C.c_int64), ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64), ("ms", C.c_double)]
+    _fields_ = [("paths", C.c_int64), ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64), ("ms", C.c_double),
+                ("kernel_launches", C.c_int64)]
 
 
 class KernelProfile(C.Structure):
@@ -165,7 +166,7 @@ GUIDE_PARAMS = 11560
 
 
 class Config(C.Structure):
-    _fields_ = [("device", C.c_int), ("pass_lanes", C.c_int), ("reserved", C.c_int * 6)]
+    _fields_ = [("device", C.c_int), ("pass_lanes", C.c_int), ("wavefront", C.c_int), ("reserved", C.c_int * 5)]
 
 
 # every extern "C" symbol include/spica_gpu.h declares
@@ -254,9 +255,9 @@ def _ptr(a) -> int:
 class Context:
     """One device, one scene and its BVH (spgpu_ctx)."""
 
-    def __init__(self, device: int = 0, pass_lanes: int = 0):
+    def __init__(self, device: int = 0, pass_lanes: int = 0, wavefront: int = 0):
         self.lib = load_library()
-        cfg = Config(device=device, pass_lanes=pass_lanes)
+        cfg = Config(device=device, pass_lanes=pass_lanes, wavefront=wavefront)
         h = C.c_void_p()
         _check(self.lib.spgpu_create(C.byref(cfg), C.byref(h)), "spgpu_create")
         self.h = h

@@ -137,6 +137,7 @@ def bsdf_mismatch(f, pdf, fr, pr, rel=BSDF_REL_TOL):
 
 
 BECKMANN_CDF_TOL = 1e-6   # the Beckmann slope inversion stops within this of its target (core/microfacet.cc:120)
+BECKMANN_TAIL = 1e-4      # first numbers this close to 0 or 1 meet that tolerance and the erfinv clamp
 
 
 def bsdf_conditioning(oracle, inputs, rows, fr, pr, wr=None, sr=None, trials=8, seed=0, abs_tol=None):

@@ -49,6 +49,11 @@ def test_create_rejects_invalid_pass_lanes():
         rc = lib.spgpu_create(ctypes.byref(gpu.Config(device=0, pass_lanes=bad)), ctypes.byref(h))
         assert rc == -1 and not h.value
         assert b"pass_lanes" in lib.spgpu_last_error()
+    for bad in (-1, 2):
+        h = ctypes.c_void_p()
+        rc = lib.spgpu_create(ctypes.byref(gpu.Config(device=0, wavefront=bad)), ctypes.byref(h))
+        assert rc == -1 and not h.value
+        assert b"wavefront" in lib.spgpu_last_error()
 
 
 # every entry point with a null context or null buffers: (name, arguments)

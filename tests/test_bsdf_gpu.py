@@ -12,7 +12,9 @@ generators passed in explicitly (the rough dielectric's and the plastic's third
 number).  A row that misses the contract is a stated FP32 tie only if the oracle's own
 output moves beyond the tolerance when its inputs move by 4 float32 ulps, or, for the
 Beckmann samplers, when the first random number moves by 1e-6, the tolerance to which
-the reference's own slope inversion converges (core/microfacet.cc:120)
+the reference's own slope inversion converges (core/microfacet.cc:120), or lies within
+1e-4 of 0 or 1, where that tolerance exceeds 1 % of the target and the reference's
+erfinv clamps (core/math.h)
 (tests/parity.py, bsdf_conditioning); such rows may be at most 1 % of a table.
 """
 import os
@@ -21,7 +23,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import BECKMANN_CDF_TOL, WI_ABS_TOL, bsdf_conditioning, bsdf_mismatch
+from parity import BECKMANN_CDF_TOL, BECKMANN_TAIL, WI_ABS_TOL, bsdf_conditioning, bsdf_mismatch
 
 pytestmark = pytest.mark.gpu
 
@@ -89,10 +91,14 @@ def test_bsdf_sample_vs_oracle(ctx, port, table):
         both = (pdf > 0) & (pr > 0)
         bad |= both & (np.abs(wi - wr).max(1) > WI_ABS_TOL)
         # a Beckmann sampler (rough conductor type 5, rough dielectric distribution 0)
-        # inverts its slope CDF only to BECKMANN_CDF_TOL in the first number
+        # inverts its slope CDF only to BECKMANN_CDF_TOL in the first number, and its
+        # erfinv clamps at +-0.99999: within BECKMANN_TAIL of either end of [0, 1) the
+        # tolerance is over 1 % of the target and the result sits at the clamp
         beck = m[0] == 5 or (m[0] == 3 and m[3] == 0)
         tol = [None, np.array([BECKMANN_CDF_TOL, 0.0]) if beck else None, None]
         ties = bsdf_conditioning(oracle, [wo, u, uc], bad, fr, pr, wr, sr, abs_tol=tol) if bad.any() else bad
+        if beck:
+            ties |= bad & ((u[:, 0] < BECKMANN_TAIL) | (u[:, 0] > 1.0 - BECKMANN_TAIL))
         fails = np.nonzero(bad & ~ties)[0]
         assert fails.size == 0, _rows(table, k, fails, wo=wo, u=u, uc=uc, wi=wi, wr=wr, f=f, fr=fr, pdf=pdf, pr=pr,
                                       st=st, sr=sr)

@@ -59,8 +59,11 @@ def test_adam_steps_match_oracle(gpulib):
     lr, seed = 2e-3, 13
     g = GpuGuide(acc, seed=seed, lr=lr, batch=4096)
     f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
-    g.render(sc.camera, {"width": W, "height": H, "sampleCount": 8, "maxDepth": sc.max_depth}, f,
-             GUIDE_GUIDED | GUIDE_COLLECT, seed=5)
+    for k in range(64):   # collection passes until the ring holds a few thousand entries
+        g.render(sc.camera, {"width": W, "height": H, "sampleCount": 16, "maxDepth": sc.max_depth}, f,
+                 GUIDE_GUIDED | GUIDE_COLLECT, seed=5, sample_offset=16 * k)
+        if g.samples() >= 4096:
+            break
     torch.cuda.synchronize()
     ring = g.ring(1 << 20)
     avail = ring.shape[0]
@@ -78,12 +81,19 @@ def test_adam_steps_match_oracle(gpulib):
         assert np.linalg.norm(gd - want) < 1e-2 * np.linalg.norm(want)
         m = 0.9 * m + 0.1 * gd
         v = 0.999 * v + 0.001 * gd * gd
-        p_next = p - lr * (m / (1 - 0.9 ** (step + 1))) / (np.sqrt(v / (1 - 0.999 ** (step + 1))) + 1e-8)
+        vhat = v / (1 - 0.999 ** (step + 1))
+        p_next = p - lr * (m / (1 - 0.9 ** (step + 1))) / (np.sqrt(vhat) + 1e-8)
         g.train(1)
         got = g.params().astype(np.float64)
-        # the update is the same up to float32 rounding and the order of the device's
-        # gradient sums (atomic adds): 1 % of a step, where a step is lr
-        assert np.abs(got - p_next).max() <= 1e-2 * lr + 1e-6, (step, np.abs(got - p_next).max())
+        # Where sqrt(v_hat) is well above eps, the update is the same up to float32
+        # rounding and the order of the device's gradient sums (atomic adds): within 1 % of
+        # a step (lr).  Parameters whose gradients are at the level of that summation noise
+        # (dead units, cancelling terms) still move by at most one step.
+        firm = np.sqrt(vhat) > 1e-5
+        assert firm.mean() > 0.5
+        err = np.abs(got - p_next)
+        assert err[firm].max() <= 1e-2 * lr + 1e-6, (step, err[firm].max(), int(np.argmax(np.where(firm, err, 0))))
+        assert np.abs(got - p).max() <= 1.1 * lr, (step, np.abs(got - p).max())
         assert np.abs(got - p).max() > 0.5 * lr
         p = got
 
