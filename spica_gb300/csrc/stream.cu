@@ -460,7 +460,9 @@ int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampl
     if (spp <= 0 || W <= 0 || H <= 0) return 0;
     StreamArgs a;
     if (int rc = setupStream(C, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
-    if (int rc = ensureStreamGraph(C, a, stream)) return rc;
+    // captured on the context's own stream (the caller's may be the legacy default stream,
+    // which cannot be captured), replayed on the caller's
+    if (int rc = ensureStreamGraph(C, a, C.stream)) return rc;
     StreamQueues &q = C.sq;
     const long long total = static_cast<long long>(W) * H * spp;
     const StreamInit init = streamInit(total, sampleOffset, film);
