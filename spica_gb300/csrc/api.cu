@@ -566,7 +566,7 @@ void spgpu_destroy(spgpu_ctx *h) {
     cudaSetDevice(C.device);
     if (C.stream) cudaStreamSynchronize(C.stream);
     freeScene(C);
-    freeStreamQueues(&C.sq);
+    for (auto &q : C.sq) freeStreamQueues(&q);
     freeRenderQueues(&C.rq);
     for (int k = 0; k < Ctx::kPassLanes - 1; k++) {
         freeRenderQueues(&C.rqLane[k]);
@@ -697,7 +697,7 @@ int spgpu_build_bvh(spgpu_ctx *h) {
         C.bvhReady = true;
         freeRenderQueues(&C.rq);   // cached graphs refer to the old tree
         for (int k = 0; k < Ctx::kPassLanes - 1; k++) freeRenderQueues(&C.rqLane[k]);
-        freeStreamQueues(&C.sq);
+        for (auto &q : C.sq) freeStreamQueues(&q);
         return 0;
     });
 }

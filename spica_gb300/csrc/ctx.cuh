@@ -142,8 +142,18 @@ struct Ctx {
     int passLanes = kPassLanes;            // lanes in use (spgpu_config::pass_lanes)
     // spgpu_render's streaming wavefront (the default); the pass-by-pass wavefront with
     // pass lanes below serves guided passes and spgpu_config.wavefront = 1
-    static constexpr int kStreamSlots = 1 << 21;   // path slots of the streaming pool
-    StreamQueues sq;
+#ifndef SPGPU_STREAM_SLOTS_LOG2
+#define SPGPU_STREAM_SLOTS_LOG2 21
+#endif
+#ifndef SPGPU_POOL_LANES
+#define SPGPU_POOL_LANES 2
+#endif
+    // path slots of one streaming pool; pools in flight at once, each on its own stream
+    // rendering its share of the samples, so that one pool's latency-bound kernel tails
+    // overlap the other's work
+    static constexpr int kStreamSlots = 1 << SPGPU_STREAM_SLOTS_LOG2;
+    static constexpr int kPoolLanes = SPGPU_POOL_LANES;
+    StreamQueues sq[kPoolLanes];
     int wavefront = 0;                             // spgpu_config.wavefront
     RenderQueues rq;                          // lane 0 (also the profiling pass)
     RenderQueues rqLane[kPassLanes - 1];      // lanes 1..

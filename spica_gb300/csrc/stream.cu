@@ -370,13 +370,12 @@ StreamInit streamInit(long long total, int sampleOffset, float4 *film) {
     return s;
 }
 
-int setupStream(Ctx &C, const float *camera, int W, int H, int spp, int maxDepth, uint32_t seed, int integrator,
-                StreamArgs *out) {
+int setupStream(Ctx &C, StreamQueues &q, const float *camera, int W, int H, int spp, int maxDepth, uint32_t seed,
+                int integrator, StreamArgs *out) {
     const long long npix = static_cast<long long>(W) * H;
     const long long total = npix * spp;
     const int cap = static_cast<int>(std::min<long long>(std::max<long long>(total, 1), Ctx::kStreamSlots));
-    if (int rc = ensureStreamQueues(C.sq, cap)) return rc;
-    StreamQueues &q = C.sq;
+    if (int rc = ensureStreamQueues(q, cap)) return rc;
     StreamArgs &a = *out;
     std::memset(&a, 0, sizeof(a));
     a.sv = C.view();
@@ -404,8 +403,7 @@ int setupStream(Ctx &C, const float *camera, int W, int H, int spp, int maxDepth
 }
 
 // (re)capture the graph of kIterPerGraph iterations when anything baked into it changes
-int ensureStreamGraph(Ctx &C, const StreamArgs &a, cudaStream_t s) {
-    StreamQueues &q = C.sq;
+int ensureStreamGraph(Ctx &C, StreamQueues &q, const StreamArgs &a, cudaStream_t s) {
     const uint64_t key = hashBytesS(&a, sizeof(a));
     if (q.graph && q.graphKey == key) return 0;
     if (q.graph) cudaGraphExecDestroy(q.graph);
@@ -458,58 +456,102 @@ int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampl
     for (int j = 0; j < 4; j++) statsOut[j] = 0;
     *msOut = 0.0f;
     if (spp <= 0 || W <= 0 || H <= 0) return 0;
-    StreamArgs a;
-    if (int rc = setupStream(C, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
-    // captured on the context's own stream (the caller's may be the legacy default stream,
-    // which cannot be captured), replayed on the caller's
-    if (int rc = ensureStreamGraph(C, a, C.stream)) return rc;
-    StreamQueues &q = C.sq;
-    const long long total = static_cast<long long>(W) * H * spp;
-    const StreamInit init = streamInit(total, sampleOffset, film);
+    // pool lanes: lane k renders a contiguous share of the samples, lane 0 on the caller's
+    // stream, lane k > 0 on the context's lane stream k - 1
+    const int lanes = std::max(1, std::min(spp, Ctx::kPoolLanes));
+    StreamArgs a[Ctx::kPoolLanes];
+    StreamInit init[Ctx::kPoolLanes];
+    cudaStream_t ls[Ctx::kPoolLanes];
+    long long maxReplays[Ctx::kPoolLanes], replays[Ctx::kPoolLanes];
+    bool finished[Ctx::kPoolLanes];
+    int first = sampleOffset;
+    for (int k = 0; k < lanes; k++) {
+        const int sppK = spp / lanes + (k < spp % lanes ? 1 : 0);
+        if (int rc = setupStream(C, C.sq[k], camera, W, H, sppK, maxDepth, seed, integrator, &a[k])) return rc;
+        // captured on the context's own stream (the caller's may be the legacy default
+        // stream, which cannot be captured), replayed on the lane's
+        if (int rc = ensureStreamGraph(C, C.sq[k], a[k], C.stream)) return rc;
+        const long long total = static_cast<long long>(W) * H * sppK;
+        init[k] = streamInit(total, first, film);
+        first += sppK;
+        ls[k] = k == 0 ? stream : C.laneStream[k - 1];
+        maxReplays[k] = iterationBound(a[k], total) / kIterPerGraph + kReplayLag + 2;
+        replays[k] = 0;
+        finished[k] = false;
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaError_t e = cudaEventRecord(e0, stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(q.ctr, 0, sizeof(int) * kNumCtr, stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(q.big, init.big, sizeof(init.big), cudaMemcpyHostToDevice, stream);
-    const long long maxReplays = iterationBound(a, total) / kIterPerGraph + kReplayLag + 2;
-    long long replays = 0;
-    bool finished = false;
-    while (e == cudaSuccess && !finished) {
-        if (replays >= maxReplays) break;
-        const int slot = static_cast<int>(replays % kDoneRing);
-        e = cudaGraphLaunch(q.graph, stream);
+    if (e == cudaSuccess && lanes > 1) e = cudaEventRecord(C.laneFork, stream);
+    for (int k = 0; k < lanes && e == cudaSuccess; k++) {
+        StreamQueues &q = C.sq[k];
+        if (k > 0) e = cudaStreamWaitEvent(ls[k], C.laneFork, 0);
+        if (e == cudaSuccess) e = cudaMemsetAsync(q.ctr, 0, sizeof(int) * kNumCtr, ls[k]);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(&q.doneHost[slot], q.ctr + kCtrDone, sizeof(int), cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess) e = cudaEventRecord(q.doneEv[slot], stream);
-        replays++;
-        if (e == cudaSuccess && replays > kReplayLag) {
-            const int back = static_cast<int>((replays - 1 - kReplayLag) % kDoneRing);
-            e = cudaEventSynchronize(q.doneEv[back]);
-            if (e == cudaSuccess && q.doneHost[back]) finished = true;
+            e = cudaMemcpyAsync(q.big, init[k].big, sizeof(init[k].big), cudaMemcpyHostToDevice, ls[k]);
+    }
+    // replay each lane's graph until its pool drains, reading each lane's done flag
+    // kReplayLag replays back
+    int open = lanes;
+    while (e == cudaSuccess && open > 0) {
+        for (int k = 0; k < lanes && e == cudaSuccess; k++) {
+            if (finished[k]) continue;
+            StreamQueues &q = C.sq[k];
+            if (replays[k] >= maxReplays[k]) {
+                finished[k] = true;   // reported below: the done flag stays unset
+                open--;
+                continue;
+            }
+            const int slot = static_cast<int>(replays[k] % kDoneRing);
+            e = cudaGraphLaunch(q.graph, ls[k]);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(&q.doneHost[slot], q.ctr + kCtrDone, sizeof(int), cudaMemcpyDeviceToHost, ls[k]);
+            if (e == cudaSuccess) e = cudaEventRecord(q.doneEv[slot], ls[k]);
+            replays[k]++;
+            if (e == cudaSuccess && replays[k] > kReplayLag) {
+                const int back = static_cast<int>((replays[k] - 1 - kReplayLag) % kDoneRing);
+                e = cudaEventSynchronize(q.doneEv[back]);
+                if (e == cudaSuccess && q.doneHost[back]) {
+                    finished[k] = true;
+                    open--;
+                }
+            }
         }
     }
+    for (int k = 1; k < lanes && e == cudaSuccess; k++) {
+        e = cudaEventRecord(C.laneJoin[k - 1], ls[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, C.laneJoin[k - 1], 0);
+    }
     if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
-    unsigned long long big[kNumBig] = {};
-    int ctr[kNumCtr] = {};
-    if (e == cudaSuccess) e = cudaMemcpyAsync(big, q.big, sizeof(big), cudaMemcpyDeviceToHost, stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctr, q.ctr, sizeof(ctr), cudaMemcpyDeviceToHost, stream);
+    unsigned long long big[Ctx::kPoolLanes][kNumBig] = {};
+    int ctr[Ctx::kPoolLanes][kNumCtr] = {};
+    for (int k = 0; k < lanes && e == cudaSuccess; k++) {
+        e = cudaMemcpyAsync(big[k], C.sq[k].big, sizeof(big[k]), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctr[k], C.sq[k].ctr, sizeof(ctr[k]), cudaMemcpyDeviceToHost, stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     float ms = 0.0f;
     if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cudaFail("spgpu_render", e);
-    statsOut[0] = big[kBigPaths];
-    statsOut[1] = big[kBigClosest];
-    statsOut[2] = big[kBigShadow];
-    statsOut[3] = static_cast<unsigned long long>(replays) * kIterPerGraph * kSNumClasses;
+    int err = 0;
+    bool drained = true;
+    for (int k = 0; k < lanes; k++) {
+        statsOut[0] += big[k][kBigPaths];
+        statsOut[1] += big[k][kBigClosest];
+        statsOut[2] += big[k][kBigShadow];
+        statsOut[3] += static_cast<unsigned long long>(replays[k]) * kIterPerGraph * kSNumClasses;
+        err |= ctr[k][kCtrErr];
+        drained = drained && ctr[k][kCtrDone];
+    }
     *msOut = ms;
-    if (ctr[kCtrErr]) {
+    if (err) {
         setError("spgpu_render: traversal stack overflow");
         return SPGPU_EKERNEL;
     }
-    if (!ctr[kCtrDone]) {
+    if (!drained) {
         setError("spgpu_render: the path pool did not drain within its iteration bound");
         return SPGPU_EKERNEL;
     }
@@ -527,8 +569,8 @@ int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, in
     for (int k = 0; k < 4; k++) statsOut[k] = visitOut[k] = 0;
     if (spp <= 0 || W <= 0 || H <= 0) return 0;
     StreamArgs a;
-    if (int rc = setupStream(C, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
-    StreamQueues &q = C.sq;
+    StreamQueues &q = C.sq[0];
+    if (int rc = setupStream(C, q, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
     const GridsS g = streamGrids(C.device, a.cap);
     const long long total = static_cast<long long>(W) * H * spp;
     const StreamInit init = streamInit(total, sampleOffset, film);
