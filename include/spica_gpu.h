@@ -51,8 +51,8 @@ typedef struct {
     int pass_lanes;      /* pass-by-pass wavefront (wavefront = 1) and guided passes: sample
                             passes in flight at once, each with its own wavefront queues
                             (~200 bytes per pixel) and stream; 0 = 8, at most 8 */
-    int wavefront;       /* spgpu_render: 0 = streaming (default): two pools of 2^22 path
-                            slots (~1.4 GB each) refilled with new camera paths as paths
+    int wavefront;       /* spgpu_render: 0 = streaming (default): two pools of 2^23 path
+                            slots (~2.8 GB each) refilled with new camera paths as paths
                             end, each rendering half of the samples on its own stream;
                             1 = pass by pass: one sample per pixel at a time, in pass lanes.
                             Both draw the same samples; films agree up to the order of

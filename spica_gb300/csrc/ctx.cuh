@@ -143,7 +143,7 @@ struct Ctx {
     // spgpu_render's streaming wavefront (the default); the pass-by-pass wavefront with
     // pass lanes below serves guided passes and spgpu_config.wavefront = 1
 #ifndef SPGPU_STREAM_SLOTS_LOG2
-#define SPGPU_STREAM_SLOTS_LOG2 22
+#define SPGPU_STREAM_SLOTS_LOG2 23
 #endif
 #ifndef SPGPU_POOL_LANES
 #define SPGPU_POOL_LANES 2

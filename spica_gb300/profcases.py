@@ -9,8 +9,9 @@ case), separate from the benchmark:
     python -m spica_gb300.profcases film [--width W] [--height H]
 
 render  the mid-scale scene (500 instances, ~2.03M triangles, depth 16) at W x H:
-        K warm-up passes on every pass lane, then N sample passes (extend, shade,
-        shadow, raygen, finish kernels)
+        a warm-up render of 8 K samples per pixel, then a render of N samples per pixel
+        inside the NVTX range "profiled" (streaming wavefront: k_sregen, k_sextend,
+        k_sshade<0..2>, k_sshadow, k_sadvance)
 micro   the intersection microbench's sphere (1,048,576 triangles) and N of its rays,
         closest then any hit (k_trace)
 batch   the first N seeded box-room variants in one persistent batch launch (k_batch)
@@ -40,8 +41,10 @@ def _render(args, torch):
     film = torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda")
     integ.render_device(sc.camera, acc, dict(p, sampleCount=8 * max(args.warmup, 1)), film)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("profiled")
     st = integ.render_device(sc.camera, acc, dict(p, sampleCount=args.spp), film, sample_offset=1 << 12)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     return {"case": "render", "width": sc.width, "height": sc.height, "spp": args.spp, "ms": st.ms,
             "paths": int(st.paths)}
 
