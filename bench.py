@@ -483,10 +483,9 @@ def main():
     prof_film = torch.zeros_like(film)
     pr = integ.profile_device(scene.camera, acc, dict(params, sampleCount=8), prof_film, sample_offset=1 << 20,
                               stream=stream)
-    nk = len(KERNEL_CLASSES)
-    total_k = sum(pr.kernel_ms[i] for i in range(nk))
+    total_k = sum(pr.kernel_ms[i] for i in range(7))
     kernels = {KERNEL_CLASSES[i]: {"ms": pr.kernel_ms[i], "launches": int(pr.launches[i]),
-                                   "share": pr.kernel_ms[i] / total_k if total_k else 0.0} for i in range(nk)}
+                                   "share": pr.kernel_ms[i] / total_k if total_k else 0.0} for i in range(7)}
     ext_ms_per_launch = pr.kernel_ms[1] / max(pr.launches[1], 1)
     rays_per_launch = pr.rays_closest / max(pr.launches[1], 1)
     bytes_per_ray = 32 + 16 + 80 * pr.closest_nodes_per_ray + 48 * pr.closest_tris_per_ray

@@ -46,28 +46,13 @@ constexpr int kDoneRing = StreamQueues::kEvents;
 // counters (ints): [0] rays in the pool, [1] continuations written, [2..4] class
 // counts, [5] shadow rays, [6] extend ray fetch, [7] shadow ray fetch, [8] done, [9]
 // iterations, [10] error flags
-enum : int {
-    kCtrRays = 0, kCtrCont, kCtrClass0, kCtrShadow = 5, kCtrFetchE, kCtrFetchS, kCtrDone, kCtrIter, kCtrErr,
-    kCtrFetchF, kCtrFinBlocks   // [11] drain path fetch, [12] drain blocks finished
-};
+enum : int { kCtrRays = 0, kCtrCont, kCtrClass0, kCtrShadow = 5, kCtrFetchE, kCtrFetchS, kCtrDone, kCtrIter, kCtrErr };
 constexpr int kNumCtr = 16;
 // 64-bit counters: [0] paths started, [1] paths, [2] closest rays, [3] shadow rays,
 // [4..7] visits (extend nodes, triangles, shadow nodes, triangles); then the call's own
 // parameters, written by the host per render so that one captured graph serves every
-// call: [8] paths of the render (spp * npix), [9] sample offset, [10] film address;
-// [11] closest-hit rays traced by the drain kernel
-enum : int {
-    kBigStarted = 0, kBigPaths, kBigClosest, kBigShadow, kBigVisit, kBigTotal = 8, kBigOffset, kBigFilm, kBigDrainRays
-};
-// The drain: once every path of the render has started and no more than kDrainRays paths
-// are left, k_sfinish traces each of them to its end in one thread (extend, shade and
-// shadow rays in a loop, as the batch megakernel does).  The last iterations of a pool
-// hold few paths, and each would otherwise cost a full round of launches timed by its
-// slowest ray; one thread per path pays for a path's own rays only.
-#ifndef SPGPU_DRAIN_RAYS
-#define SPGPU_DRAIN_RAYS 131072
-#endif
-constexpr int kDrainRays = SPGPU_DRAIN_RAYS;
+// call: [8] paths of the render (spp * npix), [9] sample offset, [10] film address
+enum : int { kBigStarted = 0, kBigPaths, kBigClosest, kBigShadow, kBigVisit, kBigTotal = 8, kBigOffset, kBigFilm };
 constexpr int kNumBig = 12;
 
 // a path's depth (bits 0..7) and specular flag (bit 8), carried in the w of its direction
@@ -81,7 +66,6 @@ struct StreamArgs {
     uint32_t seed;
     int direct;
     int cap;           // path slots
-    int drainRays;     // most paths k_sfinish takes on (0: no drain kernel work)
     // the pool: (origin, pixel), (direction, depth | specular << 8), (throughput, sample)
     float4 *rO, *rD, *rB;
     // class queues, cap rows per class: the pool record and the hit (t, slot, u, v)
@@ -287,101 +271,7 @@ __global__ void k_sadvance(StreamArgs p) {
     p.ctr[kCtrDone] = (p.ctr[kCtrRays] == 0 && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p)) ? 1 : 0;
 }
 
-// the drain (see kDrainRays): after k_sadvance, when every path has started and at most
-// p.drainRays are left, each thread takes whole paths from the pool and traces them to
-// their end; the last block to finish empties the pool and raises the done flag
-template <bool STATS>
-__global__ void __launch_bounds__(kTraceBlock) k_sfinish(StreamArgs p) {
-    __shared__ uint2 stack[kStackShared * kTraceBlock];
-    __shared__ bool sLast;
-    const int n = p.ctr[kCtrRays];
-    if (!(n > 0 && n <= p.drainRays && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p))) return;
-    float4 *film = filmOf(p);
-    bool overflow = false;
-    uint32_t nodeC = 0, triC = 0, nodeS = 0, triS = 0;
-    unsigned long long nClosest = 0, nShadow = 0;
-    while (true) {
-        const int i = atomicAdd(&p.ctr[kCtrFetchF], 1);
-        if (i >= n) break;
-        const float4 o4 = p.rO[i], d4 = p.rD[i], b4 = p.rB[i];
-        const int pix = __float_as_int(o4.w), sample = __float_as_int(b4.w);
-        int meta = __float_as_int(d4.w);
-        const int fi = filmIndexS(p, pix);
-        float3 o = xyz(o4), d = xyz(d4), beta = xyz(b4), L = mk(0, 0, 0);
-        for (int guard = 0; guard <= 255; guard++) {   // a path ends within maxDepth + 1 vertices
-            const int depth = meta & 255;
-            const bool spec = (meta & 256) != 0;
-            float tmax = kInfT, u, v;
-            int slot;
-            nClosest++;
-            const bool hit = traceWide<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, o, d, 0.0f, tmax,
-                                                     slot, u, v, stack + threadIdx.x, kTraceBlock, &nodeC, &triC,
-                                                     &overflow);
-            if (!hit) {
-                if (p.sv.hasEnv && (depth == 0 || spec)) L = L + beta * envLe(p.sv.env, d);
-                break;
-            }
-            HitRecord h;
-            h.t = tmax;
-            h.prim = slot;
-            h.u = u;
-            h.v = v;
-            ShadeResult R;
-            shadeHit(p.sv, h, o, d, beta, spec, depth, p.maxDepth, p.seed, static_cast<uint32_t>(fi),
-                     static_cast<uint32_t>(sample), fi, R, p.direct != 0);
-            L = L + R.emit;
-            if (R.sh0) {
-                nShadow++;
-                float tm = R.s0D.w;
-                if (!traceWide<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(R.s0O), xyz(R.s0D),
-                                            0.0f, tm, slot, u, v, stack + threadIdx.x, kTraceBlock, &nodeS, &triS,
-                                            &overflow))
-                    L = L + xyz(R.s0L);
-            }
-            if (R.sh1) {
-                nShadow++;
-                float tm = R.s1D.w;
-                if (!traceWide<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, xyz(R.s1O), xyz(R.s1D),
-                                            0.0f, tm, slot, u, v, stack + threadIdx.x, kTraceBlock, &nodeS, &triS,
-                                            &overflow))
-                    L = L + xyz(R.s1L);
-            }
-            if (!R.cont || p.direct) break;
-            o = xyz(R.cO);
-            d = xyz(R.cD);
-            beta = R.beta;
-            meta = (depth + 1) | (R.spec ? 256 : 0);
-        }
-        if (!isBlack(L)) atomicAdd(&film[fi], make_float4(L.x, L.y, L.z, 0.0f));
-    }
-    if (overflow) atomicOr(&p.ctr[kCtrErr], 1);
-    if (nClosest) {
-        atomicAdd(&p.big[kBigClosest], nClosest);
-        atomicAdd(&p.big[kBigDrainRays], nClosest);
-    }
-    if (nShadow) atomicAdd(&p.big[kBigShadow], nShadow);
-    if (STATS) {
-        atomicAdd(&p.big[kBigVisit + 0], static_cast<unsigned long long>(nodeC));
-        atomicAdd(&p.big[kBigVisit + 1], static_cast<unsigned long long>(triC));
-        atomicAdd(&p.big[kBigVisit + 2], static_cast<unsigned long long>(nodeS));
-        atomicAdd(&p.big[kBigVisit + 3], static_cast<unsigned long long>(triS));
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        sLast = atomicAdd(&p.ctr[kCtrFinBlocks], 1) == static_cast<int>(gridDim.x) - 1;
-    }
-    __syncthreads();
-    if (sLast && threadIdx.x == 0) {
-        __threadfence();
-        p.ctr[kCtrRays] = 0;
-        p.ctr[kCtrFetchF] = 0;
-        p.ctr[kCtrFinBlocks] = 0;
-        p.ctr[kCtrDone] = 1;
-    }
-}
-
-enum KernelClassS { kSRegen = 0, kSExtend, kSShadeL, kSShadeC, kSShadeD, kSShadow, kSAdvance, kSDrain, kSNumClasses };
+enum KernelClassS { kSRegen = 0, kSExtend, kSShadeL, kSShadeC, kSShadeD, kSShadow, kSAdvance, kSNumClasses };
 
 struct GridsS {
     int trace, shade, regen;
@@ -433,9 +323,6 @@ void launchIteration(const StreamArgs &a, const GridsS &g, cudaStream_t s, cudaE
     done();
     mark(kSAdvance);
     k_sadvance<<<1, 32, 0, s>>>(a);
-    done();
-    mark(kSDrain);
-    k_sfinish<STATS><<<g.trace, kTraceBlock, 0, s>>>(a);
     done();
 }
 
@@ -500,7 +387,6 @@ int setupStream(Ctx &C, StreamQueues &q, const float *camera, int W, int H, int 
     a.seed = seed;
     a.direct = integrator == SPGPU_INTEGRATOR_DIRECT ? 1 : 0;
     a.cap = q.capacity;
-    a.drainRays = kDrainRays;
     a.rO = q.rO;
     a.rD = q.rD;
     a.rB = q.rB;
@@ -685,15 +571,12 @@ int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, in
     StreamArgs a;
     StreamQueues &q = C.sq[0];
     if (int rc = setupStream(C, q, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
-    // the profile times the wavefront kernels alone: no drain, so that every closest-hit ray
-    // is traced by k_sextend and the extend roofline counts exactly its own rays
-    a.drainRays = 0;
     const GridsS g = streamGrids(C.device, a.cap);
     const long long total = static_cast<long long>(W) * H * spp;
     const StreamInit init = streamInit(total, sampleOffset, film);
     const long long bound = iterationBound(a, total);
-    std::vector<cudaEvent_t> ev(2 * kSNumClasses);
-    std::vector<int> cls(kSNumClasses + 1);
+    std::vector<cudaEvent_t> ev(2 * 7);
+    std::vector<int> cls(8);
     for (auto &x : ev) cudaEventCreate(&x);
     unsigned long long big[kNumBig] = {};
     int ctr[kNumCtr] = {};

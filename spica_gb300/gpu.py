@@ -58,11 +58,7 @@ class KernelProfile(C.Structure):
                 ("shadow_tris_per_ray", C.c_double)]
 
 
-# kernel classes of spgpu_render_profile: camera rays (k_sregen / k_raygen), closest hit,
-# the three shading classes, shadow rays, the per-iteration or per-pass bookkeeping
-# (k_sadvance / k_finish), and the streaming wavefront's drain kernel (k_sfinish)
-KERNEL_CLASSES = ["raygen", "extend", "shade_lambert", "shade_conductor", "shade_dielectric", "shadow", "finish",
-                  "drain"]
+KERNEL_CLASSES = ["raygen", "extend", "shade_lambert", "shade_conductor", "shade_dielectric", "shadow", "finish"]
 
 
 class BatchItem(C.Structure):
