@@ -40,6 +40,10 @@ namespace spgpu {
 namespace {
 
 constexpr int kShadeBlockS = 128;
+#ifndef SPGPU_TRACE_MIN_BLOCKS
+#define SPGPU_TRACE_MIN_BLOCKS 8
+#endif
+constexpr int kTraceMinBlocks = SPGPU_TRACE_MIN_BLOCKS;   // resident traversal blocks per SM (register budget)
 constexpr int kIterPerGraph = 8;
 constexpr int kReplayLag = 2;
 constexpr int kDoneRing = StreamQueues::kEvents;
@@ -126,7 +130,7 @@ __global__ void k_sregen(StreamArgs p) {
 }
 
 template <bool STATS>
-__global__ void __launch_bounds__(kTraceBlock, 8) k_sextend(StreamArgs p) {
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(StreamArgs p) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     uint32_t nodeCount = 0, triCount = 0;
     const int n = p.ctr[kCtrRays] + newPaths(p);
@@ -227,7 +231,7 @@ __global__ void __launch_bounds__(kShadeBlockS) k_sshade(StreamArgs p) {
 }
 
 template <bool STATS>
-__global__ void __launch_bounds__(kTraceBlock, 8) k_sshadow(StreamArgs p) {
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sshadow(StreamArgs p) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     const int n = p.ctr[kCtrShadow];
     float4 *film = filmOf(p);
