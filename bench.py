@@ -51,9 +51,10 @@ CONFIG = {"workload": "mid-scale plain render: 500 instances, ~2.03M triangles, 
 
 E2E_SPP = 16   # samples per pixel per host-API render call in the end-to-end measurement
 PASS_LANES = 8   # sample passes in flight (spgpu_config.pass_lanes 0 = 8)
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one sample pass's 17 extend
-# launches on the 1920x1080 workload, averaged per launch.  A constant: it is measured
-# by the ncu command in profiles/ and must be re-measured whenever the tree, the
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the extend launches of the
+# per-kernel profile below (one pool, 8 samples per pixel, 1920x1080), averaged per
+# launch.  A constant: it is measured by the ncu command in
+# profiles/extend_traffic_stream_1080p.md and must be re-measured whenever the tree, the
 # traversal or the queue layout changes.
 EXTEND_DRAM_BYTES_PER_LAUNCH = 28.68e6
 

@@ -58,7 +58,7 @@ public:
         const int n = static_cast<int>(owner_.size());
         std::vector<int32_t> mat(n, 0);
         const float grey[8] = {SPGPU_MAT_LAMBERT, 0.5f, 0.5f, 0.5f, 0, 0, 0, 0};
-        spgpu_config cfg = {device_, 0, {0}};
+        spgpu_config cfg = {device_, 0, 0, {0}};
         check(spgpu_create(&cfg, &ctx_));
         check(spgpu_upload_scene(ctx_, n, verts.data(), mat.data(), 1, grey, nullptr, 0, 0, nullptr));
         check(spgpu_build_bvh(ctx_));

@@ -57,6 +57,7 @@ public:
     explicit GpuPathIntegrator(RenderParams &params)
         : device_{params.getInt("gpuDevice", 0, true)},
           passLanes_{params.getInt("gpuPassLanes", 0, true)},
+          wavefront_{params.getInt("gpuWavefront", 0, true)},
           seed_{static_cast<uint32_t>(params.getInt("seed", 0, true))} {}
 
     void render(const std::shared_ptr<const Camera> &camera, const Scene &scene, RenderParams &params) override {
@@ -102,7 +103,7 @@ public:
                 }
         }
         spgpu_ctx *ctx = nullptr;
-        spgpu_config cfg = {device_, passLanes_, {0}};
+        spgpu_config cfg = {device_, passLanes_, wavefront_, {0}};
         check(spgpu_create(&cfg, &ctx));
         check(spgpu_upload_scene(ctx, static_cast<int32_t>(triMat.size()), verts.data(), triMat.data(),
                                  static_cast<int32_t>(mats.size() / 8), mats.data(), emit.data(), ew, eh,
@@ -170,7 +171,8 @@ private:
     }
 
     int device_;
-    int passLanes_;   // sample passes in flight (spgpu_config::pass_lanes; 0 = default)
+    int passLanes_;   // pass-by-pass wavefront: sample passes in flight (spgpu_config::pass_lanes; 0 = default)
+    int wavefront_;   // spgpu_config::wavefront: 0 streaming (default), 1 pass by pass
     uint32_t seed_;
 };
 
