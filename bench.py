@@ -56,7 +56,7 @@ PASS_LANES = 8   # sample passes in flight (spgpu_config.pass_lanes 0 = 8)
 # launch.  A constant: it is measured by the ncu command in
 # profiles/extend_traffic_stream_1080p.md and must be re-measured whenever the tree, the
 # traversal or the queue layout changes.
-EXTEND_DRAM_BYTES_PER_LAUNCH = 28.68e6
+EXTEND_DRAM_BYTES_PER_LAUNCH = 201.04e6
 
 
 def max_over_ranks(torch, x: float, ws: int, device: str = "cuda") -> float:
