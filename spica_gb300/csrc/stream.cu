@@ -44,8 +44,14 @@ constexpr int kShadeBlockS = 128;
 #define SPGPU_TRACE_MIN_BLOCKS 8
 #endif
 constexpr int kTraceMinBlocks = SPGPU_TRACE_MIN_BLOCKS;   // resident traversal blocks per SM (register budget)
-constexpr int kIterPerGraph = 8;
-constexpr int kReplayLag = 2;
+#ifndef SPGPU_ITER_PER_GRAPH
+#define SPGPU_ITER_PER_GRAPH 8
+#endif
+#ifndef SPGPU_REPLAY_LAG
+#define SPGPU_REPLAY_LAG 2
+#endif
+constexpr int kIterPerGraph = SPGPU_ITER_PER_GRAPH;   // iterations captured in one graph
+constexpr int kReplayLag = SPGPU_REPLAY_LAG;          // replays in flight before the host reads a done flag
 constexpr int kDoneRing = StreamQueues::kEvents;
 // counters (ints): [0] rays in the pool, [1] continuations written, [2..4] class
 // counts, [5] shadow rays, [6] extend ray fetch, [7] shadow ray fetch, [8] done, [9]
