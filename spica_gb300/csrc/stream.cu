@@ -48,7 +48,7 @@ constexpr int kTraceMinBlocks = SPGPU_TRACE_MIN_BLOCKS;   // resident traversal 
 #define SPGPU_ITER_PER_GRAPH 8
 #endif
 #ifndef SPGPU_REPLAY_LAG
-#define SPGPU_REPLAY_LAG 2
+#define SPGPU_REPLAY_LAG 1
 #endif
 constexpr int kIterPerGraph = SPGPU_ITER_PER_GRAPH;   // iterations captured in one graph
 constexpr int kReplayLag = SPGPU_REPLAY_LAG;          // replays in flight before the host reads a done flag
