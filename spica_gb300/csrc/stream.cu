@@ -57,17 +57,7 @@ constexpr int kDoneRing = StreamQueues::kEvents;
 // counts, [5] shadow rays, [6] extend ray fetch, [7] shadow ray fetch, [8] done, [9]
 // iterations, [10] error flags
 enum : int { kCtrRays = 0, kCtrCont, kCtrClass0, kCtrShadow = 5, kCtrFetchE, kCtrFetchS, kCtrDone, kCtrIter, kCtrErr };
-// Continuations are written into kBins bins by the octant of their direction (one bin:
-// no binning), so that the rays of a warp in the next extend share their octant and with
-// it the order in which they visit a node's children; camera rays of the iteration go to
-// a segment of their own after the bins.  [16 + b] continuations written into bin b,
-// [24 + b] rays of bin b in the pool this iteration.
-#ifndef SPGPU_OCTANT_BINS
-#define SPGPU_OCTANT_BINS 1
-#endif
-constexpr int kBins = SPGPU_OCTANT_BINS ? 8 : 1;
-constexpr int kCtrBinCont0 = 16, kCtrBinHave0 = 24;
-constexpr int kNumCtr = 32;
+constexpr int kNumCtr = 16;
 // 64-bit counters: [0] paths started, [1] paths, [2] closest rays, [3] shadow rays,
 // [4..7] visits (extend nodes, triangles, shadow nodes, triangles); then the call's own
 // parameters, written by the host per render so that one captured graph serves every
@@ -122,40 +112,8 @@ __device__ __forceinline__ int warpAppendS(bool want, int *counter) {
     return want ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
-// warp-aggregated append of the wanting lanes to counters[key]: one atomic per key
-__device__ __forceinline__ int warpAppendKeyed(bool want, int key, int *counters) {
-    const unsigned active = __activemask();
-    if (!__ballot_sync(active, want)) return -1;
-    const unsigned group = __match_any_sync(active, want ? key : -1);
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(group) - 1;
-    int base = 0;
-    if (want && lane == leader) base = atomicAdd(&counters[key], __popc(group));
-    base = __shfl_sync(active, base, leader);
-    return want ? base + __popc(group & ((1u << lane) - 1u)) : -1;
-}
-
-__device__ __forceinline__ int dirOctant(float4 d) { return (d.x < 0.0f) | ((d.y < 0.0f) << 1) | ((d.z < 0.0f) << 2); }
-
-// the pool slot of ray i of this iteration: the bins in order, then the camera rays
-__device__ __forceinline__ int64_t poolSlot(const StreamArgs &p, const int *have, int i) {
-    int seg = kBins;
-#pragma unroll
-    for (int b = 0; b < kBins; b++) {
-        if (seg == kBins) {
-            if (i < have[b]) seg = b;
-            else i -= have[b];
-        }
-    }
-    return static_cast<int64_t>(seg) * p.cap + i;
-}
-
-__device__ __forceinline__ void loadHave(const StreamArgs &p, int *have) {
-#pragma unroll
-    for (int b = 0; b < kBins; b++) have[b] = p.ctr[kCtrBinHave0 + b];
-}
-
 __global__ void k_sregen(StreamArgs p) {
+    const int have = p.ctr[kCtrRays];
     const int nNew = newPaths(p);
     const long long started = static_cast<long long>(p.big[kBigStarted]);
     const int sampleOffset = static_cast<int>(p.big[kBigOffset]);
@@ -169,7 +127,7 @@ __global__ void k_sregen(StreamArgs p) {
         const Rand4 r = rand4(p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), 0xFFFFu, 0u);
         float3 o, d;
         spawnCameraRay(p.cam, x, y, r.a, r.b, &o, &d);
-        const int64_t k = static_cast<int64_t>(kBins) * p.cap + j;   // the camera-ray segment
+        const int k = have + j;
         p.rO[k] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
         p.rD[k] = make_float4(d.x, d.y, d.z, packMeta(0, false));
         p.rB[k] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(sample));
@@ -183,13 +141,10 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
     uint32_t nodeCount = 0, triCount = 0;
     const int n = p.ctr[kCtrRays] + newPaths(p);
     float4 *film = filmOf(p);
-    int have[kBins];
-    loadHave(p, have);
     bool overflow = false;
     auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
-        const int64_t s = poolSlot(p, have, i);
-        *o = xyz(p.rO[s]);
-        *d = xyz(p.rD[s]);
+        *o = xyz(p.rO[i]);
+        *d = xyz(p.rD[i]);
         *t0 = 0.0f;
         *t1 = kInfT;
     };
@@ -198,10 +153,9 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
         int cls = -1;
         float4 o4 = make_float4(0, 0, 0, 0), d4 = o4, b4 = o4;
         if (i >= 0) {
-            const int64_t s = poolSlot(p, have, i);
-            o4 = p.rO[s];
-            d4 = p.rD[s];
-            b4 = p.rB[s];
+            o4 = p.rO[i];
+            d4 = p.rD[i];
+            b4 = p.rB[i];
             if (L.found) {
                 cls = shadeClass(__ldg(&p.sv.mats[__ldg(&p.sv.slotShade[L.hitSlot]).x].type));
             } else if (p.sv.hasEnv) {
@@ -261,14 +215,11 @@ __global__ void __launch_bounds__(kShadeBlockS) k_sshade(StreamArgs p) {
                      static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), fi, R, p.direct != 0);
             if (!isBlack(R.emit)) atomicAdd(&film[fi], make_float4(R.emit.x, R.emit.y, R.emit.z, 0.0f));
         }
-        const bool cont = R.cont && !p.direct;
-        const int oct = kBins == 1 ? 0 : dirOctant(R.cD);
-        const int k = warpAppendKeyed(cont, oct, &p.ctr[kCtrBinCont0]);
+        const int k = warpAppendS(R.cont && !p.direct, &p.ctr[kCtrCont]);
         if (k >= 0) {
-            const int64_t slot = static_cast<int64_t>(oct) * p.cap + k;
-            p.rO[slot] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pix));
-            p.rD[slot] = make_float4(R.cD.x, R.cD.y, R.cD.z, packMeta((meta & 255) + 1, R.spec));
-            p.rB[slot] = make_float4(R.beta.x, R.beta.y, R.beta.z, __int_as_float(sample));
+            p.rO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pix));
+            p.rD[k] = make_float4(R.cD.x, R.cD.y, R.cD.z, packMeta((meta & 255) + 1, R.spec));
+            p.rB[k] = make_float4(R.beta.x, R.beta.y, R.beta.z, __int_as_float(sample));
         }
         const int s0 = warpAppendS(R.sh0, &p.ctr[kCtrShadow]);
         if (s0 >= 0) {
@@ -324,14 +275,7 @@ __global__ void k_sadvance(StreamArgs p) {
     p.big[kBigPaths] += static_cast<unsigned long long>(nNew);
     p.big[kBigClosest] += static_cast<unsigned long long>(n);
     p.big[kBigShadow] += static_cast<unsigned long long>(p.ctr[kCtrShadow]);
-    int cont = 0;
-    for (int b = 0; b < kBins; b++) {
-        const int c = p.ctr[kCtrBinCont0 + b];
-        p.ctr[kCtrBinHave0 + b] = c;
-        p.ctr[kCtrBinCont0 + b] = 0;
-        cont += c;
-    }
-    p.ctr[kCtrRays] = cont;
+    p.ctr[kCtrRays] = p.ctr[kCtrCont];
     for (int k = kCtrCont; k <= kCtrFetchS; k++) p.ctr[k] = 0;
     if (n > 0) p.ctr[kCtrIter] += 1;
     p.ctr[kCtrDone] = (p.ctr[kCtrRays] == 0 && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p)) ? 1 : 0;
@@ -406,8 +350,7 @@ int ensureStreamQueues(StreamQueues &q, int cap) {
         return cudaMalloc(reinterpret_cast<void **>(ptr), sizeof(T) * std::max<size_t>(count, 1)) == cudaSuccess;
     };
     const size_t c = static_cast<size_t>(cap);
-    const size_t pool = (kBins + 1) * c;   // the bins and the camera-ray segment, cap slots each
-    bool ok = alloc(&q.rO, pool) && alloc(&q.rD, pool) && alloc(&q.rB, pool) && alloc(&q.qO, 3 * c) && alloc(&q.qD, 3 * c) &&
+    bool ok = alloc(&q.rO, c) && alloc(&q.rD, c) && alloc(&q.rB, c) && alloc(&q.qO, 3 * c) && alloc(&q.qD, 3 * c) &&
               alloc(&q.qB, 3 * c) && alloc(&q.qH, 3 * c) && alloc(&q.shO, 2 * c) && alloc(&q.shD, 2 * c) &&
               alloc(&q.shL, 2 * c) && alloc(&q.ctr, kNumCtr) && alloc(&q.big, kNumBig);
     if (ok) ok = cudaMallocHost(reinterpret_cast<void **>(&q.doneHost), sizeof(int) * kDoneRing) == cudaSuccess;
