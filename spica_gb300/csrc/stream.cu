@@ -44,6 +44,10 @@ constexpr int kShadeBlockS = 128;
 #define SPGPU_TRACE_MIN_BLOCKS 8
 #endif
 constexpr int kTraceMinBlocks = SPGPU_TRACE_MIN_BLOCKS;   // resident traversal blocks per SM (register budget)
+#ifndef SPGPU_SHADE_MIN_BLOCKS
+#define SPGPU_SHADE_MIN_BLOCKS 1
+#endif
+constexpr int kShadeMinBlocks = SPGPU_SHADE_MIN_BLOCKS;   // resident shading blocks per SM (register budget)
 #ifndef SPGPU_ITER_PER_GRAPH
 #define SPGPU_ITER_PER_GRAPH 8
 #endif
@@ -189,7 +193,7 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
 }
 
 template <int CLS>
-__global__ void __launch_bounds__(kShadeBlockS) k_sshade(StreamArgs p) {
+__global__ void __launch_bounds__(kShadeBlockS, kShadeMinBlocks) k_sshade(StreamArgs p) {
     const int n = p.ctr[kCtrClass0 + CLS];
     const int stride = gridDim.x * blockDim.x;
     const int nIter = (n + stride - 1) / stride;   // uniform trip count keeps warps whole for the ballots
