@@ -45,7 +45,7 @@ constexpr int kShadeBlockS = 128;
 #endif
 constexpr int kTraceMinBlocks = SPGPU_TRACE_MIN_BLOCKS;   // resident traversal blocks per SM (register budget)
 #ifndef SPGPU_SHADE_MIN_BLOCKS
-#define SPGPU_SHADE_MIN_BLOCKS 1
+#define SPGPU_SHADE_MIN_BLOCKS 6
 #endif
 constexpr int kShadeMinBlocks = SPGPU_SHADE_MIN_BLOCKS;   // resident shading blocks per SM (register budget)
 #ifndef SPGPU_ITER_PER_GRAPH
