@@ -63,9 +63,18 @@ struct BatchState {
 namespace {
 
 constexpr int kMaxBatchBlock = 256;
+// resident threads per SM the megakernel is compiled for (0: no bound; the register
+// budget is then the compiler's)
+#ifndef SPGPU_BATCH_THREADS_PER_SM
+#define SPGPU_BATCH_THREADS_PER_SM 0
+#endif
+template <int BLOCK>
+constexpr int batchMinBlocks() {
+    return SPGPU_BATCH_THREADS_PER_SM > 0 ? (SPGPU_BATCH_THREADS_PER_SM + BLOCK - 1) / BLOCK : 1;
+}
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_batch(SceneView base, const RenderMeta *__restrict__ meta,
+__global__ void __launch_bounds__(BLOCK, batchMinBlocks<BLOCK>()) k_batch(SceneView base, const RenderMeta *__restrict__ meta,
                                                  const BatchItem *__restrict__ items, int nItems, float4 *film,
                                                  int *ctl, unsigned long long *times, unsigned long long *stats) {
     __shared__ uint2 stack[kStackShared * BLOCK];
