@@ -66,7 +66,7 @@ constexpr int kMaxBatchBlock = 256;
 // resident threads per SM the megakernel is compiled for (0: no bound; the register
 // budget is then the compiler's)
 #ifndef SPGPU_BATCH_THREADS_PER_SM
-#define SPGPU_BATCH_THREADS_PER_SM 0
+#define SPGPU_BATCH_THREADS_PER_SM 1024
 #endif
 template <int BLOCK>
 constexpr int batchMinBlocks() {
