@@ -13,7 +13,10 @@ namespace spgpu {
 // one node group per level of the current path: its first kStackShared entries live
 // in shared memory, deeper ones spill to a per-thread local array.
 constexpr int kStackDepth = 48;
-constexpr int kStackShared = 16;
+#ifndef SPGPU_STACK_SHARED
+#define SPGPU_STACK_SHARED 16
+#endif
+constexpr int kStackShared = SPGPU_STACK_SHARED;
 constexpr int kTraceBlock = 128;
 
 struct DeviceBVH {
@@ -245,7 +248,10 @@ __device__ __forceinline__ bool traceWide(const WideNode *__restrict__ nodes, co
 // 2009).  fetch(i, &o, &d, &tmin, &tmax) loads ray i; done(i, L) consumes its result.
 // All 32 lanes of each warp execute every iteration of the loop (warp-uniform control),
 // so done() may use warp-collective operations.
-constexpr int kRefill = 8;
+#ifndef SPGPU_REFILL
+#define SPGPU_REFILL 8
+#endif
+constexpr int kRefill = SPGPU_REFILL;
 
 template <bool ANY, bool STATS, class Fetch, class Done>
 __device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nodes,
