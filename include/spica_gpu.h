@@ -276,7 +276,10 @@ typedef struct {
                               * the barrier is never signalled; the wait is cut to 1024
                               * polls); the call then returns SPGPU_EKERNEL and the context
                               * stays usable.  0 otherwise. */
-    int32_t reserved[2];
+    int32_t guided_bounces;   /* wavefront guided passes: the network samples at bounces
+                                 0 .. guided_bounces - 1 and plain BSDF sampling at the
+                                 others; 0 (or negative): at every bounce but the last */
+    int32_t reserved[1];
 } spgpu_guiding_config;
 
 #define SPGPU_GUIDE_FAULT_WAIT 1

@@ -14,7 +14,7 @@ namespace spgpu {
 // in shared memory, deeper ones spill to a per-thread local array.
 constexpr int kStackDepth = 48;
 #ifndef SPGPU_STACK_SHARED
-#define SPGPU_STACK_SHARED 16
+#define SPGPU_STACK_SHARED 8
 #endif
 constexpr int kStackShared = SPGPU_STACK_SHARED;
 constexpr int kTraceBlock = 128;

@@ -232,6 +232,7 @@ struct GuideView {
     float *ring;              // training-sample ring, 16 floats per entry
     int capacity;
     int *ringCtl;             // [0] entries written (monotonic)
+    int guidedBounces;        // bounces 0 .. guidedBounces-1 sample the network (0: all but the last)
 };
 
 // guide.cu: grid of a persistent kernel that runs the network per 128-thread CTA

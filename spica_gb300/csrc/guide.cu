@@ -1000,6 +1000,7 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
             gv.ring = G->samples;
             gv.capacity = G->capacity;
             gv.ringCtl = G->ctl;
+            gv.guidedBounces = G->cfg.guided_bounces;
         }
         return renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
                            d->integrator, film, statsOut, msOut, s, guided ? &gv : nullptr);

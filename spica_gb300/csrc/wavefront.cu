@@ -67,6 +67,7 @@ struct PassArgs {
     const float *biasPad;
     float3 guideLo, guideInvExt;
     float guideAlpha;
+    int guidedBounces;   // network sampling at bounces below this one (0: all but the last)
     // training-sample collection (guided passes with collect != 0): radiance gathered by
     // each path, its record count (kRecOpen: the last record waits for the hit of its
     // continuation ray), the records, and the training ring they end in
@@ -530,7 +531,7 @@ void launchPass(const PassArgs &a, const Grids &g, cudaStream_t cs, size_t ctrBy
         else k_extend<STATS><<<g.trace, kTraceBlock, 0, cs>>>(a, b);
         done();
         mark(kShadeL);
-        if (a.packFwd && b < a.maxDepth) {
+        if (a.packFwd && b < a.maxDepth && (a.guidedBounces <= 0 || b < a.guidedBounces)) {
             if (a.collect) k_shade_guided<true><<<g.guided, kGTile, kTileSmem, cs>>>(a, b);
             else k_shade_guided<false><<<g.guided, kGTile, kTileSmem, cs>>>(a, b);
         } else {
@@ -622,6 +623,7 @@ int setupPass(Ctx &C, RenderQueues &q, const float *camera, int W, int H, int ma
         a.packFwd = gv->packFwd;
         a.biasPad = gv->biasPad;
         a.guideAlpha = gv->alpha;
+        a.guidedBounces = gv->guidedBounces;
         if (gv->collect) {
             if (!q.recs) {
                 cudaMalloc(&q.pathL, sizeof(float4) * q.capacity);

@@ -74,7 +74,7 @@ class BatchTuning(C.Structure):
 class GuidingConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("bsdf_fraction", C.c_float), ("batch", C.c_int32),
                 ("seed", C.c_uint32), ("capacity", C.c_int32), ("fault_injection", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("guided_bounces", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 GUIDE_GUIDED, GUIDE_COLLECT, GUIDE_MEGAKERNEL = 1, 2, 4
@@ -608,11 +608,11 @@ class GpuGuide:
     """Learned guiding on a constructed accelerator's scene (spgpu_guiding_*)."""
 
     def __init__(self, accel: GpuBVHAccel, lr: float = 1e-3, bsdf_fraction: float = 0.3, batch: int = 16384,
-                 seed: int = 0, capacity: int = 1 << 21, fault_injection: int = 0):
+                 seed: int = 0, capacity: int = 1 << 21, fault_injection: int = 0, guided_bounces: int = 0):
         self.accel = accel
         self.ctx = accel.ctx
         cfg = GuidingConfig(learning_rate=lr, bsdf_fraction=bsdf_fraction, batch=batch, seed=seed,
-                            capacity=capacity, fault_injection=fault_injection)
+                            capacity=capacity, fault_injection=fault_injection, guided_bounces=guided_bounces)
         _check(self.ctx.lib.spgpu_guiding_init(self.ctx.h, C.byref(cfg)), "spgpu_guiding_init")
 
     def params(self):

@@ -172,6 +172,32 @@ def test_streaming_and_pass_by_pass_render_the_same_samples(gpulib, scene):
         assert close.mean() > 0.999, close.mean()
 
 
+def test_streaming_pool_refills_within_a_sample(gpulib):
+    """A film larger than a streaming pool (4096 x 2304 = 9.4M pixels, 2^23 path slots per
+    pool): each pool refills while its sample is still in flight, and the film holds the
+    same samples as the pass-by-pass wavefront's: every pixel's count, the path and ray
+    counts, and the sums up to the order of the film's additions."""
+    from spica_gb300.gpu import Context
+    sc = scenes.box_room(width=4096, height=2304)
+    params = {"width": 4096, "height": 2304, "maxDepth": 8, "sampleCount": 2}
+    out = {}
+    for wf in (0, 1):
+        acc = GpuBVHAccel(sc, ctx=Context(0, pass_lanes=1, wavefront=wf)).construct()
+        integ = GpuPathIntegrator(seed=17)
+        film = integ.render(sc.camera, acc, params, sample_offset=3)
+        st = integ.last_stats
+        out[wf] = (film, (st.paths, st.rays_closest, st.rays_shadow), st.kernel_launches)
+    (fs, ss, ls), (fp, sp, lp) = out[0], out[1]
+    assert ss == sp and ss[0] == 2 * 4096 * 2304
+    # streaming: replays of 8 iterations of 7 kernels; pass by pass: 2 + 5 (depth + 1) per pass
+    assert ls > 0 and ls % 56 == 0 and lp == 2 * (2 + 5 * 9)
+    np.testing.assert_array_equal(fs[..., 3], fp[..., 3])
+    assert np.all(fs[..., 3] == 2)
+    scale = float(np.abs(fp[..., :3]).max())
+    close = np.abs(fs[..., :3] - fp[..., :3]) <= 1e-5 * np.abs(fp[..., :3]) + 1e-6 * scale
+    assert close.mean() > 0.999, close.mean()
+
+
 def test_checkpoint_resume_continues_the_sample_index(gpulib, tmp_path):
     """Checkpoint / resume: the film (sum of L, sample count) saved after k samples and
     rendered on from sample_offset = k holds exactly the samples of one uninterrupted
