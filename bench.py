@@ -341,8 +341,9 @@ def batch_bench(torch, GpuBatch, scenes, reps=3, count=64, autotune=True):
 
 def guiding_bench(torch, GpuBVHAccel, scenes, W=1280, H=720, budget_spp=1024, ref_spp=4096):
     """Learned guiding on the indirect-lit room (1280 x 720, max depth 12): relMSE at equal
-    device time (the time of budget_spp plain wavefront samples per pixel) against the
-    plain wavefront path tracer, the guided run training online for the first 25% of it
+    device time (the time of budget_spp plain samples per pixel) against the plain path
+    tracer on the streaming wavefront (the default renderer; guided passes run on it too,
+    collection passes pass by pass), the guided run training online for the first 25% of it
     (collection passes of 2 spp, each followed by 128 Adam steps; their samples kept in
     the image).  relMSE is taken against a ref_spp plain reference with the reference's
     own noise subtracted (its per-pixel variance from 16 independent chunks), which
@@ -380,6 +381,7 @@ def guiding_bench(torch, GpuBVHAccel, scenes, W=1280, H=720, budget_spp=1024, re
                   "frac": flop / (step_ms / 1e3) / 1e12 / peak, "peak_source": src, "ms_per_step": step_ms,
                   "flop_per_step": flop}
     return {"scene": "indirect-lit room, 2418 tris", "width": W, "height": H, "reference_spp": ref_spp,
+            "wavefront": "streaming (plain and guided passes), pass by pass (collection passes)",
             "budget_ms": budget, "relmse_plain": e_p, "relmse_guided": e_g, "equal_time_gain": e_p / e_g,
             "relmse_reference_noise": noise, "equal_time_gain_raw": raw_p / raw_g,
             "per_sample_gain": (e_p * pi["render_spp"] / (e_g * (gi["render_spp"] + gi["kept_training_spp"]))

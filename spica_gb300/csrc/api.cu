@@ -1043,7 +1043,7 @@ int spgpu_guiding_render(spgpu_ctx *h, const spgpu_render_desc *d, float *film, 
         stats->rays_closest = static_cast<int64_t>(st[1]);
         stats->rays_shadow = static_cast<int64_t>(st[2]);
         stats->ms = ms;
-        stats->kernel_launches = 0;
+        stats->kernel_launches = static_cast<int64_t>(st[3]);
     }
     return rc;
 }

@@ -245,12 +245,15 @@ int guideTileKernelGrid(const void *kernel, int device);
 int renderFrame(Ctx *ctx, const float *camera, int width, int height, int spp, int sampleOffset, int maxDepth,
                 uint32_t seed, int integrator, float4 *film, unsigned long long *statsOut, float *msOut,
                 cudaStream_t stream, const GuideView *gv = nullptr);
-// stream.cu: the same render on the streaming wavefront (path pool refilled as paths end)
+// stream.cu: the same render on the streaming wavefront (path pool refilled as paths end);
+// with gv, guided (never collecting) passes
 int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
-                 int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream);
+                 int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream,
+                 const GuideView *gv = nullptr);
 int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth,
                         uint32_t seed, int integrator, float4 *film, double *kernelMs, long long *launches,
-                        unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream);
+                        unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream,
+                        const GuideView *gv = nullptr);
 // the same samples launched kernel by kernel (no graph), each timed by events, then
 // again with BVH visit counters; kernelMs/launches per kernel class
 int renderProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,

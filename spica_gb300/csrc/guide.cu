@@ -1002,6 +1002,12 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
             gv.ringCtl = G->ctl;
             gv.guidedBounces = G->cfg.guided_bounces;
         }
+        // plain and guided passes on the streaming wavefront unless the context asks for
+        // pass-by-pass passes; collection passes keep per-path records in one slot for
+        // the whole path, which the pass-by-pass wavefront provides
+        if (!collect && C.wavefront == 0)
+            return renderStream(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
+                                d->integrator, film, statsOut, msOut, s, guided ? &gv : nullptr);
         return renderFrame(&C, d->camera, d->width, d->height, d->spp, d->sample_offset, d->max_depth, d->seed,
                            d->integrator, film, statsOut, msOut, s, guided ? &gv : nullptr);
     }
@@ -1070,6 +1076,7 @@ int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film,
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cudaFail("spgpu_guiding_render", e);
     for (int k = 0; k < 3; k++) statsOut[k] = st[k];
+    statsOut[3] = 1;   // one persistent launch
     *msOut = ms;
     if (err) {
         setError("spgpu_guiding_render: traversal overflow or tensor-core wait timed out");

@@ -17,6 +17,8 @@
 //                    into the pool, shadow rays into the shadow queue
 //   shadow           any-hit for the shadow rays; unoccluded ones add to the film
 //   advance          counters for the next iteration, the render's done flag
+// A guided render (learned guiding proposal) shades the Lambert queue with the network
+// instead (k_sshade_guided: tensor-core tiles of 128 queue rows).
 // A path's random numbers are keyed by (seed, film pixel) and counted by (sample, depth,
 // stream), exactly as in the pass-by-pass wavefront (wavefront.cu), so a render draws the
 // same samples whichever slot or iteration a path runs in; only the order of the film's
@@ -33,6 +35,7 @@
 
 #include "../../include/spica_gpu.h"
 #include "ctx.cuh"
+#include "guided_shade.cuh"
 #include "shade.cuh"
 
 namespace spgpu {
@@ -48,6 +51,10 @@ constexpr int kTraceMinBlocks = SPGPU_TRACE_MIN_BLOCKS;   // resident traversal 
 #define SPGPU_SHADE_MIN_BLOCKS 6
 #endif
 constexpr int kShadeMinBlocks = SPGPU_SHADE_MIN_BLOCKS;   // resident shading blocks per SM (register budget)
+#ifndef SPGPU_GUIDED_MIN_BLOCKS
+#define SPGPU_GUIDED_MIN_BLOCKS 3
+#endif
+constexpr int kGuidedMinBlocks = SPGPU_GUIDED_MIN_BLOCKS;   // resident guided shading blocks per SM
 #ifndef SPGPU_ITER_PER_GRAPH
 #define SPGPU_ITER_PER_GRAPH 8
 #endif
@@ -87,6 +94,14 @@ struct StreamArgs {
     float4 *shO, *shD, *shL;   // shadow queue, 2 * cap rows: (origin, film index), (dir, tmax), contribution
     int *ctr;
     unsigned long long *big;
+    // guided renders: the network's packed weights and biases (null: plain BSDF
+    // sampling), the proposal's BSDF share, the depths that sample it (0: all but the
+    // last), and the scene box that normalises the network's position input
+    const uint8_t *packFwd;
+    const float *biasPad;
+    float guideAlpha;
+    int guidedBounces;
+    float3 guideLo, guideInvExt;
 };
 
 __device__ __forceinline__ int filmIndexS(const StreamArgs &p, int pix) {
@@ -192,13 +207,47 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
     }
 }
 
+// a shaded hit's emission, continuation (back into the pool) and shadow rays; whole
+// warps call this
+__device__ __forceinline__ void emitShadeResultS(const StreamArgs &p, const ShadeResult &R, bool live, int pix,
+                                                 int meta, int sample) {
+    if (live && !isBlack(R.emit))
+        atomicAdd(&filmOf(p)[filmIndexS(p, pix)], make_float4(R.emit.x, R.emit.y, R.emit.z, 0.0f));
+    const int k = warpAppendS(R.cont && !p.direct, &p.ctr[kCtrCont]);
+    if (k >= 0) {
+        p.rO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pix));
+        p.rD[k] = make_float4(R.cD.x, R.cD.y, R.cD.z, packMeta((meta & 255) + 1, R.spec));
+        p.rB[k] = make_float4(R.beta.x, R.beta.y, R.beta.z, __int_as_float(sample));
+    }
+    const int s0 = warpAppendS(R.sh0, &p.ctr[kCtrShadow]);
+    if (s0 >= 0) {
+        p.shO[s0] = R.s0O;
+        p.shD[s0] = R.s0D;
+        p.shL[s0] = R.s0L;
+    }
+    const int s1 = warpAppendS(R.sh1, &p.ctr[kCtrShadow]);
+    if (s1 >= 0) {
+        p.shO[s1] = R.s1O;
+        p.shD[s1] = R.s1D;
+        p.shL[s1] = R.s1L;
+    }
+}
+
+__device__ __forceinline__ HitRecord hitOfRow(float4 h4) {
+    HitRecord h;
+    h.t = h4.x;
+    h.prim = __float_as_int(h4.y);
+    h.u = h4.z;
+    h.v = h4.w;
+    return h;
+}
+
 template <int CLS>
 __global__ void __launch_bounds__(kShadeBlockS, kShadeMinBlocks) k_sshade(StreamArgs p) {
     const int n = p.ctr[kCtrClass0 + CLS];
     const int stride = gridDim.x * blockDim.x;
     const int nIter = (n + stride - 1) / stride;   // uniform trip count keeps warps whole for the ballots
     const int64_t base = static_cast<int64_t>(CLS) * p.cap;
-    float4 *film = filmOf(p);
     for (int it = 0; it < nIter; it++) {
         const int j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
         ShadeResult R;
@@ -210,34 +259,77 @@ __global__ void __launch_bounds__(kShadeBlockS, kShadeMinBlocks) k_sshade(Stream
             meta = __float_as_int(d4.w);
             sample = __float_as_int(b4.w);
             const int fi = filmIndexS(p, pix);
-            HitRecord h;
-            h.t = h4.x;
-            h.prim = __float_as_int(h4.y);
-            h.u = h4.z;
-            h.v = h4.w;
-            shadeHit(p.sv, h, xyz(o4), xyz(d4), xyz(b4), (meta & 256) != 0, meta & 255, p.maxDepth, p.seed,
+            shadeHit(p.sv, hitOfRow(h4), xyz(o4), xyz(d4), xyz(b4), (meta & 256) != 0, meta & 255, p.maxDepth, p.seed,
                      static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), fi, R, p.direct != 0);
-            if (!isBlack(R.emit)) atomicAdd(&film[fi], make_float4(R.emit.x, R.emit.y, R.emit.z, 0.0f));
         }
-        const int k = warpAppendS(R.cont && !p.direct, &p.ctr[kCtrCont]);
-        if (k >= 0) {
-            p.rO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pix));
-            p.rD[k] = make_float4(R.cD.x, R.cD.y, R.cD.z, packMeta((meta & 255) + 1, R.spec));
-            p.rB[k] = make_float4(R.beta.x, R.beta.y, R.beta.z, __int_as_float(sample));
-        }
-        const int s0 = warpAppendS(R.sh0, &p.ctr[kCtrShadow]);
-        if (s0 >= 0) {
-            p.shO[s0] = R.s0O;
-            p.shD[s0] = R.s0D;
-            p.shL[s0] = R.s0L;
-        }
-        const int s1 = warpAppendS(R.sh1, &p.ctr[kCtrShadow]);
-        if (s1 >= 0) {
-            p.shO[s1] = R.s1O;
-            p.shD[s1] = R.s1D;
-            p.shL[s1] = R.s1L;
-        }
+        emitShadeResultS(p, R, j < n, pix, meta, sample);
     }
+}
+
+// Lambert hits of a guided render.  Each CTA takes 128-row tiles of the Lambert queue:
+// every thread forms its row's network inputs, the tile runs through the four layers on
+// the tensor cores (tcgen05, accumulator in TMEM), and each row is shaded with its
+// mixture straight from registers (shadeGuidedLambert).  Rows at the last depth, or past
+// the guided depths, are shaded with plain BSDF sampling as in k_sshade.  The queue
+// mixes depths, so one launch covers what the pass-by-pass wavefront does in one guided
+// launch per bounce.
+__global__ void __launch_bounds__(kGTile, kGuidedMinBlocks) k_sshade_guided(StreamArgs p) {
+    const int n = p.ctr[kCtrClass0 + kMatLambert];
+    if (static_cast<int>(blockIdx.x) * kGTile >= n) return;   // no tile for this CTA
+    extern __shared__ __align__(128) uint8_t sm[];
+    const int64_t base = static_cast<int64_t>(kMatLambert) * p.cap;
+    bool ok = true;
+    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad, &ok);
+    const float *bias = reinterpret_cast<const float *>(sm + kTileSmOffBias);
+    uint8_t *xh = sm + kTileSmOffXH;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+    uint32_t phase = 0;
+    for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
+        const int j = tile * kGTile + static_cast<int>(threadIdx.x);
+        const bool live = j < n;
+        float4 o4 = make_float4(0, 0, 0, 0), d4 = make_float4(0, 0, 1, 0), b4 = o4, h4 = o4;
+        float3 ps = mk(0, 0, 0), nn = mk(0, 0, 1);
+        float xf[16];
+        for (int k = 0; k < 16; k++) xf[k] = 0.0f;
+        if (live) {
+            o4 = p.qO[base + j];
+            d4 = p.qD[base + j];
+            b4 = p.qB[base + j];
+            h4 = p.qH[base + j];
+            ps = hitPoint(xyz(o4), xyz(d4), h4.x);
+            nn = triNormal(p.sv.tris[__float_as_int(h4.y)]);
+            guideFeatures(ps, nn, -xyz(d4), p.guideLo, p.guideInvExt, xf);
+        }
+        storeRow8(xh, threadIdx.x, 0, kGK0, xf);
+        storeRow8(xh, threadIdx.x, 8, kGK0, xf + 8);
+        float raw[kGOut];
+        ok = mlpForwardRow(tmem, sm, bias, xh, bar, phase, raw);   // CTA-uniform
+        if (!ok) break;
+        ShadeResult R;
+        R.cont = R.sh0 = R.sh1 = false;
+        const int pix = __float_as_int(o4.w), meta = __float_as_int(d4.w), sample = __float_as_int(b4.w);
+        if (live) {
+            const int fi = filmIndexS(p, pix);
+            const int depth = meta & 255;
+            const bool spec = (meta & 256) != 0;
+            if (depth < p.maxDepth && (p.guidedBounces <= 0 || depth < p.guidedBounces)) {
+                const int2 sh = __ldg(&p.sv.slotShade[__float_as_int(h4.y)]);
+                Mixture M;
+                mixtureFromRaw(raw, M);
+                float3 fc;
+                float pdf;
+                shadeGuidedLambert(p.sv, ps, nn, p.sv.mats[sh.x], sh.y, xyz(d4), xyz(b4), spec, depth, M,
+                                   p.guideAlpha, p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), R,
+                                   &fc, &pdf);
+            } else {
+                shadeHit(p.sv, hitOfRow(h4), xyz(o4), xyz(d4), xyz(b4), spec, depth, p.maxDepth, p.seed,
+                         static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), fi, R, false);
+            }
+        }
+        emitShadeResultS(p, R, live, pix, meta, sample);
+    }
+    tileKernelTeardown(sm, tmem, ok, phase);
+    if (!ok && threadIdx.x == 0) atomicOr(&p.ctr[kCtrErr], 2);
 }
 
 template <bool STATS>
@@ -288,10 +380,10 @@ __global__ void k_sadvance(StreamArgs p) {
 enum KernelClassS { kSRegen = 0, kSExtend, kSShadeL, kSShadeC, kSShadeD, kSShadow, kSAdvance, kSNumClasses };
 
 struct GridsS {
-    int trace, shade, regen;
+    int trace, shade, regen, guided;
 };
 
-GridsS streamGrids(int device, int cap) {
+GridsS streamGrids(int device, int cap, bool guided) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int occT = 0, occS = 0;
@@ -301,6 +393,7 @@ GridsS streamGrids(int device, int cap) {
     g.trace = sms * std::max(occT, 1);
     g.shade = sms * std::max(occS, 1);
     g.regen = std::max(1, std::min((cap + 255) / 256, sms * 8));
+    g.guided = guided ? guideTileKernelGrid(reinterpret_cast<const void *>(k_sshade_guided), device) : 0;
     return g;
 }
 
@@ -324,7 +417,8 @@ void launchIteration(const StreamArgs &a, const GridsS &g, cudaStream_t s, cudaE
     k_sextend<STATS><<<g.trace, kTraceBlock, 0, s>>>(a);
     done();
     mark(kSShadeL);
-    k_sshade<kMatLambert><<<g.shade, kShadeBlockS, 0, s>>>(a);
+    if (a.packFwd) k_sshade_guided<<<g.guided, kGTile, kTileSmem, s>>>(a);
+    else k_sshade<kMatLambert><<<g.shade, kShadeBlockS, 0, s>>>(a);
     done();
     mark(kSShadeC);
     k_sshade<kMatConductor><<<g.shade, kShadeBlockS, 0, s>>>(a);
@@ -385,7 +479,7 @@ StreamInit streamInit(long long total, int sampleOffset, float4 *film) {
 }
 
 int setupStream(Ctx &C, StreamQueues &q, const float *camera, int W, int H, int spp, int maxDepth, uint32_t seed,
-                int integrator, StreamArgs *out) {
+                int integrator, const GuideView *gv, StreamArgs *out) {
     const long long npix = static_cast<long long>(W) * H;
     const long long total = npix * spp;
     const int cap = static_cast<int>(std::min<long long>(std::max<long long>(total, 1), Ctx::kStreamSlots));
@@ -413,6 +507,16 @@ int setupStream(Ctx &C, StreamQueues &q, const float *camera, int W, int H, int 
     a.shL = q.shL;
     a.ctr = q.ctr;
     a.big = q.big;
+    if (gv) {
+        a.packFwd = gv->packFwd;
+        a.biasPad = gv->biasPad;
+        a.guideAlpha = gv->alpha;
+        a.guidedBounces = gv->guidedBounces;
+        a.guideLo = C.bvh.lo;
+        const float3 ext = C.bvh.hi - C.bvh.lo;
+        a.guideInvExt = mk(ext.x > 0 ? 1.0f / ext.x : 0.0f, ext.y > 0 ? 1.0f / ext.y : 0.0f,
+                           ext.z > 0 ? 1.0f / ext.z : 0.0f);
+    }
     return 0;
 }
 
@@ -422,7 +526,7 @@ int ensureStreamGraph(Ctx &C, StreamQueues &q, const StreamArgs &a, cudaStream_t
     if (q.graph && q.graphKey == key) return 0;
     if (q.graph) cudaGraphExecDestroy(q.graph);
     q.graph = nullptr;
-    const GridsS g = streamGrids(C.device, a.cap);
+    const GridsS g = streamGrids(C.device, a.cap, a.packFwd != nullptr);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cudaFail("cudaStreamBeginCapture", e);
@@ -465,7 +569,8 @@ void freeStreamQueues(StreamQueues *q) {
 }
 
 int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth, uint32_t seed,
-                 int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream) {
+                 int integrator, float4 *film, unsigned long long *statsOut, float *msOut, cudaStream_t stream,
+                 const GuideView *gv) {
     Ctx &C = *ctx;
     for (int j = 0; j < 4; j++) statsOut[j] = 0;
     *msOut = 0.0f;
@@ -481,7 +586,7 @@ int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampl
     int first = sampleOffset;
     for (int k = 0; k < lanes; k++) {
         const int sppK = spp / lanes + (k < spp % lanes ? 1 : 0);
-        if (int rc = setupStream(C, C.sq[k], camera, W, H, sppK, maxDepth, seed, integrator, &a[k])) return rc;
+        if (int rc = setupStream(C, C.sq[k], camera, W, H, sppK, maxDepth, seed, integrator, gv, &a[k])) return rc;
         // captured on the context's own stream (the caller's may be the legacy default
         // stream, which cannot be captured), replayed on the lane's
         if (int rc = ensureStreamGraph(C, C.sq[k], a[k], C.stream)) return rc;
@@ -562,7 +667,8 @@ int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampl
     }
     *msOut = ms;
     if (err) {
-        setError("spgpu_render: traversal stack overflow");
+        setError(err & 1 ? "spgpu_render: traversal stack overflow"
+                         : "spgpu_render: tensor-core wait of the guided shading timed out");
         return SPGPU_EKERNEL;
     }
     if (!drained) {
@@ -574,7 +680,8 @@ int renderStream(Ctx *ctx, const float *camera, int W, int H, int spp, int sampl
 
 int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, int sampleOffset, int maxDepth,
                         uint32_t seed, int integrator, float4 *film, double *kernelMs, long long *launches,
-                        unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream) {
+                        unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream,
+                        const GuideView *gv) {
     Ctx &C = *ctx;
     for (int k = 0; k < kSNumClasses; k++) {
         kernelMs[k] = 0.0;
@@ -584,8 +691,8 @@ int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, in
     if (spp <= 0 || W <= 0 || H <= 0) return 0;
     StreamArgs a;
     StreamQueues &q = C.sq[0];
-    if (int rc = setupStream(C, q, camera, W, H, spp, maxDepth, seed, integrator, &a)) return rc;
-    const GridsS g = streamGrids(C.device, a.cap);
+    if (int rc = setupStream(C, q, camera, W, H, spp, maxDepth, seed, integrator, gv, &a)) return rc;
+    const GridsS g = streamGrids(C.device, a.cap, a.packFwd != nullptr);
     const long long total = static_cast<long long>(W) * H * spp;
     const StreamInit init = streamInit(total, sampleOffset, film);
     const long long bound = iterationBound(a, total);
@@ -624,7 +731,8 @@ int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, in
     for (auto &x : ev) cudaEventDestroy(x);
     if (e != cudaSuccess) return cudaFail("spgpu_render_profile", e);
     if (ctr[kCtrErr]) {
-        setError("spgpu_render_profile: traversal stack overflow");
+        setError(ctr[kCtrErr] & 1 ? "spgpu_render_profile: traversal stack overflow"
+                                  : "spgpu_render_profile: tensor-core wait of the guided shading timed out");
         return SPGPU_EKERNEL;
     }
     return 0;

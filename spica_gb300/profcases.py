@@ -4,7 +4,7 @@ case), separate from the benchmark:
     python -m spica_gb300.profcases render [--width W] [--height H] [--spp N] [--warmup K]
     python -m spica_gb300.profcases micro [--rays N]
     python -m spica_gb300.profcases batch [--renders N]
-    python -m spica_gb300.profcases guided
+    python -m spica_gb300.profcases guided [--wavefront 0|1]
     python -m spica_gb300.profcases build [--levels L]
     python -m spica_gb300.profcases film [--width W] [--height H]
 
@@ -17,8 +17,9 @@ micro   the intersection microbench's sphere (1,048,576 triangles) and N of its 
 batch   the first N seeded box-room variants in one persistent batch launch (k_batch)
 guided  the guiding room at 640 x 360: 8 collection passes of 2 spp with 32 Adam steps
         each (k_collect, k_gather, k_guide_train, k_adam), then one plain and one guided
-        render of 8 spp inside the NVTX range "profiled" (k_shade_guided), then one
-        network evaluation of 65,536 inputs (k_guide_forward)
+        render of 8 spp inside the NVTX range "profiled" (k_sshade_guided on the streaming
+        wavefront; k_shade_guided with --wavefront 1, pass by pass), then one network
+        evaluation of 65,536 inputs (k_guide_forward)
 build   the device BVH build of the mid-scale scene, or of the microbench sphere with
         --levels (Morton keys, clustering rounds, SAH programme, collapse)
 film    a rendered box room at W x H resolved by every film format (RGBE, gamma,
@@ -84,11 +85,11 @@ def _batch(args, torch):
 def _guided(args, torch):
     import numpy as np
 
-    from . import GpuBVHAccel, scenes
+    from . import Context, GpuBVHAccel, scenes
     from .gpu import GUIDE_COLLECT, GUIDE_GUIDED, GpuGuide
     W, H = 640, 360
     sc = scenes.guiding_room(width=W, height=H)
-    acc = GpuBVHAccel(sc).construct()
+    acc = GpuBVHAccel(sc, ctx=Context(0, wavefront=args.wavefront)).construct()
     g = GpuGuide(acc, seed=2)
     p = {"width": W, "height": H, "maxDepth": sc.max_depth}
     f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
@@ -104,7 +105,8 @@ def _guided(args, torch):
     raw = torch.zeros((65536, 40), dtype=torch.float32, device="cuda")
     g.mlp(feats, raw)
     torch.cuda.synchronize()
-    return {"case": "guided", "width": W, "height": H, "spp": 8, "plain_ms": sp.ms, "guided_ms": sg.ms}
+    return {"case": "guided", "width": W, "height": H, "spp": 8, "wavefront": args.wavefront, "plain_ms": sp.ms,
+            "guided_ms": sg.ms}
 
 
 def _build(args, torch):
@@ -143,6 +145,7 @@ def main(argv=None):
     ap.add_argument("--rays", type=int, default=1 << 21)
     ap.add_argument("--renders", type=int, default=4)
     ap.add_argument("--levels", type=int, default=0)
+    ap.add_argument("--wavefront", type=int, default=0, choices=[0, 1])
     args = ap.parse_args(argv)
     import torch
     torch.cuda.set_device(0)

@@ -259,6 +259,39 @@ def test_guided_wavefront_matches_guided_megakernel(gpulib):
     np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=2e-3, atol=2e-3)
 
 
+def test_streaming_guided_matches_pass_by_pass(gpulib):
+    """Guided passes on the streaming wavefront (the default: one guided shading launch
+    per iteration over a Lambert queue that mixes depths) and on the pass-by-pass
+    wavefront (one guided launch per bounce) draw the same numbers for every (pixel,
+    sample, depth) and give the network the same inputs, so with the same weights the
+    films agree up to the order of the film's atomic additions; likewise plain passes."""
+    import torch
+    from spica_gb300 import Context
+    sc = _room(40)
+    W, H = 96, 56
+    p = {"width": W, "height": H, "maxDepth": sc.max_depth}
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=5)
+    scratch = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    for k in range(6):
+        g.render(sc.camera, dict(p, sampleCount=4), scratch, GUIDE_GUIDED | GUIDE_COLLECT, seed=70, sample_offset=4 * k)
+        g.train(16)
+    acc1 = GpuBVHAccel(sc, ctx=Context(0, wavefront=1)).construct()
+    g1 = GpuGuide(acc1, seed=5)
+    g1.set_params(g.params())
+    for flags in (GUIDE_GUIDED, 0):
+        films = []
+        for guide in (g, g1):
+            f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+            st = guide.render(sc.camera, dict(p, sampleCount=24), f, flags, seed=8, sample_offset=3)
+            assert st.paths == W * H * 24 and st.kernel_launches > 0
+            films.append(f.cpu().numpy())
+        a, b = films
+        assert np.array_equal(a[..., 3], b[..., 3])
+        assert a[..., :3].sum() > 0
+        np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=2e-3, atol=2e-3)
+
+
 def test_wavefront_collection_matches_megakernel(gpulib):
     """Training records collected in the wavefront (per-path records closed when their
     continuation ray finds its hit, turned into ring entries at the end of the pass)
