@@ -315,7 +315,8 @@ def microbench(torch, GpuBVHAccel, scenes, reps=3, rays=16 << 20, cpu=False):
 
 def batch_bench(torch, GpuBatch, scenes, reps=3, count=64, autotune=True):
     """64 seeded box-room variants (resolution 64..512 squared, 16..256 spp) in one
-    persistent graph-captured launch; launch shape from the autotuner."""
+    graph launch; the engine (streaming wavefront or persistent megakernel) and its
+    launch shape from the autotuner."""
     vs = scenes.batch_variants(count, seed=0)
     t0 = time.perf_counter()
     b = GpuBatch(vs, seed=7, autotune=autotune)
@@ -334,7 +335,10 @@ def batch_bench(torch, GpuBatch, scenes, reps=3, count=64, autotune=True):
     return {"renders": len(vs), "path_samples": int(samples), "ms": st.ms,
             "samples_per_s": samples / (st.ms / 1e3), "mrays_s": (st.rays_closest + st.rays_shadow) / (st.ms * 1e3),
             "latency_ms_p50": float(np.percentile(ms, 50)), "latency_ms_p99": float(np.percentile(ms, 99)),
-            "tuning": {"block": b.tuning.block, "tile_pixels": b.tuning.tile_pixels, "chunk_spp": b.tuning.chunk_spp,
+            "tuning": {"engine": {1: "streaming wavefront", 2: "persistent megakernel"}.get(b.tuning.engine),
+                       "pool_slots": b.tuning.pool_slots, "pool_lanes": b.tuning.pool_lanes,
+                       "iterations": b.tuning.iterations, "block": b.tuning.block,
+                       "tile_pixels": b.tuning.tile_pixels, "chunk_spp": b.tuning.chunk_spp,
                        "candidates": b.tuning.candidates, "calib_ms": b.tuning.calib_ms},
             "prepare_s": prep_s}
 

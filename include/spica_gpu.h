@@ -224,14 +224,28 @@ int spgpu_render_host(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film
 /* ---- batched renders ---------------------------------------------------------------
  * replaces: a sequence of Integrator::render calls on many small scenes
  * (core/integrator.cc:46), one per scene.  A batch is prepared once (scenes uploaded,
- * one BVH each, work list planned, launch shape chosen by the autotuner when
- * `autotune` != 0) and then traced by spgpu_batch_run in a single persistent kernel
- * launch replayed from a CUDA graph.  Preparing a batch replaces the context's scene
- * (the last item's scene remains uploaded).  Scenes of a batch have no environment
- * map.  films: device memory of spgpu_batch_film_pixels() float4 pixels, the items'
- * films back to back in item order, each in the reference film's pixel order;
- * accumulated in place.  render_ms[i]: time from the launch's start until the last
- * sample of item i was added. */
+ * one BVH each, merged) and then traced by spgpu_batch_run as ONE launch of a CUDA
+ * graph, by one of two engines:
+ *   SPGPU_BATCH_STREAM      the streaming wavefront over all renders of the batch: pools
+ *                           of path slots refilled from one path sequence (render after
+ *                           render), whose iteration loop runs on the device inside the
+ *                           graph (a conditional while node);
+ *   SPGPU_BATCH_PERSISTENT  one persistent megakernel pulling (render, pixel tile,
+ *                           sample chunk) work items, each thread tracing whole paths.
+ * autotune: 0 takes the streaming wavefront with its default pool (or, when `tuning` is
+ * given with pool_slots > 0 on input, with pool_slots slots in each of pool_lanes
+ * pools); 1 times every
+ * candidate of both engines (pool slots and lanes; block, tile and chunk) on a copy of
+ * the batch with 1/16 of the samples and keeps the fastest; SPGPU_BATCH_PERSISTENT takes
+ * the megakernel with its default shape.  Preparing a batch replaces the context's
+ * scene (the last item's scene remains uploaded).  Scenes of a batch have no
+ * environment map.  films: device memory of spgpu_batch_film_pixels() float4 pixels
+ * (fewer than 2^31), the items' films back to back in item order, each in the
+ * reference film's pixel order; accumulated in place.  render_ms[i]: time from the
+ * launch's start until the last path of item i ended (streaming) or its last sample
+ * was added (persistent). */
+#define SPGPU_BATCH_STREAM 1
+#define SPGPU_BATCH_PERSISTENT 2
 typedef struct {
     int32_t ntri;
     const float *verts;
@@ -243,11 +257,15 @@ typedef struct {
 } spgpu_batch_item;
 
 typedef struct {
-    int32_t block;          /* threads per block */
-    int32_t tile_pixels;    /* pixels per work item */
-    int32_t chunk_spp;      /* samples per pixel per work item */
+    int32_t block;          /* persistent: threads per block */
+    int32_t tile_pixels;    /* persistent: pixels per work item */
+    int32_t chunk_spp;      /* persistent: samples per pixel per work item */
     int32_t candidates;     /* configurations the autotuner timed */
     double calib_ms;        /* device time spent timing them */
+    int32_t engine;         /* SPGPU_BATCH_STREAM or SPGPU_BATCH_PERSISTENT */
+    int32_t pool_slots;     /* streaming: path slots per pool */
+    int32_t pool_lanes;     /* streaming: pools in flight, each on its own share of the paths */
+    int32_t iterations;     /* streaming: wavefront iterations per round of the device loop */
 } spgpu_batch_tuning;
 
 int spgpu_batch_prepare(spgpu_ctx *ctx, int32_t count, const spgpu_batch_item *items, int32_t autotune,

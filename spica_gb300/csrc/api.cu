@@ -962,7 +962,7 @@ int spgpu_batch_prepare(spgpu_ctx *h, int32_t count, const spgpu_batch_item *ite
                         spgpu_batch_tuning *tuning) {
     return guarded("spgpu_batch_prepare", [&]() -> int {
         NvtxRange nvtxRange("spgpu_batch_prepare");
-        if (!h || count <= 0 || !items) {
+        if (!h || count <= 0 || !items || autotune < 0 || autotune > SPGPU_BATCH_PERSISTENT) {
             setError("spgpu_batch_prepare: invalid arguments");
             return SPGPU_EINVAL;
         }
@@ -974,33 +974,35 @@ int spgpu_batch_prepare(spgpu_ctx *h, int32_t count, const spgpu_batch_item *ite
 int64_t spgpu_batch_film_pixels(spgpu_ctx *h) { return h && h->c.batch ? batchPixels(*h->c.batch) : -1; }
 
 int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_stats *stats, void *stream) {
-    NvtxRange nvtxRange("spgpu_batch_run");
-    if (!h || !films || !render_ms) {
-        setError("spgpu_batch_run: invalid arguments");
-        return SPGPU_EINVAL;
-    }
-    Ctx &C = h->c;
-    if (!C.batch) {
-        setError("spgpu_batch_run: no batch prepared");
-        return SPGPU_ESTATE;
-    }
-    if (reinterpret_cast<uintptr_t>(films) & 15) {
-        setError("spgpu_batch_run: films must be 16-byte aligned");
-        return SPGPU_EINVAL;
-    }
-    cudaSetDevice(C.device);
-    unsigned long long st[4] = {0, 0, 0, 0};
-    float ms = 0.0f;
-    const int rc = batchRun(C, *C.batch, reinterpret_cast<float4 *>(films), render_ms, st, &ms,
-                            static_cast<cudaStream_t>(stream));
-    if (stats) {
-        stats->paths = static_cast<int64_t>(st[0]);
-        stats->rays_closest = static_cast<int64_t>(st[1]);
-        stats->rays_shadow = static_cast<int64_t>(st[2]);
-        stats->ms = ms;
-        stats->kernel_launches = 0;
-    }
-    return rc;
+    return guarded("spgpu_batch_run", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_batch_run");
+        if (!h || !films || !render_ms) {
+            setError("spgpu_batch_run: invalid arguments");
+            return SPGPU_EINVAL;
+        }
+        Ctx &C = h->c;
+        if (!C.batch) {
+            setError("spgpu_batch_run: no batch prepared");
+            return SPGPU_ESTATE;
+        }
+        if (reinterpret_cast<uintptr_t>(films) & 15) {
+            setError("spgpu_batch_run: films must be 16-byte aligned");
+            return SPGPU_EINVAL;
+        }
+        cudaSetDevice(C.device);
+        unsigned long long st[4] = {0, 0, 0, 0};
+        float ms = 0.0f;
+        const int rc = batchRun(C, *C.batch, reinterpret_cast<float4 *>(films), render_ms, st, &ms,
+                                static_cast<cudaStream_t>(stream));
+        if (stats) {
+            stats->paths = static_cast<int64_t>(st[0]);
+            stats->rays_closest = static_cast<int64_t>(st[1]);
+            stats->rays_shadow = static_cast<int64_t>(st[2]);
+            stats->ms = ms;
+            stats->kernel_launches = static_cast<int64_t>(st[3]);
+        }
+        return rc;
+    });
 }
 
 int spgpu_guiding_init(spgpu_ctx *h, const spgpu_guiding_config *cfg) {

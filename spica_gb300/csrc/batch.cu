@@ -22,15 +22,6 @@
 
 namespace spgpu {
 
-struct RenderMeta {
-    CameraView cam;
-    int W, H, spp, maxDepth;
-    uint32_t seed;
-    uint32_t root;
-    int lightBase, nArea;
-    int64_t filmOffset;   // in pixels
-};
-
 struct BatchItem {
     int render;
     int pix0, npix;   // raster pixels [pix0, pix0 + npix)
@@ -58,6 +49,11 @@ struct BatchState {
     int block = 128, tile = 128, chunk = 4;
     cudaGraphExec_t graph = nullptr;
     float *graphFilm = nullptr;
+    // engine: SPGPU_BATCH_STREAM (the streaming wavefront over all renders, stream.cu) or
+    // SPGPU_BATCH_PERSISTENT (the megakernel below)
+    int engine = SPGPU_BATCH_STREAM;
+    StreamBatch *sb = nullptr;
+    int poolSlots = 0, poolLanes = 0, iterations = 0;
 };
 
 namespace {
@@ -239,6 +235,7 @@ int resetBatch(BatchState &B, const std::vector<int> &perRender, cudaStream_t s,
 
 void freeBatch(BatchState *B) {
     if (!B) return;
+    freeStreamBatch(B->sb);
     if (B->graph) cudaGraphExecDestroy(B->graph);
     cudaFree(B->nodes);
     cudaFree(B->tris);
@@ -322,6 +319,10 @@ int batchPrepare(spgpu_ctx *self, BatchState **slot, int count, const spgpu_batc
         B->totalSamples += static_cast<int64_t>(d.width) * d.height * d.spp;
         B->hostMeta.push_back(M);
     }
+    if (rc == 0 && B->totalPixels > INT32_MAX) {
+        setError("spgpu_batch_prepare: the batch's films exceed 2^31 pixels");
+        rc = SPGPU_EINVAL;
+    }
     if (rc == 0) {
         B->nNodes = static_cast<int>(nodes.size());
         B->nTris = static_cast<int>(tris.size());
@@ -334,22 +335,44 @@ int batchPrepare(spgpu_ctx *self, BatchState **slot, int count, const spgpu_batc
             if (e != cudaSuccess) rc = cudaFail("spgpu_batch_prepare", e);
         }
     }
-    // autotune (block, tile, chunk) on a reduced-spp copy of the batch
+    // The launch: by default the streaming wavefront with its default pool; with
+    // autotune, every candidate of both engines -- pool slots and lanes of the streaming
+    // wavefront, (block, tile, chunk) of the persistent megakernel -- is timed on a copy of
+    // the batch with 1/16 of the samples, and the fastest is kept
     if (rc == 0) {
         struct Cand {
-            int block, tile, chunk;
+            int engine, block, tile, chunk, slots, lanes;
         };
+        constexpr int kIters = 8;   // wavefront iterations per round of the device loop
         std::vector<Cand> cands;
-        if (autotune) {
+        if (autotune == SPGPU_BATCH_PERSISTENT) {
+            cands.push_back({SPGPU_BATCH_PERSISTENT, 128, 128, 4, 0, 0});
+        } else if (autotune) {
+            for (int sl : {1 << 20, 1 << 21, 1 << 22})
+                for (int ln : {1, 2}) cands.push_back({SPGPU_BATCH_STREAM, 0, 0, 0, sl, ln});
             for (int bl : {64, 128, 256})
                 for (int ti : {64, 256})
-                    for (int ch : {1, 4, 16}) cands.push_back({bl, ti, ch});
+                    for (int ch : {1, 4, 16}) cands.push_back({SPGPU_BATCH_PERSISTENT, bl, ti, ch, 0, 0});
+        } else if (tuning && tuning->pool_slots > 0) {
+            cands.push_back({SPGPU_BATCH_STREAM, 0, 0, 0, tuning->pool_slots, tuning->pool_lanes});   // the caller's pool
         } else {
-            cands.push_back({128, 128, 4});
+            cands.push_back({SPGPU_BATCH_STREAM, 0, 0, 0, 1 << 22, 2});
         }
+        SceneView merged{};
+        merged.nodes = B->nodes;
+        merged.tris = B->tris;
+        merged.slotShade = B->slotShade;
+        merged.nNodes = static_cast<uint32_t>(B->nNodes);
+        merged.nTris = static_cast<uint32_t>(B->nTris);
+        merged.mats = B->mats;
+        merged.lights = B->lights;
+        std::vector<RenderMeta> reduced = B->hostMeta;
+        for (auto &M : reduced) M.spp = std::max(1, M.spp / 16);
         float4 *scratchFilm = nullptr;
-        cudaError_t e = cudaMalloc(&scratchFilm, sizeof(float4) * std::max<int64_t>(B->totalPixels, 1));
-        if (e != cudaSuccess) rc = cudaFail("spgpu_batch_prepare", e);
+        if (cands.size() > 1) {
+            cudaError_t e = cudaMalloc(&scratchFilm, sizeof(float4) * std::max<int64_t>(B->totalPixels, 1));
+            if (e != cudaSuccess) rc = cudaFail("spgpu_batch_prepare", e);
+        }
         BatchItem *dItems = nullptr;
         float best = 3.0e38f;
         Cand bestC = cands[0];
@@ -358,44 +381,72 @@ int batchPrepare(spgpu_ctx *self, BatchState **slot, int count, const spgpu_batc
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         for (size_t ci = 0; ci < cands.size() && rc == 0 && cands.size() > 1; ci++) {
-            std::vector<BatchItem> its;
-            std::vector<int> per;
-            buildItems(*B, cands[ci].tile, cands[ci].chunk, 16, &its, &per);
-            cudaFree(dItems);
-            dItems = nullptr;
-            if ((rc = devUpload(&dItems, its))) break;
+            const Cand &c = cands[ci];
             float msBest = 3.0e38f;
-            for (int rep = 0; rep < 2 && rc == 0; rep++) {
-                if ((rc = resetBatch(*B, per, C.stream, rep == 0))) break;
-                cudaEventRecord(e0, C.stream);
-                rc = launchBatch(C, *B, dItems, static_cast<int>(its.size()), scratchFilm, C.stream, cands[ci].block);
-                cudaEventRecord(e1, C.stream);
-                cudaEventSynchronize(e1);
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                msBest = std::min(msBest, ms);
-                calibMs += ms;
+            if (c.engine == SPGPU_BATCH_STREAM) {
+                StreamBatch *tb = nullptr;
+                rc = streamBatchCreate(C, &tb, merged, reduced, c.slots, c.lanes, kIters);
+                std::vector<double> rms(reduced.size());
+                unsigned long long st[4];
+                for (int rep = 0; rep < 2 && rc == 0; rep++) {
+                    float ms = 0.0f;
+                    rc = streamBatchRun(C, *tb, scratchFilm, rms.data(), st, &ms, C.stream);
+                    msBest = std::min(msBest, ms);
+                    calibMs += ms;
+                }
+                freeStreamBatch(tb);
+            } else {
+                std::vector<BatchItem> its;
+                std::vector<int> per;
+                buildItems(*B, c.tile, c.chunk, 16, &its, &per);
+                cudaFree(dItems);
+                dItems = nullptr;
+                if ((rc = devUpload(&dItems, its))) break;
+                for (int rep = 0; rep < 2 && rc == 0; rep++) {
+                    if ((rc = resetBatch(*B, per, C.stream, rep == 0))) break;
+                    cudaEventRecord(e0, C.stream);
+                    rc = launchBatch(C, *B, dItems, static_cast<int>(its.size()), scratchFilm, C.stream, c.block);
+                    cudaEventRecord(e1, C.stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    msBest = std::min(msBest, ms);
+                    calibMs += ms;
+                }
             }
             if (msBest < best) {
                 best = msBest;
-                bestC = cands[ci];
+                bestC = c;
             }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         cudaFree(dItems);
         cudaFree(scratchFilm);
-        B->block = bestC.block;
-        B->tile = bestC.tile;
-        B->chunk = bestC.chunk;
+        B->engine = bestC.engine;
+        if (bestC.engine == SPGPU_BATCH_PERSISTENT) {
+            B->block = bestC.block;
+            B->tile = bestC.tile;
+            B->chunk = bestC.chunk;
+        } else {
+            B->poolSlots = bestC.slots;
+            B->poolLanes = bestC.lanes;
+            B->iterations = kIters;
+        }
         if (tuning) {
-            tuning->block = bestC.block;
-            tuning->tile_pixels = bestC.tile;
-            tuning->chunk_spp = bestC.chunk;
+            tuning->engine = bestC.engine;
+            tuning->block = bestC.engine == SPGPU_BATCH_PERSISTENT ? bestC.block : 0;
+            tuning->tile_pixels = bestC.engine == SPGPU_BATCH_PERSISTENT ? bestC.tile : 0;
+            tuning->chunk_spp = bestC.engine == SPGPU_BATCH_PERSISTENT ? bestC.chunk : 0;
+            tuning->pool_slots = bestC.slots;
+            tuning->pool_lanes = bestC.lanes;
+            tuning->iterations = bestC.engine == SPGPU_BATCH_STREAM ? kIters : 0;
             tuning->candidates = static_cast<int32_t>(cands.size());
             tuning->calib_ms = calibMs;
         }
-        if (rc == 0) {
+        if (rc == 0 && B->engine == SPGPU_BATCH_STREAM) {
+            rc = streamBatchCreate(C, &B->sb, merged, B->hostMeta, B->poolSlots, B->poolLanes, B->iterations);
+        } else if (rc == 0) {
             std::vector<BatchItem> its;
             std::vector<int> per;
             buildItems(*B, B->tile, B->chunk, 1, &its, &per);
@@ -415,6 +466,7 @@ int64_t batchPixels(const BatchState &B) { return B.totalPixels; }
 
 int batchRun(Ctx &C, BatchState &B, float4 *film, double *renderMs, unsigned long long *statsOut, float *msOut,
              cudaStream_t stream) {
+    if (B.engine == SPGPU_BATCH_STREAM) return streamBatchRun(C, *B.sb, film, renderMs, statsOut, msOut, stream);
     std::vector<BatchItem> its;
     std::vector<int> per;
     buildItems(B, B.tile, B.chunk, 1, &its, &per);
@@ -460,6 +512,7 @@ int batchRun(Ctx &C, BatchState &B, float4 *film, double *renderMs, unsigned lon
     for (int r = 0; r < B.count; r++)
         renderMs[r] = times[1 + r] >= times[0] ? (times[1 + r] - times[0]) * 1.0e-6 : -1.0;
     for (int k = 0; k < 3; k++) statsOut[k] = st[k];
+    statsOut[3] = 2;   // counter reset and the persistent kernel
     *msOut = ms;
     if (ctl[1]) {
         setError("spgpu_batch_run: traversal stack overflow");

@@ -2,6 +2,8 @@
 // traversal routine shared by the ray-batch kernels and the wavefront renderer.
 #pragma once
 
+#include <type_traits>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -281,8 +283,12 @@ __device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nod
                 if (r < n) {
                     float3 o, d;
                     float t0, t1;
-                    fetch(r, &o, &d, &t0, &t1);
-                    laneInit(L, o, d, t0, t1);
+                    uint32_t root = 0;   // a fetch that takes a sixth argument names the ray's tree root
+                    if constexpr (std::is_invocable_v<Fetch &, int, float3 *, float3 *, float *, float *, uint32_t *>)
+                        fetch(r, &o, &d, &t0, &t1, &root);
+                    else
+                        fetch(r, &o, &d, &t0, &t1);
+                    laneInit(L, o, d, t0, t1, root);
                     ray = r;
                 } else {
                     ray = -2;

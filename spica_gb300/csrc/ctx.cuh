@@ -223,6 +223,28 @@ struct CameraView {
 };
 CameraView makeCamera(const float *camera, int width, int height);
 
+// One render of a batch: its camera, film, samples, and where its scene sits in the
+// batch's merged tree, light and film arrays
+struct RenderMeta {
+    CameraView cam;
+    int W, H, spp, maxDepth;
+    uint32_t seed;
+    uint32_t root;        // its tree's root node in the merged node array
+    int lightBase, nArea;
+    int64_t filmOffset;   // in pixels
+};
+
+// stream.cu: a batch on the streaming wavefront -- one path sequence over all renders
+// (render after render, sample after sample), traced by pools of path slots whose
+// iteration loop runs on the device (a CUDA graph with a conditional while node), so a
+// run is one graph launch
+struct StreamBatch;
+int streamBatchCreate(Ctx &C, StreamBatch **slot, const SceneView &merged, const std::vector<RenderMeta> &renders,
+                      int poolSlots, int lanes, int iterations);
+int streamBatchRun(Ctx &C, StreamBatch &SB, float4 *film, double *renderMs, unsigned long long *statsOut,
+                   float *msOut, cudaStream_t stream);
+void freeStreamBatch(StreamBatch *SB);
+
 // learned-guiding state that a guided wavefront pass reads (guide.cu fills it)
 struct GuideView {
     const uint8_t *packFwd;   // packed bf16 forward weights

@@ -72,12 +72,18 @@ constexpr int kNumCtr = 16;
 // 64-bit counters: [0] paths started, [1] paths, [2] closest rays, [3] shadow rays,
 // [4..7] visits (extend nodes, triangles, shadow nodes, triangles); then the call's own
 // parameters, written by the host per render so that one captured graph serves every
-// call: [8] paths of the render (spp * npix), [9] sample offset, [10] film address
-enum : int { kBigStarted = 0, kBigPaths, kBigClosest, kBigShadow, kBigVisit, kBigTotal = 8, kBigOffset, kBigFilm };
+// call: [8] paths of the render (spp * npix), [9] sample offset (batches: the lane's
+// first path of the batch's sequence), [10] film address; [11] iterations run (batches)
+enum : int { kBigStarted = 0, kBigPaths, kBigClosest, kBigShadow, kBigVisit, kBigTotal = 8, kBigOffset, kBigFilm,
+             kBigRounds };
 constexpr int kNumBig = 12;
 
-// a path's depth (bits 0..7) and specular flag (bit 8), carried in the w of its direction
-__device__ __forceinline__ float packMeta(int depth, bool spec) { return __int_as_float(depth | (spec ? 256 : 0)); }
+// a path's depth (bits 0..7), specular flag (bit 8) and, in batches, its render (bits
+// 9..), carried in the w of its direction
+__device__ __forceinline__ float packMeta(int depth, bool spec, int render = 0) {
+    return __int_as_float(depth | (spec ? 256 : 0) | (render << 9));
+}
+__device__ __forceinline__ int metaRender(int meta) { return static_cast<int>(static_cast<unsigned>(meta) >> 9); }
 
 struct StreamArgs {
     SceneView sv;
@@ -102,6 +108,17 @@ struct StreamArgs {
     float guideAlpha;
     int guidedBounces;
     float3 guideLo, guideInvExt;
+    // batches: the renders, the first path of each in the batch's path sequence
+    // (nRenders + 1 entries), paths ended per render, the start and completion times
+    // (globaltimer ns: [0] start, [1 + r] render r), the device loop's condition and its
+    // iteration limit
+    const RenderMeta *renders;
+    const long long *pathStart;
+    int nRenders;
+    unsigned long long *ended;
+    unsigned long long *times;
+    cudaGraphConditionalHandle cond;
+    long long iterLimit;
 };
 
 __device__ __forceinline__ int filmIndexS(const StreamArgs &p, int pix) {
@@ -131,42 +148,82 @@ __device__ __forceinline__ int warpAppendS(bool want, int *counter) {
     return want ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
+// batches: the render of path g of the batch's sequence (binary search of pathStart)
+__device__ __forceinline__ int renderOfPath(const StreamArgs &p, long long g) {
+    int lo = 0, hi = p.nRenders;   // pathStart[lo] <= g < pathStart[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&p.pathStart[mid]) <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// batches: add the warp's ended paths to their renders' counts (whole warps call this)
+__device__ __forceinline__ void countEnded(const StreamArgs &p, bool ended, int render) {
+    const unsigned mask = __ballot_sync(__activemask(), ended);
+    if (!ended) return;
+    const unsigned same = __match_any_sync(mask, render);
+    if ((threadIdx.x & 31) == __ffs(same) - 1)
+        atomicAdd(&p.ended[render], static_cast<unsigned long long>(__popc(same)));
+}
+
+// film pixel of raster pixel pix in a film of width W (x mirrored, core/integrator.cc:88)
+__device__ __forceinline__ int mirrored(int pix, int W) {
+    const int y = pix / W, x = pix - y * W;
+    return y * W + (W - 1 - x);
+}
+
+template <bool BATCH>
 __global__ void k_sregen(StreamArgs p) {
     const int have = p.ctr[kCtrRays];
     const int nNew = newPaths(p);
     const long long started = static_cast<long long>(p.big[kBigStarted]);
-    const int sampleOffset = static_cast<int>(p.big[kBigOffset]);
+    // one render: the first sample of the call; batches: the lane's first path in the
+    // batch's sequence
+    const long long offset = static_cast<long long>(p.big[kBigOffset]);
     float4 *film = filmOf(p);
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nNew; j += gridDim.x * blockDim.x) {
         const long long g = started + j;
-        const int sample = sampleOffset + static_cast<int>(g / p.npix);
-        const int pix = static_cast<int>(g % p.npix);
-        const int y = pix / p.W, x = pix - y * p.W;
-        const int fi = y * p.W + (p.W - 1 - x);
-        const Rand4 r = rand4(p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), 0xFFFFu, 0u);
+        int render = 0, sample, pix, fi;
+        long long filmBase = 0;
         float3 o, d;
-        spawnCameraRay(p.cam, x, y, r.a, r.b, &o, &d);
+        if constexpr (BATCH) {
+            const long long gb = offset + g;
+            render = renderOfPath(p, gb);
+            const RenderMeta &M = p.renders[render];
+            const long long local = gb - __ldg(&p.pathStart[render]);
+            const int npix = M.W * M.H;
+            sample = static_cast<int>(local / npix);
+            pix = static_cast<int>(local % npix);
+            const int y = pix / M.W, x = pix - y * M.W;
+            fi = y * M.W + (M.W - 1 - x);
+            const Rand4 r = rand4(M.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), 0xFFFFu, 0u);
+            spawnCameraRay(M.cam, x, y, r.a, r.b, &o, &d);
+            filmBase = M.filmOffset;
+        } else {
+            sample = static_cast<int>(offset) + static_cast<int>(g / p.npix);
+            pix = static_cast<int>(g % p.npix);
+            const int y = pix / p.W, x = pix - y * p.W;
+            fi = y * p.W + (p.W - 1 - x);
+            const Rand4 r = rand4(p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), 0xFFFFu, 0u);
+            spawnCameraRay(p.cam, x, y, r.a, r.b, &o, &d);
+        }
         const int k = have + j;
         p.rO[k] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
-        p.rD[k] = make_float4(d.x, d.y, d.z, packMeta(0, false));
+        p.rD[k] = make_float4(d.x, d.y, d.z, packMeta(0, false, render));
         p.rB[k] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(sample));
-        atomicAdd(&film[fi].w, 1.0f);
+        atomicAdd(&film[filmBase + fi].w, 1.0f);
     }
 }
 
-template <bool STATS>
+template <bool STATS, bool BATCH>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(StreamArgs p) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     uint32_t nodeCount = 0, triCount = 0;
     const int n = p.ctr[kCtrRays] + newPaths(p);
     float4 *film = filmOf(p);
     bool overflow = false;
-    auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
-        *o = xyz(p.rO[i]);
-        *d = xyz(p.rD[i]);
-        *t0 = 0.0f;
-        *t1 = kInfT;
-    };
     auto done = [&](int i, const TraceLane &L) {
         if (!__any_sync(0xffffffffu, i >= 0)) return;
         int cls = -1;
@@ -177,7 +234,7 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
             b4 = p.rB[i];
             if (L.found) {
                 cls = shadeClass(__ldg(&p.sv.mats[__ldg(&p.sv.slotShade[L.hitSlot]).x].type));
-            } else if (p.sv.hasEnv) {
+            } else if (!BATCH && p.sv.hasEnv) {
                 // escaped: the environment at the first vertex or after a specular bounce
                 const int meta = __float_as_int(d4.w);
                 if ((meta & 255) == 0 || (meta & 256)) {
@@ -186,6 +243,7 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
                 }
             }
         }
+        if constexpr (BATCH) countEnded(p, i >= 0 && !L.found, metaRender(__float_as_int(d4.w)));   // no environment
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const int k = warpAppendS(cls == c, &p.ctr[kCtrClass0 + c]);
@@ -198,8 +256,30 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
             }
         }
     };
-    tracePersistent<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchE],
-                                  stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
+    if constexpr (BATCH) {
+        // each render's rays start at its own tree's root
+        auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1, uint32_t *root) {
+            const float4 d4 = p.rD[i];
+            *o = xyz(p.rO[i]);
+            *d = xyz(d4);
+            *t0 = 0.0f;
+            *t1 = kInfT;
+            *root = p.renders[metaRender(__float_as_int(d4.w))].root;
+        };
+        tracePersistent<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchE],
+                                      stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch,
+                                      done);
+    } else {
+        auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
+            *o = xyz(p.rO[i]);
+            *d = xyz(p.rD[i]);
+            *t0 = 0.0f;
+            *t1 = kInfT;
+        };
+        tracePersistent<false, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchE],
+                                      stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch,
+                                      done);
+    }
     if (overflow) atomicOr(&p.ctr[kCtrErr], 1);
     if (STATS) {
         atomicAdd(&p.big[kBigVisit + 0], static_cast<unsigned long long>(nodeCount));
@@ -207,16 +287,18 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sextend(Stream
     }
 }
 
-// a shaded hit's emission, continuation (back into the pool) and shadow rays; whole
-// warps call this
-__device__ __forceinline__ void emitShadeResultS(const StreamArgs &p, const ShadeResult &R, bool live, int pix,
-                                                 int meta, int sample) {
+// a shaded hit's emission (at film pixel filmIdx), continuation (back into the pool) and
+// shadow rays; whole warps call this.  Batches count the paths that end here.
+template <bool BATCH = false>
+__device__ __forceinline__ void emitShadeResultS(const StreamArgs &p, const ShadeResult &R, bool live, long long filmIdx,
+                                                 int pix, int meta, int sample) {
     if (live && !isBlack(R.emit))
-        atomicAdd(&filmOf(p)[filmIndexS(p, pix)], make_float4(R.emit.x, R.emit.y, R.emit.z, 0.0f));
+        atomicAdd(&filmOf(p)[filmIdx], make_float4(R.emit.x, R.emit.y, R.emit.z, 0.0f));
+    if constexpr (BATCH) countEnded(p, live && !R.cont, metaRender(meta));
     const int k = warpAppendS(R.cont && !p.direct, &p.ctr[kCtrCont]);
     if (k >= 0) {
         p.rO[k] = make_float4(R.cO.x, R.cO.y, R.cO.z, __int_as_float(pix));
-        p.rD[k] = make_float4(R.cD.x, R.cD.y, R.cD.z, packMeta((meta & 255) + 1, R.spec));
+        p.rD[k] = make_float4(R.cD.x, R.cD.y, R.cD.z, packMeta((meta & 255) + 1, R.spec, metaRender(meta)));
         p.rB[k] = make_float4(R.beta.x, R.beta.y, R.beta.z, __int_as_float(sample));
     }
     const int s0 = warpAppendS(R.sh0, &p.ctr[kCtrShadow]);
@@ -242,7 +324,7 @@ __device__ __forceinline__ HitRecord hitOfRow(float4 h4) {
     return h;
 }
 
-template <int CLS>
+template <int CLS, bool BATCH>
 __global__ void __launch_bounds__(kShadeBlockS, kShadeMinBlocks) k_sshade(StreamArgs p) {
     const int n = p.ctr[kCtrClass0 + CLS];
     const int stride = gridDim.x * blockDim.x;
@@ -253,16 +335,33 @@ __global__ void __launch_bounds__(kShadeBlockS, kShadeMinBlocks) k_sshade(Stream
         ShadeResult R;
         R.cont = R.sh0 = R.sh1 = false;
         int pix = 0, meta = 0, sample = 0;
+        long long filmIdx = 0;
         if (j < n) {
             const float4 o4 = p.qO[base + j], d4 = p.qD[base + j], b4 = p.qB[base + j], h4 = p.qH[base + j];
             pix = __float_as_int(o4.w);
             meta = __float_as_int(d4.w);
             sample = __float_as_int(b4.w);
-            const int fi = filmIndexS(p, pix);
-            shadeHit(p.sv, hitOfRow(h4), xyz(o4), xyz(d4), xyz(b4), (meta & 256) != 0, meta & 255, p.maxDepth, p.seed,
-                     static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), fi, R, p.direct != 0);
+            if constexpr (BATCH) {
+                // the render's own lights, film, depth and random streams
+                const int render = metaRender(meta);
+                const RenderMeta &M = p.renders[render];
+                SceneView S = p.sv;
+                S.lightBase = M.lightBase;
+                S.nArea = M.nArea;
+                S.nLights = M.nArea;
+                const int fi = mirrored(pix, M.W);
+                filmIdx = M.filmOffset + fi;
+                shadeHit(S, hitOfRow(h4), xyz(o4), xyz(d4), xyz(b4), (meta & 256) != 0, meta & 255, M.maxDepth, M.seed,
+                         static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), static_cast<int>(filmIdx), R, false);
+                R.s0L.w = R.s1L.w = __int_as_float(render);   // the shadow rays' tree
+            } else {
+                const int fi = filmIndexS(p, pix);
+                filmIdx = fi;
+                shadeHit(p.sv, hitOfRow(h4), xyz(o4), xyz(d4), xyz(b4), (meta & 256) != 0, meta & 255, p.maxDepth,
+                         p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), fi, R, p.direct != 0);
+            }
         }
-        emitShadeResultS(p, R, j < n, pix, meta, sample);
+        emitShadeResultS<BATCH>(p, R, j < n, filmIdx, pix, meta, sample);
     }
 }
 
@@ -326,34 +425,47 @@ __global__ void __launch_bounds__(kGTile, kGuidedMinBlocks) k_sshade_guided(Stre
                          static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), fi, R, false);
             }
         }
-        emitShadeResultS(p, R, live, pix, meta, sample);
+        emitShadeResultS(p, R, live, live ? filmIndexS(p, pix) : 0, pix, meta, sample);
     }
     tileKernelTeardown(sm, tmem, ok, phase);
     if (!ok && threadIdx.x == 0) atomicOr(&p.ctr[kCtrErr], 2);
 }
 
-template <bool STATS>
+template <bool STATS, bool BATCH>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sshadow(StreamArgs p) {
     __shared__ uint2 stack[kStackShared * kTraceBlock];
     const int n = p.ctr[kCtrShadow];
     float4 *film = filmOf(p);
     bool overflow = false;
     uint32_t nodeCount = 0, triCount = 0;
-    auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
-        const float4 d4 = p.shD[i];
-        *o = xyz(p.shO[i]);
-        *d = xyz(d4);
-        *t0 = 0.0f;
-        *t1 = d4.w;
-    };
     auto done = [&](int i, const TraceLane &L) {
         if (i >= 0 && !L.found) {
             const float3 c = xyz(p.shL[i]);
             atomicAdd(&film[__float_as_int(p.shO[i].w)], make_float4(c.x, c.y, c.z, 0.0f));
         }
     };
-    tracePersistent<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchS],
-                                 stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
+    if constexpr (BATCH) {
+        auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1, uint32_t *root) {
+            const float4 d4 = p.shD[i];
+            *o = xyz(p.shO[i]);
+            *d = xyz(d4);
+            *t0 = 0.0f;
+            *t1 = d4.w;
+            *root = p.renders[__float_as_int(p.shL[i].w)].root;
+        };
+        tracePersistent<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchS],
+                                     stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
+    } else {
+        auto fetch = [&](int i, float3 *o, float3 *d, float *t0, float *t1) {
+            const float4 d4 = p.shD[i];
+            *o = xyz(p.shO[i]);
+            *d = xyz(d4);
+            *t0 = 0.0f;
+            *t1 = d4.w;
+        };
+        tracePersistent<true, STATS>(p.sv.nodes, p.sv.tris, p.sv.nNodes, p.sv.nTris, n, &p.ctr[kCtrFetchS],
+                                     stack + threadIdx.x, kTraceBlock, &nodeCount, &triCount, &overflow, fetch, done);
+    }
     if (overflow) atomicOr(&p.ctr[kCtrErr], 1);
     if (STATS) {
         atomicAdd(&p.big[kBigVisit + 2], static_cast<unsigned long long>(nodeCount));
@@ -362,7 +474,11 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sshadow(Stream
 }
 
 // one thread: account the iteration, hand the continuations to the next one, reset the
-// per-iteration counters, raise the done flag once no path is left
+// per-iteration counters, raise the done flag once no path is left.  Batches also stamp
+// the completion time of every render whose paths have all ended, and set the device
+// loop's condition: another round while paths remain and the iteration limit is not
+// reached.
+template <bool BATCH>
 __global__ void k_sadvance(StreamArgs p) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int nNew = newPaths(p);
@@ -374,7 +490,19 @@ __global__ void k_sadvance(StreamArgs p) {
     p.ctr[kCtrRays] = p.ctr[kCtrCont];
     for (int k = kCtrCont; k <= kCtrFetchS; k++) p.ctr[k] = 0;
     if (n > 0) p.ctr[kCtrIter] += 1;
-    p.ctr[kCtrDone] = (p.ctr[kCtrRays] == 0 && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p)) ? 1 : 0;
+    const bool done = p.ctr[kCtrRays] == 0 && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p);
+    p.ctr[kCtrDone] = done ? 1 : 0;
+    if constexpr (BATCH) {
+        unsigned long long now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        for (int r = 0; r < p.nRenders; r++) {
+            const unsigned long long paths = static_cast<unsigned long long>(p.pathStart[r + 1] - p.pathStart[r]);
+            if (p.times[1 + r] == 0 && atomicAdd(&p.ended[r], 0ull) == paths) atomicCAS(&p.times[1 + r], 0ull, now);
+        }
+        const long long rounds = static_cast<long long>(++p.big[kBigRounds]);
+        if (!done && rounds >= p.iterLimit) p.ctr[kCtrErr] |= 4;   // the pool did not drain in time
+        cudaGraphSetConditional(p.cond, !done && rounds < p.iterLimit ? 1u : 0u);
+    }
 }
 
 enum KernelClassS { kSRegen = 0, kSExtend, kSShadeL, kSShadeC, kSShadeD, kSShadow, kSAdvance, kSNumClasses };
@@ -387,8 +515,8 @@ GridsS streamGrids(int device, int cap, bool guided) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int occT = 0, occS = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occT, k_sextend<false>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occS, k_sshade<0>, kShadeBlockS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occT, k_sextend<false, false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occS, k_sshade<0, false>, kShadeBlockS, 0);
     GridsS g;
     g.trace = sms * std::max(occT, 1);
     g.shade = sms * std::max(occS, 1);
@@ -398,7 +526,7 @@ GridsS streamGrids(int device, int cap, bool guided) {
 }
 
 // one iteration on stream s; with ev, every kernel is bracketed by a pair of events
-template <bool STATS>
+template <bool STATS, bool BATCH = false>
 void launchIteration(const StreamArgs &a, const GridsS &g, cudaStream_t s, cudaEvent_t *ev, int *evClass,
                      int *nev) {
     auto mark = [&](int cls) {
@@ -411,26 +539,26 @@ void launchIteration(const StreamArgs &a, const GridsS &g, cudaStream_t s, cudaE
         if (ev) cudaEventRecord(ev[(*nev)++], s);
     };
     mark(kSRegen);
-    k_sregen<<<g.regen, 256, 0, s>>>(a);
+    k_sregen<BATCH><<<g.regen, 256, 0, s>>>(a);
     done();
     mark(kSExtend);
-    k_sextend<STATS><<<g.trace, kTraceBlock, 0, s>>>(a);
+    k_sextend<STATS, BATCH><<<g.trace, kTraceBlock, 0, s>>>(a);
     done();
     mark(kSShadeL);
     if (a.packFwd) k_sshade_guided<<<g.guided, kGTile, kTileSmem, s>>>(a);
-    else k_sshade<kMatLambert><<<g.shade, kShadeBlockS, 0, s>>>(a);
+    else k_sshade<kMatLambert, BATCH><<<g.shade, kShadeBlockS, 0, s>>>(a);
     done();
     mark(kSShadeC);
-    k_sshade<kMatConductor><<<g.shade, kShadeBlockS, 0, s>>>(a);
+    k_sshade<kMatConductor, BATCH><<<g.shade, kShadeBlockS, 0, s>>>(a);
     done();
     mark(kSShadeD);
-    k_sshade<kMatDielectric><<<g.shade, kShadeBlockS, 0, s>>>(a);
+    k_sshade<kMatDielectric, BATCH><<<g.shade, kShadeBlockS, 0, s>>>(a);
     done();
     mark(kSShadow);
-    k_sshadow<STATS><<<g.trace, kTraceBlock, 0, s>>>(a);
+    k_sshadow<STATS, BATCH><<<g.trace, kTraceBlock, 0, s>>>(a);
     done();
     mark(kSAdvance);
-    k_sadvance<<<1, 32, 0, s>>>(a);
+    k_sadvance<BATCH><<<1, 32, 0, s>>>(a);
     done();
 }
 
@@ -546,7 +674,254 @@ long long iterationBound(const StreamArgs &a, long long total) {
     return 2 * (static_cast<long long>(a.maxDepth) + 2) * (total / std::max(a.cap, 1) + 2) + 16;
 }
 
+// the start of a batch run: every lane's counters and parameters (its share of the
+// batch's path sequence, the film), the per-render counts and times.  One kernel, so
+// that the reset is part of the batch's graph.
+struct BatchReset {
+    int *ctr[Ctx::kPoolLanes];
+    unsigned long long *big[Ctx::kPoolLanes];
+    long long first[Ctx::kPoolLanes], count[Ctx::kPoolLanes];
+    int lanes;
+    int nRenders;
+    unsigned long long film;
+    unsigned long long *ended, *times;
+};
+
+__global__ void k_sbatch_reset(BatchReset in) {
+    const int t = threadIdx.x;
+    for (int k = 0; k < in.lanes; k++) {
+        for (int i = t; i < kNumCtr; i += blockDim.x) in.ctr[k][i] = 0;
+        for (int i = t; i < kNumBig; i += blockDim.x)
+            in.big[k][i] = i == kBigTotal    ? static_cast<unsigned long long>(in.count[k])
+                           : i == kBigOffset ? static_cast<unsigned long long>(in.first[k])
+                           : i == kBigFilm   ? in.film
+                                             : 0ull;
+    }
+    for (int r = t; r < in.nRenders; r += blockDim.x) {
+        in.ended[r] = 0;
+        in.times[1 + r] = 0;
+    }
+    if (t == 0) {
+        unsigned long long now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        in.times[0] = now;
+    }
+}
+
 }  // namespace
+
+struct StreamBatch {
+    int lanes = 1, iterations = 0;
+    StreamQueues q[Ctx::kPoolLanes];   // the batch's own pools (the context's serve spgpu_render)
+    SceneView sv{};                    // the merged scenes
+    RenderMeta *renders = nullptr;     // device
+    long long *pathStart = nullptr;    // device, nRenders + 1
+    unsigned long long *ended = nullptr, *times = nullptr;
+    int nRenders = 0, maxDepth = 0;
+    std::vector<long long> hostStart;
+    cudaGraphExec_t exec = nullptr;
+    float4 *execFilm = nullptr;
+    long long rounds[Ctx::kPoolLanes] = {};
+};
+
+void freeStreamBatch(StreamBatch *SB) {
+    if (!SB) return;
+    if (SB->exec) cudaGraphExecDestroy(SB->exec);
+    for (auto &q : SB->q) freeStreamQueues(&q);
+    cudaFree(SB->renders);
+    cudaFree(SB->pathStart);
+    cudaFree(SB->ended);
+    cudaFree(SB->times);
+    delete SB;
+}
+
+int streamBatchCreate(Ctx &C, StreamBatch **slot, const SceneView &merged, const std::vector<RenderMeta> &renders,
+                      int poolSlots, int lanes, int iterations) {
+    freeStreamBatch(*slot);
+    *slot = nullptr;
+    if (renders.empty() || poolSlots <= 0 || lanes < 1 || lanes > Ctx::kPoolLanes || iterations < 1) {
+        setError("spgpu_batch_prepare: invalid streaming batch shape");
+        return SPGPU_EINVAL;
+    }
+    auto *SB = new StreamBatch();
+    SB->lanes = lanes;
+    SB->iterations = iterations;
+    SB->sv = merged;
+    SB->nRenders = static_cast<int>(renders.size());
+    SB->hostStart.assign(renders.size() + 1, 0);
+    for (size_t r = 0; r < renders.size(); r++) {
+        const RenderMeta &M = renders[r];
+        SB->hostStart[r + 1] = SB->hostStart[r] + static_cast<long long>(M.W) * M.H * M.spp;
+        SB->maxDepth = std::max(SB->maxDepth, M.maxDepth);
+    }
+    const long long total = SB->hostStart.back();
+    const int cap = static_cast<int>(std::min<long long>(poolSlots, std::max<long long>(1, (total + lanes - 1) / lanes)));
+    int rc = 0;
+    for (int k = 0; k < lanes && rc == 0; k++) rc = ensureStreamQueues(SB->q[k], cap);
+    cudaError_t e = cudaSuccess;
+    if (rc == 0) e = cudaMalloc(&SB->renders, sizeof(RenderMeta) * renders.size());
+    if (rc == 0 && e == cudaSuccess) e = cudaMalloc(&SB->pathStart, sizeof(long long) * SB->hostStart.size());
+    if (rc == 0 && e == cudaSuccess) e = cudaMalloc(&SB->ended, sizeof(unsigned long long) * renders.size());
+    if (rc == 0 && e == cudaSuccess) e = cudaMalloc(&SB->times, sizeof(unsigned long long) * (renders.size() + 1));
+    if (rc == 0 && e == cudaSuccess)
+        e = cudaMemcpy(SB->renders, renders.data(), sizeof(RenderMeta) * renders.size(), cudaMemcpyHostToDevice);
+    if (rc == 0 && e == cudaSuccess)
+        e = cudaMemcpy(SB->pathStart, SB->hostStart.data(), sizeof(long long) * SB->hostStart.size(),
+                       cudaMemcpyHostToDevice);
+    if (rc == 0 && e != cudaSuccess) rc = cudaFail("spgpu_batch_prepare", e);
+    if (rc) {
+        freeStreamBatch(SB);
+        return rc;
+    }
+    *slot = SB;
+    return 0;
+}
+
+namespace {
+
+// the lane's kernel arguments: the merged scenes, the lane's pool, the batch tables
+StreamArgs batchLaneArgs(const StreamBatch &SB, int k, cudaGraphConditionalHandle cond) {
+    StreamArgs a;
+    std::memset(&a, 0, sizeof(a));
+    const StreamQueues &q = SB.q[k];
+    a.sv = SB.sv;
+    a.maxDepth = SB.maxDepth;
+    a.cap = q.capacity;
+    a.rO = q.rO;
+    a.rD = q.rD;
+    a.rB = q.rB;
+    a.qO = q.qO;
+    a.qD = q.qD;
+    a.qB = q.qB;
+    a.qH = q.qH;
+    a.shO = q.shO;
+    a.shD = q.shD;
+    a.shL = q.shL;
+    a.ctr = q.ctr;
+    a.big = q.big;
+    a.renders = SB.renders;
+    a.pathStart = SB.pathStart;
+    a.nRenders = SB.nRenders;
+    a.ended = SB.ended;
+    a.times = SB.times;
+    a.cond = cond;
+    return a;
+}
+
+// The batch's graph: the reset kernel, then per lane a conditional while node whose
+// body is `iterations` wavefront iterations; the body's last k_sadvance decides
+// whether the loop goes round again.  Film address baked in (recaptured per film).
+int buildBatchGraph(Ctx &C, StreamBatch &SB, float4 *film) {
+    if (SB.exec) cudaGraphExecDestroy(SB.exec);
+    SB.exec = nullptr;
+    const long long total = SB.hostStart.back();
+    BatchReset init;
+    std::memset(&init, 0, sizeof(init));
+    init.lanes = SB.lanes;
+    init.nRenders = SB.nRenders;
+    init.film = reinterpret_cast<unsigned long long>(film);
+    init.ended = SB.ended;
+    init.times = SB.times;
+    for (int k = 0; k < SB.lanes; k++) {
+        init.ctr[k] = SB.q[k].ctr;
+        init.big[k] = SB.q[k].big;
+        init.first[k] = total * k / SB.lanes;
+        init.count[k] = total * (k + 1) / SB.lanes - init.first[k];
+    }
+    cudaStream_t cs = C.stream;
+    cudaGraph_t G = nullptr;
+    cudaError_t e = cudaGraphCreate(&G, 0);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs, G, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        k_sbatch_reset<<<1, 256, 0, cs>>>(init);
+        e = cudaStreamEndCapture(cs, &G);
+    }
+    cudaGraphNode_t resetNode = nullptr;
+    size_t nNodes = 1;
+    if (e == cudaSuccess) e = cudaGraphGetNodes(G, &resetNode, &nNodes);
+    const GridsS g = streamGrids(C.device, SB.q[0].capacity, false);
+    for (int k = 0; k < SB.lanes && e == cudaSuccess; k++) {
+        cudaGraphConditionalHandle h = 0;
+        e = cudaGraphConditionalHandleCreate(&h, G, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, G, &resetNode, nullptr, 1, &cp);
+        if (e != cudaSuccess) break;
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        StreamArgs a = batchLaneArgs(SB, k, h);
+        a.iterLimit = iterationBound(a, init.count[k]);
+        e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) break;
+        for (int it = 0; it < SB.iterations; it++) launchIteration<false, true>(a, g, cs, nullptr, nullptr, nullptr);
+        e = cudaStreamEndCapture(cs, &body);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&SB.exec, G, 0);
+    if (G) cudaGraphDestroy(G);
+    if (e != cudaSuccess) {
+        SB.exec = nullptr;
+        return cudaFail("spgpu_batch_run (graph)", e);
+    }
+    SB.execFilm = film;
+    return 0;
+}
+
+}  // namespace
+
+int streamBatchRun(Ctx &C, StreamBatch &SB, float4 *film, double *renderMs, unsigned long long *statsOut,
+                   float *msOut, cudaStream_t stream) {
+    if (!SB.exec || SB.execFilm != film) {
+        if (int rc = buildBatchGraph(C, SB, film)) return rc;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = cudaEventRecord(e0, stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(SB.exec, stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
+    std::vector<unsigned long long> times(SB.nRenders + 1);
+    unsigned long long big[Ctx::kPoolLanes][kNumBig] = {};
+    int ctr[Ctx::kPoolLanes][kNumCtr] = {};
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(times.data(), SB.times, sizeof(unsigned long long) * times.size(), cudaMemcpyDeviceToHost,
+                            stream);
+    for (int k = 0; k < SB.lanes && e == cudaSuccess; k++) {
+        e = cudaMemcpyAsync(big[k], SB.q[k].big, sizeof(big[k]), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctr[k], SB.q[k].ctr, sizeof(ctr[k]), cudaMemcpyDeviceToHost, stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cudaFail("spgpu_batch_run", e);
+    int err = 0;
+    bool drained = true;
+    for (int k = 0; k < 4; k++) statsOut[k] = 0;
+    for (int k = 0; k < SB.lanes; k++) {
+        statsOut[0] += big[k][kBigPaths];
+        statsOut[1] += big[k][kBigClosest];
+        statsOut[2] += big[k][kBigShadow];
+        statsOut[3] += big[k][kBigRounds] * kSNumClasses + 1;
+        err |= ctr[k][kCtrErr];
+        drained = drained && ctr[k][kCtrDone];
+    }
+    for (int r = 0; r < SB.nRenders; r++)
+        renderMs[r] = times[1 + r] >= times[0] && times[1 + r] ? (times[1 + r] - times[0]) * 1.0e-6 : -1.0;
+    *msOut = ms;
+    if (err & 1) {
+        setError("spgpu_batch_run: traversal stack overflow");
+        return SPGPU_EKERNEL;
+    }
+    if ((err & 4) || !drained) {
+        setError("spgpu_batch_run: the path pools did not drain within their iteration bound");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
+}
 
 void freeStreamQueues(StreamQueues *q) {
     if (q->graph) cudaGraphExecDestroy(q->graph);

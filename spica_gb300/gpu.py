@@ -68,7 +68,8 @@ class BatchItem(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("block", C.c_int32), ("tile_pixels", C.c_int32), ("chunk_spp", C.c_int32),
-                ("candidates", C.c_int32), ("calib_ms", C.c_double)]
+                ("candidates", C.c_int32), ("calib_ms", C.c_double), ("engine", C.c_int32),
+                ("pool_slots", C.c_int32), ("pool_lanes", C.c_int32), ("iterations", C.c_int32)]
 
 
 class GuidingConfig(C.Structure):
@@ -78,6 +79,7 @@ class GuidingConfig(C.Structure):
 
 
 GUIDE_GUIDED, GUIDE_COLLECT, GUIDE_MEGAKERNEL = 1, 2, 4
+BATCH_STREAM, BATCH_PERSISTENT = 1, 2   # batch engines (spgpu_batch_tuning.engine)
 FILM_RGBE, FILM_GAMMA_BYTES, FILM_REINHARD, FILM_DRAGO, FILM_DURAND = 0, 1, 2, 3, 4
 
 
@@ -556,11 +558,13 @@ class GpuDirectLightingIntegrator(GpuPathIntegrator):
 
 
 class GpuBatch:
-    """Many small renders traced in one persistent launch (spgpu_batch_prepare / run).
-    scenes: list of scenes.Scene with width, height, spp, max_depth and camera set."""
+    """Many small renders traced in one graph launch (spgpu_batch_prepare / run).
+    scenes: list of scenes.Scene with width, height, spp, max_depth and camera set.
+    autotune: False (0) for the streaming wavefront with its default pool, True (1) to
+    time the candidates of both engines, BATCH_PERSISTENT (2) for the megakernel."""
 
     def __init__(self, scene_list, seed: int = 0, autotune: bool = True, device: int = 0,
-                 ctx: Optional[Context] = None):
+                 ctx: Optional[Context] = None, pool: Optional[tuple] = None):
         self.ctx = ctx or Context(device)
         self.scenes = list(scene_list)
         self._keep = []
@@ -584,6 +588,8 @@ class GpuBatch:
             self.offsets.append(off)
             off += sc.width * sc.height
         self.tuning = BatchTuning()
+        if pool is not None:   # (slots, lanes) of the streaming pools, with autotune 0
+            self.tuning.pool_slots, self.tuning.pool_lanes = int(pool[0]), int(pool[1])
         _check(self.ctx.lib.spgpu_batch_prepare(self.ctx.h, len(self.scenes), items, int(autotune),
                                                 C.byref(self.tuning)), "spgpu_batch_prepare")
         self.pixels = int(self.ctx.lib.spgpu_batch_film_pixels(self.ctx.h))
