@@ -410,6 +410,10 @@ typedef struct {
 } spgpu_kernel_profile;
 int spgpu_render_profile(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film, spgpu_kernel_profile *out,
                          void *stream);
+/* the same for a prepared streaming batch (engine SPGPU_BATCH_STREAM): the batch's
+ * wavefront launched kernel by kernel from the host with one pool, timed per kernel
+ * class, then again with BVH visit counters; films receive both runs */
+int spgpu_batch_profile(spgpu_ctx *ctx, float *films, spgpu_kernel_profile *out, void *stream);
 
 #ifdef __cplusplus
 }

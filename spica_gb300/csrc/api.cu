@@ -1005,6 +1005,36 @@ int spgpu_batch_run(spgpu_ctx *h, float *films, double *render_ms, spgpu_render_
     });
 }
 
+int spgpu_batch_profile(spgpu_ctx *h, float *films, spgpu_kernel_profile *out, void *stream) {
+    return guarded("spgpu_batch_profile", [&]() -> int {
+        NvtxRange nvtxRange("spgpu_batch_profile");
+        if (!h || !films || !out || (reinterpret_cast<uintptr_t>(films) & 15)) {
+            setError("spgpu_batch_profile: invalid arguments (films 16-byte aligned)");
+            return SPGPU_EINVAL;
+        }
+        Ctx &C = h->c;
+        if (!C.batch) {
+            setError("spgpu_batch_profile: no batch prepared");
+            return SPGPU_ESTATE;
+        }
+        cudaSetDevice(C.device);
+        std::memset(out, 0, sizeof(*out));
+        long long launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        unsigned long long st[4] = {0, 0, 0, 0}, vis[4] = {0, 0, 0, 0};
+        const int rc = batchProfile(C, *C.batch, reinterpret_cast<float4 *>(films), out->kernel_ms, launches, st, vis,
+                                    static_cast<cudaStream_t>(stream));
+        for (int k = 0; k < 8; k++) out->launches[k] = launches[k];
+        out->paths = static_cast<int64_t>(st[0]);
+        out->rays_closest = static_cast<int64_t>(st[1]);
+        out->rays_shadow = static_cast<int64_t>(st[2]);
+        out->closest_nodes_per_ray = st[1] ? static_cast<double>(vis[0]) / st[1] : 0.0;
+        out->closest_tris_per_ray = st[1] ? static_cast<double>(vis[1]) / st[1] : 0.0;
+        out->shadow_nodes_per_ray = st[2] ? static_cast<double>(vis[2]) / st[2] : 0.0;
+        out->shadow_tris_per_ray = st[2] ? static_cast<double>(vis[3]) / st[2] : 0.0;
+        return rc;
+    });
+}
+
 int spgpu_guiding_init(spgpu_ctx *h, const spgpu_guiding_config *cfg) {
     return guarded("spgpu_guiding_init", [&]() -> int {
         NvtxRange nvtxRange("spgpu_guiding_init");

@@ -521,4 +521,14 @@ int batchRun(Ctx &C, BatchState &B, float4 *film, double *renderMs, unsigned lon
     return 0;
 }
 
+int batchProfile(Ctx &C, BatchState &B, float4 *film, double *kernelMs, long long *launches,
+                 unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream) {
+    if (B.engine != SPGPU_BATCH_STREAM || !B.sb) {
+        setError("spgpu_batch_profile: the batch runs on the persistent megakernel; profiles cover the streaming "
+                 "wavefront");
+        return SPGPU_ESTATE;
+    }
+    return streamBatchProfile(C, *B.sb, film, kernelMs, launches, statsOut, visitOut, stream);
+}
+
 }  // namespace spgpu

@@ -243,6 +243,8 @@ int streamBatchCreate(Ctx &C, StreamBatch **slot, const SceneView &merged, const
                       int poolSlots, int lanes, int iterations);
 int streamBatchRun(Ctx &C, StreamBatch &SB, float4 *film, double *renderMs, unsigned long long *statsOut,
                    float *msOut, cudaStream_t stream);
+int streamBatchProfile(Ctx &C, StreamBatch &SB, float4 *film, double *kernelMs, long long *launches,
+                       unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream);
 void freeStreamBatch(StreamBatch *SB);
 
 // learned-guiding state that a guided wavefront pass reads (guide.cu fills it)
@@ -295,6 +297,8 @@ int batchPrepare(spgpu_ctx *self, BatchState **slot, int count, const spgpu_batc
                  spgpu_batch_tuning *tuning);
 int batchRun(Ctx &C, BatchState &B, float4 *film, double *renderMs, unsigned long long *statsOut, float *msOut,
              cudaStream_t stream);
+int batchProfile(Ctx &C, BatchState &B, float4 *film, double *kernelMs, long long *launches,
+                 unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream);
 int64_t batchPixels(const BatchState &B);
 int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg);
 int guideParams(Ctx &C, GuideState &G, float *host, int set);

@@ -118,6 +118,7 @@ struct StreamArgs {
     unsigned long long *ended;
     unsigned long long *times;
     cudaGraphConditionalHandle cond;
+    int devLoop;        // the iterations run in a device loop on cond (else the host drives them)
     long long iterLimit;
 };
 
@@ -501,7 +502,7 @@ __global__ void k_sadvance(StreamArgs p) {
         }
         const long long rounds = static_cast<long long>(++p.big[kBigRounds]);
         if (!done && rounds >= p.iterLimit) p.ctr[kCtrErr] |= 4;   // the pool did not drain in time
-        cudaGraphSetConditional(p.cond, !done && rounds < p.iterLimit ? 1u : 0u);
+        if (p.devLoop) cudaGraphSetConditional(p.cond, !done && rounds < p.iterLimit ? 1u : 0u);
     }
 }
 
@@ -853,6 +854,7 @@ int buildBatchGraph(Ctx &C, StreamBatch &SB, float4 *film) {
         if (e != cudaSuccess) break;
         cudaGraph_t body = cp.conditional.phGraph_out[0];
         StreamArgs a = batchLaneArgs(SB, k, h);
+        a.devLoop = 1;
         a.iterLimit = iterationBound(a, init.count[k]);
         e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) break;
@@ -1108,6 +1110,79 @@ int renderStreamProfile(Ctx *ctx, const float *camera, int W, int H, int spp, in
     if (ctr[kCtrErr]) {
         setError(ctr[kCtrErr] & 1 ? "spgpu_render_profile: traversal stack overflow"
                                   : "spgpu_render_profile: tensor-core wait of the guided shading timed out");
+        return SPGPU_EKERNEL;
+    }
+    return 0;
+}
+
+}  // namespace spgpu
+
+namespace spgpu {
+
+// The batch's streaming wavefront launched kernel by kernel from the host (no graph),
+// lane 0's pool taking the whole path sequence: pass 0 times every kernel with events,
+// pass 1 renders the same paths again with the BVH visit counters on (the film receives
+// both passes).  kernelMs/launches per kernel class.
+int streamBatchProfile(Ctx &C, StreamBatch &SB, float4 *film, double *kernelMs, long long *launches,
+                       unsigned long long *statsOut, unsigned long long *visitOut, cudaStream_t stream) {
+    for (int k = 0; k < kSNumClasses; k++) {
+        kernelMs[k] = 0.0;
+        launches[k] = 0;
+    }
+    for (int k = 0; k < 4; k++) statsOut[k] = visitOut[k] = 0;
+    StreamArgs a = batchLaneArgs(SB, 0, 0);
+    const long long total = SB.hostStart.back();
+    a.iterLimit = iterationBound(a, total);
+    BatchReset init;
+    std::memset(&init, 0, sizeof(init));
+    init.lanes = 1;
+    init.nRenders = SB.nRenders;
+    init.film = reinterpret_cast<unsigned long long>(film);
+    init.ended = SB.ended;
+    init.times = SB.times;
+    init.ctr[0] = SB.q[0].ctr;
+    init.big[0] = SB.q[0].big;
+    init.first[0] = 0;
+    init.count[0] = total;
+    const GridsS g = streamGrids(C.device, a.cap, false);
+    std::vector<cudaEvent_t> ev(2 * kSNumClasses);
+    std::vector<int> cls(kSNumClasses + 1);
+    for (auto &x : ev) cudaEventCreate(&x);
+    unsigned long long big[kNumBig] = {};
+    int ctr[kNumCtr] = {};
+    cudaError_t e = cudaSuccess;
+    for (int pass = 0; pass < 2 && e == cudaSuccess; pass++) {
+        k_sbatch_reset<<<1, 256, 0, stream>>>(init);
+        e = cudaGetLastError();
+        for (long long it = 0; it < a.iterLimit && e == cudaSuccess; it++) {
+            int nev = 0;
+            if (pass == 0) launchIteration<false, true>(a, g, stream, ev.data(), cls.data(), &nev);
+            else launchIteration<true, true>(a, g, stream, nullptr, nullptr, nullptr);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpyAsync(ctr, SB.q[0].ctr, sizeof(ctr), cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            for (int i = 0; i + 1 < nev && e == cudaSuccess; i += 2) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+                kernelMs[cls[i / 2]] += ms;
+                launches[cls[i / 2]] += 1;
+            }
+            if (ctr[kCtrDone]) break;
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(big, SB.q[0].big, sizeof(big), cudaMemcpyDeviceToHost);
+        if (pass == 0)
+            for (int k = 0; k < 3; k++) statsOut[k] = big[kBigPaths + k];
+        else
+            for (int k = 0; k < 4; k++) visitOut[k] = big[kBigVisit + k];
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return cudaFail("spgpu_batch_profile", e);
+    if (ctr[kCtrErr] & 1) {
+        setError("spgpu_batch_profile: traversal stack overflow");
+        return SPGPU_EKERNEL;
+    }
+    if (!ctr[kCtrDone]) {
+        setError("spgpu_batch_profile: the path pool did not drain within its iteration bound");
         return SPGPU_EKERNEL;
     }
     return 0;

@@ -179,7 +179,7 @@ EXPORTS = ["spgpu_create", "spgpu_destroy", "spgpu_last_error", "spgpu_version",
            "spgpu_batch_film_pixels", "spgpu_batch_run", "spgpu_guiding_init", "spgpu_guiding_render",
            "spgpu_guiding_train", "spgpu_guiding_samples", "spgpu_guiding_ring", "spgpu_guiding_params", "spgpu_guiding_mlp",
            "spgpu_guiding_grad", "spgpu_scene_load", "spgpu_scene_free", "spgpu_load_hdr", "spgpu_bsdf_eval",
-           "spgpu_bsdf_sample", "spgpu_sampler_generate"]
+           "spgpu_bsdf_sample", "spgpu_sampler_generate", "spgpu_batch_profile"]
 
 _lib = None
 
@@ -219,6 +219,7 @@ def load_library(path: Optional[str] = None):
     lib.spgpu_batch_prepare.argtypes = [vp, i32, C.POINTER(BatchItem), i32, C.POINTER(BatchTuning)]
     lib.spgpu_batch_film_pixels.argtypes = [vp]
     lib.spgpu_batch_run.argtypes = [vp, vp, vp, C.POINTER(RenderStats), vp]
+    lib.spgpu_batch_profile.argtypes = [vp, vp, C.POINTER(KernelProfile), vp]
     lib.spgpu_guiding_init.argtypes = [vp, C.POINTER(GuidingConfig)]
     lib.spgpu_guiding_render.argtypes = [vp, C.POINTER(RenderDesc), vp, i32, C.POINTER(RenderStats), vp]
     lib.spgpu_guiding_train.argtypes = [vp, i32, C.POINTER(C.c_double)]
@@ -603,6 +604,14 @@ class GpuBatch:
         _check(self.ctx.lib.spgpu_batch_run(self.ctx.h, _ptr(films), ms.ctypes.data, C.byref(st),
                                             C.c_void_p(stream) if stream else None), "spgpu_batch_run")
         return ms, st
+
+    def profile(self, films, stream: int = 0) -> KernelProfile:
+        """Per-kernel event timings of one run of a streaming batch, launched kernel by
+        kernel from the host (spgpu_batch_profile); films receive two runs."""
+        pr = KernelProfile()
+        _check(self.ctx.lib.spgpu_batch_profile(self.ctx.h, _ptr(films), C.byref(pr),
+                                                C.c_void_p(stream) if stream else None), "spgpu_batch_profile")
+        return pr
 
     def film(self, films_host, i):
         sc = self.scenes[i]

@@ -3,7 +3,7 @@ case), separate from the benchmark:
 
     python -m spica_gb300.profcases render [--width W] [--height H] [--spp N] [--warmup K]
     python -m spica_gb300.profcases micro [--rays N]
-    python -m spica_gb300.profcases batch [--renders N]
+    python -m spica_gb300.profcases batch [--renders N] [--engine stream|persistent] [--no-graph]
     python -m spica_gb300.profcases guided [--wavefront 0|1]
     python -m spica_gb300.profcases build [--levels L]
     python -m spica_gb300.profcases film [--width W] [--height H]
@@ -14,7 +14,11 @@ render  the mid-scale scene (500 instances, ~2.03M triangles, depth 16) at W x H
         k_sshade<0..2>, k_sshadow, k_sadvance)
 micro   the intersection microbench's sphere (1,048,576 triangles) and N of its rays,
         closest then any hit (k_trace)
-batch   the first N seeded box-room variants in one persistent batch launch (k_batch)
+batch   the first N seeded box-room variants as one batch: with --engine stream (the
+        default) its graph run, then the same batch kernel by kernel from the host inside
+        the NVTX range "profiled" (k_sregen, k_sextend, k_sshade<0..2>, k_sshadow,
+        k_sadvance, their batch forms; --no-graph skips the graph run); with --engine
+        persistent the megakernel (k_batch)
 guided  the guiding room at 640 x 360: 8 collection passes of 2 spp with 32 Adam steps
         each (k_collect, k_gather, k_guide_train, k_adam), then one plain and one guided
         render of 8 spp inside the NVTX range "profiled" (k_sshade_guided on the streaming
@@ -73,13 +77,26 @@ def _micro(args, torch):
 
 def _batch(args, torch):
     from . import GpuBatch, scenes
+    from .gpu import BATCH_PERSISTENT, KERNEL_CLASSES
     vs = scenes.batch_variants(64, seed=0)[:args.renders]
-    b = GpuBatch(vs, seed=7, autotune=False)
+    persistent = args.engine == "persistent"
+    b = GpuBatch(vs, seed=7, autotune=BATCH_PERSISTENT if persistent else 0)
     films = torch.zeros((b.pixels, 4), dtype=torch.float32, device="cuda")
-    b.run(films)
-    ms, st = b.run(films)
-    torch.cuda.synchronize()
-    return {"case": "batch", "renders": len(vs), "ms": st.ms}
+    out = {"case": "batch", "engine": args.engine, "renders": len(vs)}
+    if not args.no_graph:
+        b.run(films)
+        ms, st = b.run(films)
+        torch.cuda.synchronize()
+        out.update(ms=st.ms, samples_per_s=st.paths / (st.ms / 1e3))
+    if not persistent:
+        # the same batch kernel by kernel from the host, inside the NVTX range "profiled"
+        torch.cuda.nvtx.range_push("profiled")
+        pr = b.profile(films)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out["kernel_ms"] = {n: pr.kernel_ms[k] for k, n in enumerate(KERNEL_CLASSES)}
+        out["launches"] = {n: pr.launches[k] for k, n in enumerate(KERNEL_CLASSES)}
+    return out
 
 
 def _guided(args, torch):
@@ -146,6 +163,8 @@ def main(argv=None):
     ap.add_argument("--renders", type=int, default=4)
     ap.add_argument("--levels", type=int, default=0)
     ap.add_argument("--wavefront", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--engine", default="stream", choices=["stream", "persistent"])
+    ap.add_argument("--no-graph", action="store_true", help="batch: skip the graph runs, profile only")
     args = ap.parse_args(argv)
     import torch
     torch.cuda.set_device(0)

@@ -71,6 +71,7 @@ _NULL_CALLS = [
     ("spgpu_render_profile", (None, None, None, None, None)),
     ("spgpu_batch_prepare", (None, 0, None, 0, None)),
     ("spgpu_batch_run", (None, None, None, None, None)),
+    ("spgpu_batch_profile", (None, None, None, None)),
     ("spgpu_guiding_init", (None, None)),
     ("spgpu_guiding_render", (None, None, None, 0, None, None)),
     ("spgpu_guiding_train", (None, 0, None)),

@@ -92,3 +92,28 @@ def test_streaming_batch_many_renders_small_pool(gpulib):
         ref = GpuPathIntegrator(seed=5).render(v.camera, acc, {"width": v.width, "height": v.height,
                                                                "maxDepth": v.max_depth, "sampleCount": v.spp})
         np.testing.assert_allclose(got[..., :3], ref[..., :3], rtol=2e-4, atol=2e-4)
+
+
+def test_batch_profile_matches_run(gpulib):
+    """The host-driven profile of a streaming batch traces the same paths as its graph
+    run (same counts, same films up to summation order) and times every kernel class;
+    a persistent batch has no such profile."""
+    import torch
+    from spica_gb300 import SpgpuError
+    from spica_gb300.gpu import KERNEL_CLASSES
+    vs = small_variants(4, seed=13)
+    b = GpuBatch(vs, seed=3, autotune=0, pool=(8192, 2))
+    films = torch.zeros((b.pixels, 4), dtype=torch.float32, device="cuda")
+    _, st = b.run(films)
+    prof_films = torch.zeros_like(films)
+    pr = b.profile(prof_films)
+    torch.cuda.synchronize()
+    assert pr.paths == st.paths and pr.rays_closest == st.rays_closest and pr.rays_shadow == st.rays_shadow
+    assert all(pr.launches[k] > 0 and pr.kernel_ms[k] > 0 for k in range(len(KERNEL_CLASSES)))
+    assert pr.closest_nodes_per_ray > 0
+    a, p2 = films.cpu().numpy(), prof_films.cpu().numpy() / 2   # the profile renders twice
+    np.testing.assert_array_equal(a[:, 3], p2[:, 3])
+    np.testing.assert_allclose(a[:, :3], p2[:, :3], rtol=2e-4, atol=2e-4)
+    bp = GpuBatch(vs, seed=3, autotune=BATCH_PERSISTENT)
+    with pytest.raises(SpgpuError):
+        bp.profile(films)
