@@ -104,6 +104,17 @@ void buildDistribution1D(const double *f, int n, std::vector<float> *cdfOut, dou
     cdfOut->assign(cdf.begin(), cdf.end());
 }
 
+// guide table of a cdf over n intervals (sample1DGuided): guide[k] = the largest i with
+// cdf[i] <= k / n, k = 0..n
+void buildGuide(const float *cdf, int n, int *guide) {
+    int i = 0;
+    for (int k = 0; k <= n; k++) {
+        const double t = static_cast<double>(k) / n;
+        while (i < n && static_cast<double>(cdf[i + 1]) <= t) i++;
+        guide[k] = i;
+    }
+}
+
 int uploadEnv(Ctx &C, int W, int H, const float *img, double3 center, double radius) {
     if ((W & (W - 1)) != 0 || (H & (H - 1)) != 0) {
         setError("spgpu_upload_scene: environment map width and height must be powers of two");
@@ -133,6 +144,11 @@ int uploadEnv(Ctx &C, int W, int H, const float *img, double3 center, double rad
     }
     double margInt;
     buildDistribution1D(marg.data(), H, &margCdf, &margInt);
+    std::vector<int> condGuide(static_cast<size_t>(W + 1) * H), margGuide(H + 1);
+    for (int v = 0; v < H; v++)
+        buildGuide(condCdf.data() + static_cast<size_t>(v) * (W + 1), W,
+                   condGuide.data() + static_cast<size_t>(v) * (W + 1));
+    buildGuide(margCdf.data(), H, margGuide.data());
     std::vector<float4> tex(static_cast<size_t>(W) * H);
     for (size_t i = 0; i < tex.size(); i++) tex[i] = make_float4(img[3 * i], img[3 * i + 1], img[3 * i + 2], 0.0f);
     DeviceEnv &E = C.env;
@@ -144,6 +160,8 @@ int uploadEnv(Ctx &C, int W, int H, const float *img, double3 center, double rad
     if ((rc = upload(&E.condFunc, condFunc.data(), condFunc.size(), C.stream))) return rc;
     if ((rc = upload(&E.margCdf, margCdf.data(), margCdf.size(), C.stream))) return rc;
     if ((rc = upload(&E.margFunc, margFunc.data(), margFunc.size(), C.stream))) return rc;
+    if ((rc = upload(&E.condGuide, condGuide.data(), condGuide.size(), C.stream))) return rc;
+    if ((rc = upload(&E.margGuide, margGuide.data(), margGuide.size(), C.stream))) return rc;
     E.margIntegral = static_cast<float>(margInt);
     E.center = mk(static_cast<float>(center.x), static_cast<float>(center.y), static_cast<float>(center.z));
     E.radius = static_cast<float>(radius);
@@ -156,6 +174,8 @@ void freeEnv(DeviceEnv *E) {
     cudaFree(E->condFunc);
     cudaFree(E->margCdf);
     cudaFree(E->margFunc);
+    cudaFree(E->condGuide);
+    cudaFree(E->margGuide);
     *E = DeviceEnv{};
 }
 

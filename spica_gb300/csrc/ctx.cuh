@@ -38,6 +38,8 @@ struct DeviceEnv {
     float *condFunc = nullptr;    // [h*w]
     float *margCdf = nullptr;     // [h+1]
     float *margFunc = nullptr;    // [h]  (= row integrals)
+    int *condGuide = nullptr;     // [h*(w+1)] guide tables of the rows (sample1DGuided)
+    int *margGuide = nullptr;     // [h+1]
     float margIntegral = 0.0f;
     float3 center{0, 0, 0};
     float radius = 0.0f;

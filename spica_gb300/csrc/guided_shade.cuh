@@ -94,8 +94,9 @@ __device__ __forceinline__ void shadeGuidedLambert(const SceneView &S, float3 ps
             const DeviceEnv &E = S.env;
             float pv, pu;
             int vOff, uOff;
-            const float vv = sample1D(E.margCdf, E.margFunc, E.h, E.margIntegral, r0.c, &pv, &vOff);
-            const float uu = sample1D(E.condCdf + static_cast<int64_t>(vOff) * (E.w + 1),
+            const float vv = sample1DGuided(E.margCdf, E.margGuide, E.margFunc, E.h, E.margIntegral, r0.c, &pv, &vOff);
+            const float uu = sample1DGuided(E.condCdf + static_cast<int64_t>(vOff) * (E.w + 1),
+                                      E.condGuide + static_cast<int64_t>(vOff) * (E.w + 1),
                                       E.condFunc + static_cast<int64_t>(vOff) * E.w, E.w,
                                       __ldg(&E.margFunc[vOff]), r0.b, &pu, &uOff);
             const float mapPdf = pu * pv;

@@ -34,11 +34,19 @@ __device__ __forceinline__ float3 envLe(const DeviceEnv &E, float3 d) {   // Env
     dirToUV(normalize(d), &u, &v);
     return envLookup(E, u, v);
 }
-// Distribution1D::sample over cdf[0..n] / func[0..n-1] (core/sampling.cc:75)
-__device__ __forceinline__ float sample1D(const float *cdf, const float *func, int n, float integral, float u,
-                                          float *pdf, int *off) {
-    int lo = 0, hi = n;   // largest i in [0, n] with cdf[i] <= u
-    while (lo < hi) {
+// Distribution1D::sample over cdf[0..n] / func[0..n-1] (core/sampling.cc:75): the
+// interval i of the largest cdf[i] <= u, the offset within it, and the pdf
+// func[i] / integral.  The search is
+// narrowed by a guide table (the cutpoint method of Chen and Asau, 1974): guide[k] is
+// the largest i with cdf[i] <= k / n, and for k = floor(u n)
+// computed in float, (k - 1) / n < u < (k + 2) / n, so [guide[k - 1], guide[k + 2]] holds
+// the answer.  The same comparisons on that range give the full search's result in two
+// or three steps instead of log2(n).
+__device__ __forceinline__ float sample1DGuided(const float *cdf, const int *guide, const float *func, int n,
+                                                float integral, float u, float *pdf, int *off) {
+    const int k = min(max(static_cast<int>(u * n), 0), n);
+    int lo = __ldg(&guide[max(k - 1, 0)]), hi = __ldg(&guide[min(k + 2, n)]);
+    while (lo < hi) {   // largest i in [lo, hi] with cdf[i] <= u
         const int mid = (lo + hi + 1) >> 1;
         if (__ldg(&cdf[mid]) <= u) lo = mid;
         else hi = mid - 1;
@@ -181,8 +189,9 @@ __device__ __forceinline__ void shadeHit(const SceneView &S, const HitRecord &h,
                 const DeviceEnv &E = S.env;
                 float pv, pu;
                 int vOff, uOff;
-                const float vv = sample1D(E.margCdf, E.margFunc, E.h, E.margIntegral, r0.c, &pv, &vOff);
-                const float uu = sample1D(E.condCdf + static_cast<int64_t>(vOff) * (E.w + 1),
+                const float vv = sample1DGuided(E.margCdf, E.margGuide, E.margFunc, E.h, E.margIntegral, r0.c, &pv, &vOff);
+                const float uu = sample1DGuided(E.condCdf + static_cast<int64_t>(vOff) * (E.w + 1),
+                                          E.condGuide + static_cast<int64_t>(vOff) * (E.w + 1),
                                           E.condFunc + static_cast<int64_t>(vOff) * E.w, E.w,
                                           __ldg(&E.margFunc[vOff]), r0.b, &pu, &uOff);
                 const float mapPdf = pu * pv;
