@@ -81,22 +81,38 @@ __device__ __forceinline__ float vmfPdf(float3 w, float3 mu, float kappa) {
 }
 __device__ __forceinline__ float kappaOf(float raw) { return __expf(clampf(raw, -4.0f, 7.0f)); }
 
+// The mixture as the shading kernels sample and evaluate it.  They compute it with the
+// hardware's approximate reciprocal, reciprocal square root and exponential: sampling
+// and pdf evaluation read the same lobes, so the one-sample MIS estimator stays
+// unbiased, and each row's mixture costs a few dozen special-function instructions
+// instead of IEEE divisions and expm1 (training keeps the accurate forms, vmfNorm).
+__device__ __forceinline__ float3 normalizeFast(float3 v) { return v * rsqrtf(dot(v, v)); }
+// kappa / (2 pi (1 - exp(-2 kappa))) for kappa in [e^-4, e^7] (kappaOf's range); the
+// cancellation in 1 - exp(-2 kappa) costs at most ~4e-6 relative at the smallest kappa
+__device__ __forceinline__ float vmfNormFast(float kappa) {
+    return __fdividef(kappa, 2.0f * kPi * (1.0f - __expf(-2.0f * kappa)));
+}
+
 // raw network outputs -> mixture (unit lobe axes, concentrations, softmax weights)
 __device__ __forceinline__ void mixtureFromRaw(const float *raw, Mixture &M) {
     float mx = -3.0e38f;
+#pragma unroll
     for (int k = 0; k < kGLobes; k++) mx = fmaxf(mx, raw[5 * k + 4]);
     float s = 0.0f;
+#pragma unroll
     for (int k = 0; k < kGLobes; k++) {
         const float3 m = mk(raw[5 * k], raw[5 * k + 1], raw[5 * k + 2]);
-        const float len = sqrtf(dot(m, m));
-        M.mu[k] = len > 1.0e-12f ? m * (1.0f / len) : mk(0.0f, 0.0f, 1.0f);
+        const float len2 = dot(m, m);
+        M.mu[k] = len2 > 1.0e-24f ? m * rsqrtf(len2) : mk(0.0f, 0.0f, 1.0f);
         M.kappa[k] = kappaOf(raw[5 * k + 3]);
         M.w[k] = __expf(raw[5 * k + 4] - mx);
         s += M.w[k];
     }
+    const float is = __fdividef(1.0f, s);
+#pragma unroll
     for (int k = 0; k < kGLobes; k++) {
-        M.w[k] /= s;
-        M.wn[k] = M.w[k] * vmfNorm(M.kappa[k]);
+        M.w[k] *= is;
+        M.wn[k] = M.w[k] * vmfNormFast(M.kappa[k]);
     }
 }
 __device__ __forceinline__ float mixturePdf(const Mixture &M, float3 w) {
@@ -108,14 +124,18 @@ __device__ __forceinline__ float mixturePdf(const Mixture &M, float3 w) {
 // stable sampling of the von Mises Fisher distribution on S^2 (and other tricks)" (2012).
 __device__ __forceinline__ float3 vmfSample(float3 mu, float kappa, float u1, float u2) {
     const float e = __expf(-2.0f * kappa);
-    const float c = 1.0f + __logf(u1 + (1.0f - u1) * e) / kappa;
+    const float c = 1.0f + __fdividef(__logf(u1 + (1.0f - u1) * e), kappa);
     const float cc = clampf(c, -1.0f, 1.0f);
     const float s = sqrtf(fmaxf(0.0f, 1.0f - cc * cc));
     float sp, cp;
     __sincosf(2.0f * kPi * u2, &sp, &cp);
-    float3 t, b;
-    onb(mu, &t, &b);
-    return normalize(t * (s * cp) + b * (s * sp) + mu * cc);
+    // the frame of onb() (Duff et al. 2017) with the approximate reciprocal: |s + mu.z| >= 1
+    const float sg = copysignf(1.0f, mu.z);
+    const float a = -__fdividef(1.0f, sg + mu.z);
+    const float cxy = mu.x * mu.y * a;
+    const float3 t = mk(1.0f + sg * mu.x * mu.x * a, sg * cxy, -sg * mu.x);
+    const float3 b = mk(cxy, sg + mu.y * mu.y * a, -mu.y);
+    return normalizeFast(t * (s * cp) + b * (s * sp) + mu * cc);
 }
 __device__ __forceinline__ float3 mixtureSample(const Mixture &M, float uLobe, float u1, float u2) {
     int k = 0;

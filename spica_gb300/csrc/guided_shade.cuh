@@ -101,9 +101,10 @@ __device__ __forceinline__ void shadeGuidedLambert(const SceneView &S, float3 ps
                                       __ldg(&E.margFunc[vOff]), r0.b, &pu, &uOff);
             const float mapPdf = pu * pv;
             if (mapPdf > 0.0f) {
+                // the hardware's sine and cosine: direction and pdf take the same values
                 float st, ct, sp, cp;
-                sincosf(vv * kPi, &st, &ct);
-                sincosf(uu * 2.0f * kPi, &sp, &cp);
+                __sincosf(vv * kPi, &st, &ct);
+                __sincosf(uu * 2.0f * kPi, &sp, &cp);
                 wi = mk(st * cp, st * sp, ct);
                 lightPdf = st == 0.0f ? 0.0f : mapPdf / (2.0f * kPi * kPi * st);
                 Li = envLookup(E, uu, vv);
