@@ -1152,7 +1152,7 @@ int spgpu_guiding_grad(spgpu_ctx *h, const float *samples, int32_t n, float *gra
         return SPGPU_EINVAL;
     }
     cudaSetDevice(h->c.device);
-    return guideGrad(h->c, *h->c.guide, samples, n, grad, loss, static_cast<cudaStream_t>(stream), false);
+    return guideGrad(h->c, *h->c.guide, samples, n, grad, loss, static_cast<cudaStream_t>(stream));
 }
 
 int spgpu_film_resolve(spgpu_ctx *h, const float *film, int32_t width, int32_t height, int32_t format,

@@ -305,8 +305,7 @@ int64_t batchPixels(const BatchState &B);
 int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg);
 int guideParams(Ctx &C, GuideState &G, float *host, int set);
 int guideForward(Ctx &C, GuideState &G, const float *feat, int n, float *out, cudaStream_t s);
-int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s,
-              bool accumulateOnly);
+int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s);
 int guideTrain(Ctx &C, GuideState &G, int steps, double *meanLoss);
 int guideRing(const GuideState &G, float *dst, int maxSamples, int *count);
 int guideRender(Ctx &C, GuideState *G, const spgpu_render_desc *d, float4 *film, int flags,

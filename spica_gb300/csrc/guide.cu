@@ -22,7 +22,7 @@
 namespace spgpu {
 
 struct GuideState {
-    float *master = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    float *master = nullptr, *m = nullptr, *v = nullptr;
     uint8_t *packFwd = nullptr, *packBwd = nullptr;
     float *biasPad = nullptr;
     float *samples = nullptr;   // training ring, 16 floats per sample: x[9], w[3], c, pad
@@ -32,6 +32,8 @@ struct GuideState {
     float *wsum = nullptr;      // batch weight sum / max
     float *batch = nullptr;
     int batchCap = 0;
+    float *partials = nullptr;  // per training CTA: its partial gradient (kGParams floats)
+    int partialRows = 0;
     int step = 0;
     spgpu_guiding_config cfg{};
     double lastLoss = 0.0;
@@ -171,10 +173,12 @@ __device__ __forceinline__ void accumBias(float *gb, int nOut, const float *dy) 
     }
 }
 
-// one M = 64 weight-gradient accumulator -> grad[offW + o * nIn + i] (atomic); every
-// thread takes part (tcgen05.ld is warp-wide), lanes 0-15 of each warp hold its rows
+// one M = 64 weight-gradient accumulator -> row[offW + o * nIn + i], the CTA's own
+// partial gradient (plain stores; the partial rows of all CTAs are summed afterwards in a
+// fixed order, k_grad_sum); every thread takes part (tcgen05.ld is warp-wide), lanes 0-15
+// of each warp hold its rows
 __device__ __forceinline__ void flushWeightGrad(uint32_t dTmem, uint32_t nCols, int offW, int nOut, int nIn,
-                                                float *grad) {
+                                                float *row) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int o = static_cast<int>(16 * warp + lane);
     for (uint32_t c = 0; c < nCols; c += 16) {
@@ -182,7 +186,7 @@ __device__ __forceinline__ void flushWeightGrad(uint32_t dTmem, uint32_t nCols, 
         tc::tmemLoad16(dTmem + ((warp * 32u) << 16) + c, v);
         if (lane < 16 && o < nOut)
             for (int i = 0; i < 16; i++)
-                if (static_cast<int>(c) + i < nIn) atomicAdd(&grad[offW + o * nIn + c + i], v[i]);
+                if (static_cast<int>(c) + i < nIn) row[offW + o * nIn + c + i] = v[i];
     }
 }
 
@@ -205,7 +209,7 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
                                                            const uint8_t *__restrict__ packBwd,
                                                            const float *__restrict__ biasPad,
                                                            const float *__restrict__ samples, int n,
-                                                           const float *__restrict__ wsum, float *grad,
+                                                           const float *__restrict__ wsum, float *partials,
                                                            double *lossAcc, int *err) {
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t *wf = sm + TrainLayout::wf, *wb = sm + TrainLayout::wb;
@@ -319,20 +323,23 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_train(const uint8_t *__rest
         if (t == 0) atomicOr(err, 1);
         return;
     }
+    float *row = partials + static_cast<int64_t>(blockIdx.x) * kGParams;
     if (acc) {
-        flushWeightGrad(tmem + kColDW4, kGHid, kOffW4, kGOut, kGHid, grad);
-        flushWeightGrad(tmem + kColDW3, kGHid, kOffW3, kGHid, kGHid, grad);
-        flushWeightGrad(tmem + kColDW2, kGHid, kOffW2, kGHid, kGHid, grad);
-        flushWeightGrad(tmem + kColDW1, kGK0, kOffW1, kGHid, kGIn, grad);
+        flushWeightGrad(tmem + kColDW4, kGHid, kOffW4, kGOut, kGHid, row);
+        flushWeightGrad(tmem + kColDW3, kGHid, kOffW3, kGHid, kGHid, row);
+        flushWeightGrad(tmem + kColDW2, kGHid, kOffW2, kGHid, kGHid, row);
+        flushWeightGrad(tmem + kColDW1, kGK0, kOffW1, kGHid, kGIn, row);
+    } else {
+        for (int i = t; i < kGParams; i += kGTile) row[i] = 0.0f;   // no tile: a zero partial
     }
     tc::fenceBeforeSync();
     __syncthreads();
     if (t < 32) tc::tmemDealloc(tmem, kTrainTmemCols);
     for (int o = t; o < kGHid; o += kGTile) {
-        atomicAdd(&grad[kOffB1 + o], gb[o]);
-        atomicAdd(&grad[kOffB2 + o], gb[kGHid + o]);
-        atomicAdd(&grad[kOffB3 + o], gb[2 * kGHid + o]);
-        if (o < kGOut) atomicAdd(&grad[kOffB4 + o], gb[3 * kGHid + o]);
+        row[kOffB1 + o] = gb[o];
+        row[kOffB2 + o] = gb[kGHid + o];
+        row[kOffB3 + o] = gb[2 * kGHid + o];
+        if (o < kGOut) row[kOffB4 + o] = gb[3 * kGHid + o];
     }
     for (int off = 16; off > 0; off >>= 1) {
         lossSum += __shfl_xor_sync(0xffffffffu, lossSum, off);
@@ -393,19 +400,38 @@ __global__ void __launch_bounds__(kGTile, 1) k_guide_forward(const uint8_t *__re
 }
 constexpr int kForwardSmem = kPackFwdBytes + kBiasPad * 4 + kGTile * kGK0 * 2 + kGTile * kGHid * 2 + kGTile * 41 * 4 + 16;
 
-// ------------------------------------------------------------------ Adam
-__global__ void k_adam(float *P, float *G, float *M, float *V, int n, float lr, float b1, float b2, float eps,
-                       float c1, float c2) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float g = G[i];
+// ------------------------------------------------------------------ gradient sum, Adam
+// The batch gradient is the sum of the training CTAs' partial rows.  Each block takes
+// kRedX parameters; its kRedY thread rows add every kRedY-th partial row, and the
+// column sums are added in row order, so the sum is the same every time.  ADAM applies
+// an Adam step (Kingma and Ba: bias-corrected moments, c1 = 1 - b1^t, c2 = 1 - b2^t) to
+// the master parameters out with it; otherwise the sum is written to out.
+constexpr int kRedX = 32, kRedY = 8;
+template <bool ADAM>
+__global__ void __launch_bounds__(kRedX *kRedY) k_grad_sum(const float *__restrict__ partials, int nParts, float *out,
+                                                           float *M, float *V, float lr, float b1, float b2, float eps,
+                                                           float c1, float c2) {
+    __shared__ float part[kRedY][kRedX];
+    const int i = blockIdx.x * kRedX + threadIdx.x;
+    float s = 0.0f;
+    if (i < kGParams)
+        for (int p = threadIdx.y; p < nParts; p += kRedY) s += partials[static_cast<int64_t>(p) * kGParams + i];
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y != 0 || i >= kGParams) return;
+    float g = 0.0f;
+    for (int y = 0; y < kRedY; y++) g += part[y][threadIdx.x];
+    if (ADAM) {
         const float m = b1 * M[i] + (1.0f - b1) * g;
         const float v = b2 * V[i] + (1.0f - b2) * g * g;
         M[i] = m;
         V[i] = v;
-        P[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
-        G[i] = 0.0f;
+        out[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+    } else {
+        out[i] = g;
     }
 }
+constexpr int kRedBlocks = (kGParams + kRedX - 1) / kRedX;
 
 // gather a random batch of n samples from the first `avail` ring entries (indices from
 // Philox keyed by (seed, step)) and sum their weights
@@ -778,7 +804,7 @@ int guideTileKernelGrid(const void *kernel, int device) {
 void freeGuide(GuideState *G) {
     if (!G) return;
     cudaFree(G->master);
-    cudaFree(G->grad);
+    cudaFree(G->partials);
     cudaFree(G->m);
     cudaFree(G->v);
     cudaFree(G->packFwd);
@@ -805,7 +831,10 @@ int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg) {
     G->batchCap = ((G->cfg.batch + kGTile - 1) / kGTile) * kGTile;
     G->rng.seed(G->cfg.seed);
     G->master = galloc<float>(kGParams);
-    G->grad = galloc<float>(kGParams);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
+    G->partialRows = std::max(sms, 1);
+    G->partials = galloc<float>(static_cast<size_t>(G->partialRows) * kGParams);
     G->m = galloc<float>(kGParams);
     G->v = galloc<float>(kGParams);
     G->packFwd = galloc<uint8_t>(kPackFwdBytes);
@@ -816,7 +845,7 @@ int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg) {
     G->lossAcc = galloc<double>(2);
     G->wsum = galloc<float>(2);
     G->batch = galloc<float>(static_cast<size_t>(G->batchCap) * 16);
-    if (!G->master || !G->grad || !G->m || !G->v || !G->packFwd || !G->packBwd || !G->biasPad || !G->samples ||
+    if (!G->master || !G->partials || !G->m || !G->v || !G->packFwd || !G->packBwd || !G->biasPad || !G->samples ||
         !G->ctl || !G->lossAcc || !G->wsum || !G->batch) {
         freeGuide(G);
         setError("spgpu_guiding_init: device allocation failed");
@@ -835,7 +864,6 @@ int guideInit(Ctx &C, GuideState **slot, const spgpu_guiding_config *cfg) {
     fill(kOffW4, kGOut, kGHid);
     for (int i = 0; i < kGOut * kGHid; i++) P[kOffW4 + i] *= 0.1f;   // start near a broad, uniform mixture
     cudaMemcpy(G->master, P.data(), sizeof(float) * kGParams, cudaMemcpyHostToDevice);
-    cudaMemset(G->grad, 0, sizeof(float) * kGParams);
     cudaMemset(G->m, 0, sizeof(float) * kGParams);
     cudaMemset(G->v, 0, sizeof(float) * kGParams);
     cudaMemset(G->ctl, 0, sizeof(int) * 4);
@@ -885,14 +913,16 @@ int guideForward(Ctx &C, GuideState &G, const float *feat, int n, float *out, cu
 }
 
 // Launch the gradient of the batch loss (sum_i c_i * -log p(w_i), c normalised by the
-// batch's weight sum in G.wsum[0]) into grad; the c-weighted loss is added to
-// G.lossAcc[0].  No host synchronisation.
-static int launchGrad(Ctx &C, GuideState &G, const float *samples, int n, float *grad, cudaStream_t s) {
+// batch's weight sum in G.wsum[0]): one partial row per training CTA in G.partials,
+// *nParts of them; the c-weighted loss is added to G.lossAcc[0].  No host
+// synchronisation.
+static int launchGrad(Ctx &C, GuideState &G, const float *samples, int n, int *nParts, cudaStream_t s) {
     const int tiles = (n + kGTile - 1) / kGTile;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, C.device);
-    k_guide_train<<<std::min(tiles, sms), kGTile, TrainLayout::total, s>>>(G.packFwd, G.packBwd, G.biasPad, samples,
-                                                                           n, G.wsum, grad, G.lossAcc, G.ctl + 1);
+    *nParts = std::min(std::min(tiles, sms), G.partialRows);
+    k_guide_train<<<*nParts, kGTile, TrainLayout::total, s>>>(G.packFwd, G.packBwd, G.biasPad, samples, n, G.wsum,
+                                                              G.partials, G.lossAcc, G.ctl + 1);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : cudaFail("guiding gradient", e);
 }
@@ -912,8 +942,7 @@ static int readLoss(GuideState &G, double *loss, cudaStream_t s, const char *wha
     return 0;
 }
 
-int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s,
-              bool accumulateOnly) {
+int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut, double *loss, cudaStream_t s) {
     if (n <= 0) {
         if (loss) *loss = 0.0;
         return 0;
@@ -922,9 +951,14 @@ int guideGrad(Ctx &C, GuideState &G, const float *samples, int n, float *gradOut
     cudaMemsetAsync(G.lossAcc, 0, 2 * sizeof(double), s);
     cudaMemsetAsync(G.ctl + 1, 0, sizeof(int), s);
     k_csum<<<64, 256, 0, s>>>(samples, n, G.wsum);
-    float *grad = gradOut ? gradOut : G.grad;
-    if (gradOut && !accumulateOnly) cudaMemsetAsync(gradOut, 0, sizeof(float) * kGParams, s);
-    const int rc = launchGrad(C, G, samples, n, grad, s);
+    int nParts = 0;
+    int rc = launchGrad(C, G, samples, n, &nParts, s);
+    if (rc == 0) {
+        k_grad_sum<false><<<kRedBlocks, dim3(kRedX, kRedY), 0, s>>>(G.partials, nParts, gradOut, nullptr, nullptr,
+                                                                    0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 1.0f);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cudaFail("guiding gradient sum", e);
+    }
     return rc ? rc : readLoss(G, loss, s, "spgpu_guiding_grad");
 }
 
@@ -961,14 +995,15 @@ int guideTrain(Ctx &C, GuideState &G, int steps, double *meanLoss) {
         cudaMemsetAsync(G.wsum, 0, 2 * sizeof(float), s);
         k_gather<<<std::min(64, (n + 255) / 256), 256, 0, s>>>(G.samples, avail, G.cfg.seed,
                                                                 static_cast<uint32_t>(G.step), n, G.batch, G.wsum);
-        int rc = launchGrad(C, G, G.batch, n, G.grad, s);
+        int nParts = 0;
+        int rc = launchGrad(C, G, G.batch, n, &nParts, s);
         if (rc) return rc;
         G.step++;
         const float b1 = 0.9f, b2 = 0.999f;
         const float c1 = 1.0f - std::pow(b1, static_cast<float>(G.step));
         const float c2 = 1.0f - std::pow(b2, static_cast<float>(G.step));
-        k_adam<<<32, 256, 0, s>>>(G.master, G.grad, G.m, G.v, kGParams, G.cfg.learning_rate, b1, b2, 1.0e-8f, c1,
-                                  c2);
+        k_grad_sum<true><<<kRedBlocks, dim3(kRedX, kRedY), 0, s>>>(G.partials, nParts, G.master, G.m, G.v,
+                                                                   G.cfg.learning_rate, b1, b2, 1.0e-8f, c1, c2);
         rc = packWeights(G, s);
         if (rc) return rc;
     }

@@ -20,7 +20,7 @@ batch   the first N seeded box-room variants as one batch: with --engine stream 
         k_sadvance, their batch forms; --no-graph skips the graph run); with --engine
         persistent the megakernel (k_batch)
 guided  the guiding room at 640 x 360: 8 collection passes of 2 spp with 32 Adam steps
-        each (k_collect, k_gather, k_guide_train, k_adam), then one plain and one guided
+        each (k_collect, k_gather, k_guide_train, k_grad_sum), then one plain and one guided
         render of 8 spp inside the NVTX range "profiled" (k_sshade_guided on the streaming
         wavefront; k_shade_guided with --wavefront 1, pass by pass), then one network
         evaluation of 65,536 inputs (k_guide_forward)

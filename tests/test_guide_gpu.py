@@ -85,10 +85,11 @@ def test_adam_steps_match_oracle(gpulib):
         p_next = p - lr * (m / (1 - 0.9 ** (step + 1))) / (np.sqrt(vhat) + 1e-8)
         g.train(1)
         got = g.params().astype(np.float64)
-        # Where sqrt(v_hat) is well above eps, the update is the same up to float32
-        # rounding and the order of the device's gradient sums (atomic adds): within 1 % of
-        # a step (lr).  Parameters whose gradients are at the level of that summation noise
-        # (dead units, cancelling terms) still move by at most one step.
+        # The training step sums the same per-CTA partial gradients in the same order as
+        # the gradient entry point, so where sqrt(v_hat) is well above eps the update is
+        # the same up to float32 rounding: within 1 % of a step (lr).  Parameters whose
+        # gradients sit at the level of float32 rounding (dead units, cancelling terms)
+        # still move by at most one step.
         firm = np.sqrt(vhat) > 1e-5
         assert firm.mean() > 0.5
         err = np.abs(got - p_next)
