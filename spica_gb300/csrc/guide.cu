@@ -80,36 +80,46 @@ __global__ void k_guide_pack(const float *__restrict__ P, uint8_t *fwd, uint8_t 
 }
 
 // ------------------------------------------------------------------ loss
-// -c * log p(w) of the mixture for raw outputs r; writes dLoss/draw into g, returns loss
+// -c * log p(w) of the mixture for raw outputs r; writes dLoss/draw into g, returns loss.
+// Reciprocals, square roots and exponentials are the hardware's approximations (relative
+// errors of a few 1e-6 at the smallest concentration, e^-4, far inside the gradient's
+// tolerance); the loss the step reports uses the same values.
 __device__ __forceinline__ float mixtureLossGrad(const float *r, float3 w, float c, float *g) {
     float mx = -3.0e38f;
+#pragma unroll
     for (int k = 0; k < kGLobes; k++) mx = fmaxf(mx, r[5 * k + 4]);
     float wk[kGLobes], vk[kGLobes], s = 0.0f;
     float3 mu[kGLobes];
-    float len[kGLobes], kap[kGLobes];
+    float ilen[kGLobes], kap[kGLobes];
+#pragma unroll
     for (int k = 0; k < kGLobes; k++) {
         const float3 m = mk(r[5 * k], r[5 * k + 1], r[5 * k + 2]);
-        len[k] = fmaxf(sqrtf(dot(m, m)), 1.0e-6f);
-        mu[k] = m * (1.0f / len[k]);
+        ilen[k] = rsqrtf(fmaxf(dot(m, m), 1.0e-12f));   // 1 / max(|m|, 1e-6)
+        mu[k] = m * ilen[k];
         kap[k] = kappaOf(r[5 * k + 3]);
-        vk[k] = vmfPdf(w, mu[k], kap[k]);
+        vk[k] = vmfNormFast(kap[k]) * __expf(kap[k] * (dot(mu[k], w) - 1.0f));
         wk[k] = __expf(r[5 * k + 4] - mx);
         s += wk[k];
     }
+    const float is = __fdividef(1.0f, s);
     float p = 0.0f;
+#pragma unroll
     for (int k = 0; k < kGLobes; k++) {
-        wk[k] /= s;
+        wk[k] *= is;
         p += wk[k] * vk[k];
     }
     p = fmaxf(p, 1.0e-30f);
-    const float a = -c / p;
+    const float a = -__fdividef(c, p);
+#pragma unroll
     for (int k = 0; k < kGLobes; k++) {
         const float dv = a * wk[k];   // dLoss / dv_k
         const float kr = r[5 * k + 3];
-        const float dlogv_dk = 1.0f / kap[k] - 2.0f / expm1f(2.0f * kap[k]) + (dot(mu[k], w) - 1.0f);
+        // d log v / d kappa = 1 / kappa - 2 / (e^(2 kappa) - 1) + (mu.w - 1)
+        const float dlogv_dk = __fdividef(1.0f, kap[k]) - __fdividef(2.0f, __expf(2.0f * kap[k]) - 1.0f) +
+                               (dot(mu[k], w) - 1.0f);
         g[5 * k + 3] = (kr > -4.0f && kr < 7.0f) ? dv * vk[k] * dlogv_dk * kap[k] : 0.0f;
         const float3 gmu = w * (dv * vk[k] * kap[k]);
-        const float3 gm = (gmu - mu[k] * dot(mu[k], gmu)) * (1.0f / len[k]);
+        const float3 gm = (gmu - mu[k] * dot(mu[k], gmu)) * ilen[k];
         g[5 * k] = gm.x;
         g[5 * k + 1] = gm.y;
         g[5 * k + 2] = gm.z;
@@ -190,16 +200,26 @@ __device__ __forceinline__ void flushWeightGrad(uint32_t dTmem, uint32_t nCols, 
     }
 }
 
-// backward epilogue: g = acc * relu'(h) -> dy (fp32) and dyb (bf16, K = 64)
+// backward epilogue: g = acc * relu'(h) -> dy (fp32) and dyb (bf16, K = 64); the row's
+// activations come 8 at a time (one core-matrix row, 16 bytes)
 __device__ __forceinline__ void backEpilogue(uint32_t tmem, const uint8_t *h, float *dy, uint8_t *dyb) {
     const uint32_t r = threadIdx.x;
     for (uint32_t c = 0; c < kGHid; c += 16) {
         float v[16];
         accRow16(tmem, c, v);
-        for (int i = 0; i < 16; i++) {
-            v[i] = loadBf16(h, r, c + i, kGHid) > 0.0f ? v[i] : 0.0f;
-            dy[r * kTrainStride + c + i] = v[i];
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            const uint4 q = *reinterpret_cast<const uint4 *>(h + tc::kmajorOffset(r, c + 8 * half, kGHid));
+            const __nv_bfloat162 *hb = reinterpret_cast<const __nv_bfloat162 *>(&q);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 hv = __bfloat1622float2(hb[j]);
+                float &a0 = v[8 * half + 2 * j], &a1 = v[8 * half + 2 * j + 1];
+                a0 = hv.x > 0.0f ? a0 : 0.0f;
+                a1 = hv.y > 0.0f ? a1 : 0.0f;
+            }
         }
+        for (int i = 0; i < 16; i++) dy[r * kTrainStride + c + i] = v[i];
         storeRow8(dyb, r, c, kGHid, v);
         storeRow8(dyb, r, c + 8, kGHid, v + 8);
     }
