@@ -5,6 +5,7 @@ case), separate from the benchmark:
     python -m spica_gb300.profcases micro [--rays N]
     python -m spica_gb300.profcases batch [--renders N] [--engine stream|persistent] [--no-graph]
     python -m spica_gb300.profcases guided [--wavefront 0|1]
+    python -m spica_gb300.profcases train
     python -m spica_gb300.profcases build [--levels L]
     python -m spica_gb300.profcases film [--width W] [--height H]
 
@@ -24,6 +25,9 @@ guided  the guiding room at 640 x 360: 8 collection passes of 2 spp with 32 Adam
         render of 8 spp inside the NVTX range "profiled" (k_sshade_guided on the streaming
         wavefront; k_shade_guided with --wavefront 1, pass by pass), then one network
         evaluation of 65,536 inputs (k_guide_forward)
+train   the guiding room at 1280 x 720: 8 collection passes of 2 spp, 16 + 64 Adam steps
+        of 16,384 samples (host-timed), then 20 steps inside the NVTX range "profiled"
+        (k_gather, k_guide_train, k_grad_sum, k_guide_pack)
 build   the device BVH build of the mid-scale scene, or of the microbench sphere with
         --levels (Morton keys, clustering rounds, SAH programme, collapse)
 film    a rendered box room at W x H resolved by every film format (RGBE, gamma,
@@ -126,6 +130,33 @@ def _guided(args, torch):
             "guided_ms": sg.ms}
 
 
+def _train(args, torch):
+    import time
+
+    from . import GpuBVHAccel, scenes
+    from .gpu import GUIDE_COLLECT, GUIDE_GUIDED, GpuGuide
+    W, H = 1280, 720
+    sc = scenes.guiding_room(width=W, height=H)
+    acc = GpuBVHAccel(sc).construct()
+    g = GpuGuide(acc, seed=2)
+    p = {"width": W, "height": H, "maxDepth": sc.max_depth}
+    f = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    for k in range(8):
+        g.render(sc.camera, dict(p, sampleCount=2), f, GUIDE_GUIDED | GUIDE_COLLECT, seed=1, sample_offset=2 * k)
+    g.train(16)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.train(64)
+    torch.cuda.synchronize()
+    step_ms = (time.perf_counter() - t0) * 1e3 / 64
+    torch.cuda.nvtx.range_push("profiled")
+    g.train(20)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    return {"case": "train", "width": W, "height": H, "ring": int(g.samples()), "batch": 16384,
+            "ms_per_step_host": step_ms}
+
+
 def _build(args, torch):
     from . import GpuBVHAccel, scenes
     sc = scenes.displaced_sphere(levels=args.levels, seed=0) if args.levels else scenes.mid_scale()
@@ -154,7 +185,7 @@ def _film(args, torch):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m spica_gb300.profcases")
-    ap.add_argument("case", choices=["render", "micro", "batch", "guided", "build", "film"])
+    ap.add_argument("case", choices=["render", "micro", "batch", "guided", "train", "build", "film"])
     ap.add_argument("--width", type=int, default=960)
     ap.add_argument("--height", type=int, default=540)
     ap.add_argument("--spp", type=int, default=1)
@@ -168,7 +199,8 @@ def main(argv=None):
     args = ap.parse_args(argv)
     import torch
     torch.cuda.set_device(0)
-    fn = {"render": _render, "micro": _micro, "batch": _batch, "guided": _guided, "build": _build, "film": _film}
+    fn = {"render": _render, "micro": _micro, "batch": _batch, "guided": _guided, "train": _train, "build": _build,
+          "film": _film}
     print(json.dumps(fn[args.case](args, torch)), flush=True)
     return 0
 
