@@ -295,8 +295,11 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
 // runs through the four layers on the tensor cores (tcgen05, accumulator in TMEM), and
 // each entry is shaded with its mixture straight from registers (shadeGuidedLambert, the
 // megakernel's shading).  Several CTAs per SM: one's MMA waits overlap another's shading.
+#ifndef SPGPU_GUIDED_PASS_MIN_BLOCKS
+#define SPGPU_GUIDED_PASS_MIN_BLOCKS 3
+#endif
 template <bool COLLECT>
-__global__ void __launch_bounds__(kGTile) k_shade_guided(PassArgs p, int b) {
+__global__ void __launch_bounds__(kGTile, SPGPU_GUIDED_PASS_MIN_BLOCKS) k_shade_guided(PassArgs p, int b) {
     const int *cnt = p.counters + b * kCountersPerBounce;
     const int n = cnt[1 + kMatLambert];
     if (static_cast<int>(blockIdx.x) * kGTile >= n) return;   // no tile for this CTA
