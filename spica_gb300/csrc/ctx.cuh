@@ -264,7 +264,7 @@ struct GuideView {
 // guide.cu: grid of a persistent kernel that runs the network per 128-thread CTA
 // (kTileSmem bytes of dynamic shared memory, 64 TMEM columns): SMs x CTAs that fit one
 // SM; sets the kernel's shared-memory carveout (call before stream capture)
-int guideTileKernelGrid(const void *kernel, int device);
+int guideTileKernelGrid(const void *kernel, int device, int dynSmem = 0);
 
 // wavefront.cu: trace desc->spp samples per pixel into film (device, float4 per pixel);
 // with gv, diffuse hits sample the learned guiding proposal (path integrator only)

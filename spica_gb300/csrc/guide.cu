@@ -813,12 +813,14 @@ int packWeights(GuideState &G, cudaStream_t s) {
 
 }  // namespace
 
-int guideTileKernelGrid(const void *kernel, int device) {
+int guideTileKernelGrid(const void *kernel, int device, int dynSmem) {
+    if (dynSmem <= 0) dynSmem = kTileSmem;
     cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (dynSmem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dynSmem);
     cudaGetLastError();
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    return sms * tmemKernelResidentCtas(kernel, device, kTileSmem);
+    return sms * tmemKernelResidentCtas(kernel, device, dynSmem);
 }
 
 void freeGuide(GuideState *G) {

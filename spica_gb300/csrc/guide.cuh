@@ -260,9 +260,9 @@ __device__ __forceinline__ bool mlpForwardTile(uint32_t tmem, const uint8_t *wf,
 // copy each (TMA), the MMA mbarrier, a 64-column TMEM allocation (warp 0); returns the
 // TMEM base, and in *ok whether the copies arrived
 __device__ __forceinline__ uint32_t tileKernelSetup(uint8_t *sm, const uint8_t *packFwd, const float *biasPad,
-                                                    bool *ok) {
+                                                    bool *ok, int barOff = kTileSmOffBar) {
     const int t = threadIdx.x;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + barOff);
     uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
     uint64_t *loadBar = bar + 2;
     if (t == 0) {
@@ -284,8 +284,9 @@ __device__ __forceinline__ uint32_t tileKernelSetup(uint8_t *sm, const uint8_t *
 }
 // its epilogue: after a failed (timed-out) wait, bounded waits for the copies and MMAs
 // still in flight; then the TMEM allocation is released
-__device__ __forceinline__ void tileKernelTeardown(uint8_t *sm, uint32_t tmem, bool ok, uint32_t phase) {
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+__device__ __forceinline__ void tileKernelTeardown(uint8_t *sm, uint32_t tmem, bool ok, uint32_t phase,
+                                                   int barOff = kTileSmOffBar) {
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + barOff);
     if (!ok) {
         tc::mbarWait(bar + 2, 0, kMmaWaitTries);
         tc::mbarWait(bar, phase ^ 1u, kMmaWaitTries);

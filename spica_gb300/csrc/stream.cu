@@ -52,7 +52,7 @@ constexpr int kTraceMinBlocks = SPGPU_TRACE_MIN_BLOCKS;   // resident traversal 
 #endif
 constexpr int kShadeMinBlocks = SPGPU_SHADE_MIN_BLOCKS;   // resident shading blocks per SM (register budget)
 #ifndef SPGPU_GUIDED_MIN_BLOCKS
-#define SPGPU_GUIDED_MIN_BLOCKS 3
+#define SPGPU_GUIDED_MIN_BLOCKS 4
 #endif
 constexpr int kGuidedMinBlocks = SPGPU_GUIDED_MIN_BLOCKS;   // resident guided shading blocks per SM
 #ifndef SPGPU_ITER_PER_GRAPH
@@ -366,10 +366,27 @@ __global__ void __launch_bounds__(kShadeBlockS, kShadeMinBlocks) k_sshade(Stream
     }
 }
 
+// Shared memory of k_sshade_guided: packed forward weights | biases | mbarriers and TMEM
+// slot | the input/hidden tile of the network, which once the network is done holds the
+// tile's mixtures instead, one row per thread padded to an odd number of words (so the
+// rows of a warp fall into distinct banks).  Keeping the 48-float mixture out of
+// registers through the shading lets four CTAs share an SM.
+struct MixRow {
+    Mixture m;
+    float pad;
+};
+static_assert(sizeof(MixRow) % 8 == 4, "odd word stride");
+constexpr int kGsOffBar = kTileSmOffBias + 1024;
+constexpr int kGsOffXH = kGsOffBar + 128;
+constexpr int kGsSmem = kGsOffXH + (kGTile * kGHid * 2 > kGTile * static_cast<int>(sizeof(MixRow))
+                                        ? kGTile * kGHid * 2
+                                        : kGTile * static_cast<int>(sizeof(MixRow)));
+static_assert(kGsOffXH % 128 == 0 && kGsOffBar % 8 == 0, "alignment");
+
 // Lambert hits of a guided render.  Each CTA takes 128-row tiles of the Lambert queue:
 // every thread forms its row's network inputs, the tile runs through the four layers on
 // the tensor cores (tcgen05, accumulator in TMEM), and each row is shaded with its
-// mixture straight from registers (shadeGuidedLambert).  Rows at the last depth, or past
+// mixture (shadeGuidedLambert), kept in shared memory.  Rows at the last depth, or past
 // the guided depths, are shaded with plain BSDF sampling as in k_sshade.  The queue
 // mixes depths, so one launch covers what the pass-by-pass wavefront does in one guided
 // launch per bounce.
@@ -379,10 +396,11 @@ __global__ void __launch_bounds__(kGTile, kGuidedMinBlocks) k_sshade_guided(Stre
     extern __shared__ __align__(128) uint8_t sm[];
     const int64_t base = static_cast<int64_t>(kMatLambert) * p.cap;
     bool ok = true;
-    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad, &ok);
+    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad, &ok, kGsOffBar);
     const float *bias = reinterpret_cast<const float *>(sm + kTileSmOffBias);
-    uint8_t *xh = sm + kTileSmOffXH;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+    uint8_t *xh = sm + kGsOffXH;
+    MixRow &mix = reinterpret_cast<MixRow *>(sm + kGsOffXH)[threadIdx.x];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kGsOffBar);
     uint32_t phase = 0;
     for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
         const int j = tile * kGTile + static_cast<int>(threadIdx.x);
@@ -400,10 +418,15 @@ __global__ void __launch_bounds__(kGTile, kGuidedMinBlocks) k_sshade_guided(Stre
             nn = triNormal(p.sv.tris[__float_as_int(h4.y)]);
             guideFeatures(ps, nn, -xyz(d4), p.guideLo, p.guideInvExt, xf);
         }
+        __syncthreads();   // every row of the last tile is shaded: its mixtures may go
         storeRow8(xh, threadIdx.x, 0, kGK0, xf);
         storeRow8(xh, threadIdx.x, 8, kGK0, xf + 8);
-        float raw[kGOut];
-        ok = mlpForwardRow(tmem, sm, bias, xh, bar, phase, raw);   // CTA-uniform
+        {
+            float raw[kGOut];
+            ok = mlpForwardRow(tmem, sm, bias, xh, bar, phase, raw);   // CTA-uniform
+            // the last layer's MMA has read the tile, so each row's mixture may take its place
+            if (ok) mixtureFromRaw(raw, mix.m);
+        }
         if (!ok) break;
         ShadeResult R;
         R.cont = R.sh0 = R.sh1 = false;
@@ -414,11 +437,9 @@ __global__ void __launch_bounds__(kGTile, kGuidedMinBlocks) k_sshade_guided(Stre
             const bool spec = (meta & 256) != 0;
             if (depth < p.maxDepth && (p.guidedBounces <= 0 || depth < p.guidedBounces)) {
                 const int2 sh = __ldg(&p.sv.slotShade[__float_as_int(h4.y)]);
-                Mixture M;
-                mixtureFromRaw(raw, M);
                 float3 fc;
                 float pdf;
-                shadeGuidedLambert(p.sv, ps, nn, p.sv.mats[sh.x], sh.y, xyz(d4), xyz(b4), spec, depth, M,
+                shadeGuidedLambert(p.sv, ps, nn, p.sv.mats[sh.x], sh.y, xyz(d4), xyz(b4), spec, depth, mix.m,
                                    p.guideAlpha, p.seed, static_cast<uint32_t>(fi), static_cast<uint32_t>(sample), R,
                                    &fc, &pdf);
             } else {
@@ -428,7 +449,7 @@ __global__ void __launch_bounds__(kGTile, kGuidedMinBlocks) k_sshade_guided(Stre
         }
         emitShadeResultS(p, R, live, live ? filmIndexS(p, pix) : 0, pix, meta, sample);
     }
-    tileKernelTeardown(sm, tmem, ok, phase);
+    tileKernelTeardown(sm, tmem, ok, phase, kGsOffBar);
     if (!ok && threadIdx.x == 0) atomicOr(&p.ctr[kCtrErr], 2);
 }
 
@@ -522,7 +543,7 @@ GridsS streamGrids(int device, int cap, bool guided) {
     g.trace = sms * std::max(occT, 1);
     g.shade = sms * std::max(occS, 1);
     g.regen = std::max(1, std::min((cap + 255) / 256, sms * 8));
-    g.guided = guided ? guideTileKernelGrid(reinterpret_cast<const void *>(k_sshade_guided), device) : 0;
+    g.guided = guided ? guideTileKernelGrid(reinterpret_cast<const void *>(k_sshade_guided), device, kGsSmem) : 0;
     return g;
 }
 
@@ -546,7 +567,7 @@ void launchIteration(const StreamArgs &a, const GridsS &g, cudaStream_t s, cudaE
     k_sextend<STATS, BATCH><<<g.trace, kTraceBlock, 0, s>>>(a);
     done();
     mark(kSShadeL);
-    if (a.packFwd) k_sshade_guided<<<g.guided, kGTile, kTileSmem, s>>>(a);
+    if (a.packFwd) k_sshade_guided<<<g.guided, kGTile, kGsSmem, s>>>(a);
     else k_sshade<kMatLambert, BATCH><<<g.shade, kShadeBlockS, 0, s>>>(a);
     done();
     mark(kSShadeC);
