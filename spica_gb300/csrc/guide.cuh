@@ -296,6 +296,23 @@ __device__ __forceinline__ void tileKernelTeardown(uint8_t *sm, uint32_t tmem, b
     if (threadIdx.x < 32) tc::tmemDealloc(tmem, 64);
 }
 
+// Shared memory of the guided shading kernels: packed forward weights | biases |
+// mbarriers and TMEM slot | the input/hidden tile of the network, which once the network
+// is done holds the tile's mixtures instead, one row per thread padded to an odd number
+// of words (so the rows of a warp fall into distinct banks).  Keeping the 48-float
+// mixture out of registers through the shading lets four CTAs share an SM.
+struct MixRow {
+    Mixture m;
+    float pad;
+};
+static_assert(sizeof(MixRow) % 8 == 4, "odd word stride");
+constexpr int kGsOffBar = kTileSmOffBias + 1024;
+constexpr int kGsOffXH = kGsOffBar + 128;
+constexpr int kGsSmem = kGsOffXH + (kGTile * kGHid * 2 > kGTile * static_cast<int>(sizeof(MixRow))
+                                        ? kGTile * kGHid * 2
+                                        : kGTile * static_cast<int>(sizeof(MixRow)));
+static_assert(kGsOffXH % 128 == 0 && kGsOffBar % 8 == 0, "alignment");
+
 // Forward of one tile with the outputs left in registers: thread r receives row r's 40
 // raw outputs.  xh holds the bf16 input tile [128][16] on entry and is reused for the
 // hidden activations (each layer's epilogue runs after the MMA that read it completed).

@@ -366,23 +366,6 @@ __global__ void __launch_bounds__(kShadeBlockS, kShadeMinBlocks) k_sshade(Stream
     }
 }
 
-// Shared memory of k_sshade_guided: packed forward weights | biases | mbarriers and TMEM
-// slot | the input/hidden tile of the network, which once the network is done holds the
-// tile's mixtures instead, one row per thread padded to an odd number of words (so the
-// rows of a warp fall into distinct banks).  Keeping the 48-float mixture out of
-// registers through the shading lets four CTAs share an SM.
-struct MixRow {
-    Mixture m;
-    float pad;
-};
-static_assert(sizeof(MixRow) % 8 == 4, "odd word stride");
-constexpr int kGsOffBar = kTileSmOffBias + 1024;
-constexpr int kGsOffXH = kGsOffBar + 128;
-constexpr int kGsSmem = kGsOffXH + (kGTile * kGHid * 2 > kGTile * static_cast<int>(sizeof(MixRow))
-                                        ? kGTile * kGHid * 2
-                                        : kGTile * static_cast<int>(sizeof(MixRow)));
-static_assert(kGsOffXH % 128 == 0 && kGsOffBar % 8 == 0, "alignment");
-
 // Lambert hits of a guided render.  Each CTA takes 128-row tiles of the Lambert queue:
 // every thread forms its row's network inputs, the tile runs through the four layers on
 // the tensor cores (tcgen05, accumulator in TMEM), and each row is shaded with its

@@ -293,10 +293,11 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(PassArgs p, int b) {
 // Diffuse hits of a guided pass, bounces before the last.  Each CTA takes 128-entry
 // tiles of the diffuse queue: every thread forms its entry's network inputs, the tile
 // runs through the four layers on the tensor cores (tcgen05, accumulator in TMEM), and
-// each entry is shaded with its mixture straight from registers (shadeGuidedLambert, the
-// megakernel's shading).  Several CTAs per SM: one's MMA waits overlap another's shading.
+// each entry is shaded with its mixture (shadeGuidedLambert, the megakernel's shading),
+// kept in shared memory in place of the finished input tile (kGsSmem layout).  Several
+// CTAs per SM: one's MMA waits overlap another's shading.
 #ifndef SPGPU_GUIDED_PASS_MIN_BLOCKS
-#define SPGPU_GUIDED_PASS_MIN_BLOCKS 3
+#define SPGPU_GUIDED_PASS_MIN_BLOCKS 4
 #endif
 template <bool COLLECT>
 __global__ void __launch_bounds__(kGTile, SPGPU_GUIDED_PASS_MIN_BLOCKS) k_shade_guided(PassArgs p, int b) {
@@ -312,10 +313,11 @@ __global__ void __launch_bounds__(kGTile, SPGPU_GUIDED_PASS_MIN_BLOCKS) k_shade_
     float4 *nD = (b & 1) ? p.rayD0 : p.rayD1;
     const uint32_t sample = static_cast<uint32_t>(p.ctl[0]);
     bool ok = true;
-    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad, &ok);
+    const uint32_t tmem = tileKernelSetup(sm, p.packFwd, p.biasPad, &ok, kGsOffBar);
     const float *bias = reinterpret_cast<const float *>(sm + kTileSmOffBias);
-    uint8_t *xh = sm + kTileSmOffXH;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileSmOffBar);
+    uint8_t *xh = sm + kGsOffXH;
+    MixRow &mix = reinterpret_cast<MixRow *>(sm + kGsOffXH)[threadIdx.x];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kGsOffBar);
     uint32_t phase = 0;
     for (int tile = blockIdx.x; ok && tile * kGTile < n; tile += gridDim.x) {
         const int j = tile * kGTile + static_cast<int>(threadIdx.x);
@@ -336,10 +338,15 @@ __global__ void __launch_bounds__(kGTile, SPGPU_GUIDED_PASS_MIN_BLOCKS) k_shade_
             nn = triNormal(p.sv.tris[h.prim]);
             guideFeatures(ps, nn, -xyz(d4), p.guideLo, p.guideInvExt, xf);
         }
+        __syncthreads();   // every entry of the last tile is shaded: its mixtures may go
         storeRow8(xh, threadIdx.x, 0, kGK0, xf);
         storeRow8(xh, threadIdx.x, 8, kGK0, xf + 8);
-        float raw[kGOut];
-        ok = mlpForwardRow(tmem, sm, bias, xh, bar, phase, raw);   // CTA-uniform
+        {
+            float raw[kGOut];
+            ok = mlpForwardRow(tmem, sm, bias, xh, bar, phase, raw);   // CTA-uniform
+            // the last layer's MMA has read the tile, so each row's mixture may take its place
+            if (ok) mixtureFromRaw(raw, mix.m);
+        }
         if (!ok) break;
         ShadeResult R;
         R.cont = R.sh0 = R.sh1 = false;
@@ -349,11 +356,9 @@ __global__ void __launch_bounds__(kGTile, SPGPU_GUIDED_PASS_MIN_BLOCKS) k_shade_
             const float4 bt = p.beta[pid];
             const int fi = filmIndex(p, pid);
             const int2 sh = __ldg(&p.sv.slotShade[h.prim]);
-            Mixture M;
-            mixtureFromRaw(raw, M);
             float3 fc;
             float pdf;
-            shadeGuidedLambert(p.sv, ps, nn, p.sv.mats[sh.x], sh.y, xyz(d4), xyz(bt), bt.w != 0.0f, b, M,
+            shadeGuidedLambert(p.sv, ps, nn, p.sv.mats[sh.x], sh.y, xyz(d4), xyz(bt), bt.w != 0.0f, b, mix.m,
                                p.guideAlpha, p.seed, static_cast<uint32_t>(fi), sample, R, &fc, &pdf);
             if (!isBlack(R.emit)) gather<COLLECT>(p, pid, fi, R.emit);
             if (COLLECT) {
@@ -372,7 +377,7 @@ __global__ void __launch_bounds__(kGTile, SPGPU_GUIDED_PASS_MIN_BLOCKS) k_shade_
         }
         appendShadeResult(p, R, pid, nextCnt, shCnt, nO, nD);
     }
-    tileKernelTeardown(sm, tmem, ok, phase);
+    tileKernelTeardown(sm, tmem, ok, phase, kGsOffBar);
     if (!ok && threadIdx.x == 0) atomicOr(p.err, 2);
 }
 
@@ -535,8 +540,8 @@ void launchPass(const PassArgs &a, const Grids &g, cudaStream_t cs, size_t ctrBy
         done();
         mark(kShadeL);
         if (a.packFwd && b < a.maxDepth && (a.guidedBounces <= 0 || b < a.guidedBounces)) {
-            if (a.collect) k_shade_guided<true><<<g.guided, kGTile, kTileSmem, cs>>>(a, b);
-            else k_shade_guided<false><<<g.guided, kGTile, kTileSmem, cs>>>(a, b);
+            if (a.collect) k_shade_guided<true><<<g.guided, kGTile, kGsSmem, cs>>>(a, b);
+            else k_shade_guided<false><<<g.guided, kGTile, kGsSmem, cs>>>(a, b);
         } else {
             k_shade<kMatLambert><<<g.shade, kShadeBlock, 0, cs>>>(a, b);
         }
@@ -677,7 +682,7 @@ int ensurePassGraph(Ctx &C, RenderQueues &q, const PassArgs &a, int W, int H, in
     if (a.packFwd)   // attributes and grid before the capture
         gr.guided = guideTileKernelGrid(a.collect ? reinterpret_cast<const void *>(k_shade_guided<true>)
                                                   : reinterpret_cast<const void *>(k_shade_guided<false>),
-                                        C.device);
+                                        C.device, kGsSmem);
     const size_t ctrBytes = sizeof(int) * (q.maxDepth + 2) * kCountersPerBounce;
     cudaStream_t cs = C.stream;
     cudaGraph_t g = nullptr;
