@@ -260,25 +260,28 @@ def test_guided_wavefront_matches_guided_megakernel(gpulib):
     np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=2e-3, atol=2e-3)
 
 
-def test_streaming_guided_matches_pass_by_pass(gpulib):
+@pytest.mark.parametrize("guided_bounces", [0, 2])
+def test_streaming_guided_matches_pass_by_pass(gpulib, guided_bounces):
     """Guided passes on the streaming wavefront (the default: one guided shading launch
     per iteration over a Lambert queue that mixes depths) and on the pass-by-pass
     wavefront (one guided launch per bounce) draw the same numbers for every (pixel,
     sample, depth) and give the network the same inputs, so with the same weights the
-    films agree up to the order of the film's atomic additions; likewise plain passes."""
+    films agree up to the order of the film's atomic additions; likewise plain passes.
+    With guided_bounces = 2 the deeper rows of the streaming queue take plain BSDF
+    sampling inside the guided kernel, as the pass-by-pass wavefront's later bounces do."""
     import torch
     from spica_gb300 import Context
     sc = _room(40)
     W, H = 96, 56
     p = {"width": W, "height": H, "maxDepth": sc.max_depth}
     acc = GpuBVHAccel(sc).construct()
-    g = GpuGuide(acc, seed=5)
+    g = GpuGuide(acc, seed=5, guided_bounces=guided_bounces)
     scratch = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
     for k in range(6):
         g.render(sc.camera, dict(p, sampleCount=4), scratch, GUIDE_GUIDED | GUIDE_COLLECT, seed=70, sample_offset=4 * k)
         g.train(16)
     acc1 = GpuBVHAccel(sc, ctx=Context(0, wavefront=1)).construct()
-    g1 = GpuGuide(acc1, seed=5)
+    g1 = GpuGuide(acc1, seed=5, guided_bounces=guided_bounces)
     g1.set_params(g.params())
     for flags in (GUIDE_GUIDED, 0):
         films = []
