@@ -117,3 +117,29 @@ def test_batch_profile_matches_run(gpulib):
     bp = GpuBatch(vs, seed=3, autotune=BATCH_PERSISTENT)
     with pytest.raises(SpgpuError):
         bp.profile(films)
+
+
+@pytest.mark.parametrize("autotune", [0, BATCH_PERSISTENT])
+def test_batch_edge_shapes(gpulib, autotune):
+    """A batch of one render, and a batch whose renders differ in maximum depth (0, 1, 3
+    and 8) and take 1 to 3 samples per pixel: each film equals the same scene rendered
+    alone."""
+    import torch
+    for vs in ([small_variants(1, seed=2)[0]], small_variants(4, seed=6)):
+        for k, v in enumerate(vs):
+            v.max_depth = [8, 0, 1, 3][k % 4]
+            v.spp = 1 + k % 3
+        b = GpuBatch(vs, seed=17, autotune=autotune)
+        films = torch.zeros((b.pixels, 4), dtype=torch.float32, device="cuda")
+        ms, st = b.run(films)
+        torch.cuda.synchronize()
+        host = films.cpu().numpy()
+        assert st.paths == sum(v.width * v.height * v.spp for v in vs)
+        assert np.all(ms > 0)
+        for i, v in enumerate(vs):
+            acc = GpuBVHAccel(v).construct()
+            ref = GpuPathIntegrator(seed=17).render(v.camera, acc, {"width": v.width, "height": v.height,
+                                                                    "maxDepth": v.max_depth, "sampleCount": v.spp})
+            got = b.film(host, i)
+            assert np.array_equal(got[..., 3], ref[..., 3])
+            np.testing.assert_allclose(got[..., :3], ref[..., :3], rtol=2e-4, atol=2e-4)
