@@ -254,6 +254,12 @@ __device__ __forceinline__ bool traceWide(const WideNode *__restrict__ nodes, co
 #define SPGPU_REFILL 8
 #endif
 constexpr int kRefill = SPGPU_REFILL;
+// a finished ray's result waits for the warp's next refill, so that the finished lanes
+// consume their results together (done() runs on up to 32 lanes instead of one or two)
+#ifndef SPGPU_DEFER_DONE
+#define SPGPU_DEFER_DONE 1
+#endif
+constexpr bool kDeferDone = SPGPU_DEFER_DONE != 0;
 
 template <bool ANY, bool STATS, class Fetch, class Done>
 __device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nodes,
@@ -263,18 +269,28 @@ __device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nod
                                                 bool *overflow, Fetch fetch, Done done) {
     uint2 spill[kStackDepth - kStackShared];
     TraceLane L;
-    int ray = -1;          // >= 0 in flight, -1 idle, -2 no work left
-    bool finished = false;   // ray finished in the last step, result not yet consumed
+    int ray = -1;            // >= 0 in flight (or finished), -1 idle, -2 no work left
+    bool finished = false;   // the ray has finished, its result not yet consumed
     const int lane = threadIdx.x & 31;
     while (true) {
-        done(finished ? ray : -1, L);
-        if (finished) {
-            ray = -1;
-            finished = false;
+        if (!kDeferDone) {
+            done(finished ? ray : -1, L);
+            if (finished) {
+                ray = -1;
+                finished = false;
+            }
         }
-        const unsigned idle = __ballot_sync(0xffffffffu, ray == -1);
-        const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0);
+        const unsigned idle = __ballot_sync(0xffffffffu, ray == -1 || finished);
+        const unsigned busy = __ballot_sync(0xffffffffu, ray >= 0 && !finished);
         if (idle && (__popc(idle) >= kRefill || busy == 0)) {
+            if (kDeferDone) {
+                // the results of the rays finished since the last refill, consumed together
+                done(finished ? ray : -1, L);
+                if (finished) {
+                    ray = -1;
+                    finished = false;
+                }
+            }
             int base = 0;
             if (lane == __ffs(idle) - 1) base = atomicAdd(rayCounter, __popc(idle));
             base = __shfl_sync(0xffffffffu, base, __ffs(idle) - 1);
@@ -296,7 +312,7 @@ __device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nod
             }
         }
         if (__all_sync(0xffffffffu, ray == -2)) break;
-        if (ray >= 0) {
+        if (ray >= 0 && !finished) {
             finished = laneStep<ANY, STATS>(L, nodes, tris, nNodes, nTris, stack, stride, spill, nodeCount,
                                             triCount, overflow);
         }
