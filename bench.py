@@ -53,10 +53,13 @@ E2E_SPP = 16   # samples per pixel per host-API render call in the end-to-end me
 PASS_LANES = 8   # sample passes in flight (spgpu_config.pass_lanes 0 = 8)
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the extend launches of the
 # per-kernel profile below (one pool, 8 samples per pixel, 1920x1080), averaged per
-# launch.  A constant: it is measured by the ncu command in
-# profiles/extend_traffic_stream_1080p.md and must be re-measured whenever the tree, the
-# traversal or the queue layout changes.
-EXTEND_DRAM_BYTES_PER_LAUNCH = 201.04e6
+# launch.  A constant, measured on a GB300 by
+#   ncu --nvtx --nvtx-include "spgpu_render_profile/" \
+#       --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
+#       --clock-control none -k regex:k_sextend -c 120 --csv --log-file <csv> \
+#       python bench.py --steps 4 --warmup 3 --no-cpu --no-micro --no-batch --no-guiding --no-e2e
+# and re-measured whenever the tree, the traversal or the queue layout changes.
+EXTEND_DRAM_BYTES_PER_LAUNCH = 201.28e6
 
 
 def max_over_ranks(torch, x: float, ws: int, device: str = "cuda") -> float:
