@@ -251,7 +251,7 @@ __device__ __forceinline__ bool traceWide(const WideNode *__restrict__ nodes, co
 // All 32 lanes of each warp execute every iteration of the loop (warp-uniform control),
 // so done() may use warp-collective operations.
 #ifndef SPGPU_REFILL
-#define SPGPU_REFILL 8
+#define SPGPU_REFILL 12
 #endif
 constexpr int kRefill = SPGPU_REFILL;
 // a finished ray's result waits for the warp's next refill, so that the finished lanes
