@@ -260,6 +260,11 @@ constexpr int kRefill = SPGPU_REFILL;
 #define SPGPU_DEFER_DONE 1
 #endif
 constexpr bool kDeferDone = SPGPU_DEFER_DONE != 0;
+// traversal steps between two looks at the warp's idle lanes
+#ifndef SPGPU_STEPS_PER_CHECK
+#define SPGPU_STEPS_PER_CHECK 2
+#endif
+constexpr int kStepsPerCheck = SPGPU_STEPS_PER_CHECK;
 
 template <bool ANY, bool STATS, class Fetch, class Done>
 __device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nodes,
@@ -312,9 +317,12 @@ __device__ __forceinline__ void tracePersistent(const WideNode *__restrict__ nod
             }
         }
         if (__all_sync(0xffffffffu, ray == -2)) break;
-        if (ray >= 0 && !finished) {
-            finished = laneStep<ANY, STATS>(L, nodes, tris, nNodes, nTris, stack, stride, spill, nodeCount,
-                                            triCount, overflow);
+#pragma unroll 1
+        for (int k = 0; k < kStepsPerCheck; k++) {
+            if (ray >= 0 && !finished) {
+                finished = laneStep<ANY, STATS>(L, nodes, tris, nNodes, nTris, stack, stride, spill, nodeCount,
+                                                triCount, overflow);
+            }
         }
     }
 }
