@@ -59,7 +59,7 @@ PASS_LANES = 8   # sample passes in flight (spgpu_config.pass_lanes 0 = 8)
 #       --clock-control none -k regex:k_sextend -c 120 --csv --log-file <csv> \
 #       python bench.py --steps 4 --warmup 3 --no-cpu --no-micro --no-batch --no-guiding --no-e2e
 # and re-measured whenever the tree, the traversal or the queue layout changes.
-EXTEND_DRAM_BYTES_PER_LAUNCH = 201.28e6
+EXTEND_DRAM_BYTES_PER_LAUNCH = 200.47e6
 
 
 def max_over_ranks(torch, x: float, ws: int, device: str = "cuda") -> float:
