@@ -480,12 +480,22 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks) k_sshadow(Stream
 
 // one thread: account the iteration, hand the continuations to the next one, reset the
 // per-iteration counters, raise the done flag once no path is left.  Batches also stamp
-// the completion time of every render whose paths have all ended, and set the device
-// loop's condition: another round while paths remain and the iteration limit is not
-// reached.
+// the completion time of every render whose paths have all ended (all the block's
+// threads, renders strided over them), and set the device loop's condition: another
+// round while paths remain and the iteration limit is not reached.
 template <bool BATCH>
 __global__ void k_sadvance(StreamArgs p) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0) return;
+    if constexpr (BATCH) {
+        // completion stamps, the renders strided over the block's threads
+        unsigned long long now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        for (int r = threadIdx.x; r < p.nRenders; r += blockDim.x) {
+            const unsigned long long paths = static_cast<unsigned long long>(p.pathStart[r + 1] - p.pathStart[r]);
+            if (p.times[1 + r] == 0 && atomicAdd(&p.ended[r], 0ull) == paths) atomicCAS(&p.times[1 + r], 0ull, now);
+        }
+    }
+    if (threadIdx.x != 0) return;
     const int nNew = newPaths(p);
     const int n = p.ctr[kCtrRays] + nNew;
     p.big[kBigStarted] += static_cast<unsigned long long>(nNew);
@@ -498,12 +508,6 @@ __global__ void k_sadvance(StreamArgs p) {
     const bool done = p.ctr[kCtrRays] == 0 && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p);
     p.ctr[kCtrDone] = done ? 1 : 0;
     if constexpr (BATCH) {
-        unsigned long long now;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
-        for (int r = 0; r < p.nRenders; r++) {
-            const unsigned long long paths = static_cast<unsigned long long>(p.pathStart[r + 1] - p.pathStart[r]);
-            if (p.times[1 + r] == 0 && atomicAdd(&p.ended[r], 0ull) == paths) atomicCAS(&p.times[1 + r], 0ull, now);
-        }
         const long long rounds = static_cast<long long>(++p.big[kBigRounds]);
         if (!done && rounds >= p.iterLimit) p.ctr[kCtrErr] |= 4;   // the pool did not drain in time
         if (p.devLoop) cudaGraphSetConditional(p.cond, !done && rounds < p.iterLimit ? 1u : 0u);
@@ -563,7 +567,7 @@ void launchIteration(const StreamArgs &a, const GridsS &g, cudaStream_t s, cudaE
     k_sshadow<STATS, BATCH><<<g.trace, kTraceBlock, 0, s>>>(a);
     done();
     mark(kSAdvance);
-    k_sadvance<BATCH><<<1, 32, 0, s>>>(a);
+    k_sadvance<BATCH><<<1, BATCH ? 256 : 32, 0, s>>>(a);
     done();
 }
 
