@@ -748,8 +748,10 @@ int streamBatchCreate(Ctx &C, StreamBatch **slot, const SceneView &merged, const
                       int poolSlots, int lanes, int iterations) {
     freeStreamBatch(*slot);
     *slot = nullptr;
-    if (renders.empty() || poolSlots <= 0 || lanes < 1 || lanes > Ctx::kPoolLanes || iterations < 1) {
-        setError("spgpu_batch_prepare: invalid streaming batch shape");
+    // a path carries its render in bits 9..30 of its meta word
+    if (renders.empty() || renders.size() >= (1u << 22) || poolSlots <= 0 || lanes < 1 || lanes > Ctx::kPoolLanes ||
+        iterations < 1) {
+        setError("spgpu_batch_prepare: invalid streaming batch shape (at most 2^22 - 1 renders)");
         return SPGPU_EINVAL;
     }
     auto *SB = new StreamBatch();
