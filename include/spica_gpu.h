@@ -229,7 +229,7 @@ int spgpu_render_host(spgpu_ctx *ctx, const spgpu_render_desc *desc, float *film
  *   SPGPU_BATCH_STREAM      the streaming wavefront over all renders of the batch: pools
  *                           of path slots refilled from one path sequence (render after
  *                           render), whose iteration loop runs on the device inside the
- *                           graph (a conditional while node);
+ *                           graph (a conditional while node); at most 2^22 - 1 renders;
  *   SPGPU_BATCH_PERSISTENT  one persistent megakernel pulling (render, pixel tile,
  *                           sample chunk) work items, each thread tracing whole paths.
  * autotune: 0 takes the streaming wavefront with its default pool (or, when `tuning` is
