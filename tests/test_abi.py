@@ -189,3 +189,38 @@ int main(int argc, char **argv) {
     assert r.returncode == 0, (r.returncode, r.stderr)
     assert r.stdout.split() == ["1", "1", "8", "6", "4"]
     assert (tmp_path / "o.hdr").read_bytes().startswith(b"#?RADIANCE")
+
+
+def test_python_mirrors_match_the_c_structs(tmp_path):
+    """Every ctypes mirror of a C-ABI struct has the C struct's size and field offsets
+    (compiled with the host C compiler from include/spica_gpu.h)."""
+    import ctypes
+    import subprocess
+    from spica_gb300 import gpu
+    pairs = [("spgpu_config", gpu.Config), ("spgpu_bvh_info", gpu.BVHInfo),
+             ("spgpu_trace_counters", gpu.TraceCounters), ("spgpu_render_desc", gpu.RenderDesc),
+             ("spgpu_render_stats", gpu.RenderStats), ("spgpu_kernel_profile", gpu.KernelProfile),
+             ("spgpu_batch_item", gpu.BatchItem), ("spgpu_batch_tuning", gpu.BatchTuning),
+             ("spgpu_guiding_config", gpu.GuidingConfig), ("spgpu_scene_file", gpu.SceneFile)]
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "spica_gpu.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, *_ in py._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    r = subprocess.run(["gcc", "-std=c99", "-I", inc, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        parts = line.split()
+        if len(parts) == 3:
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, py in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, *_ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
