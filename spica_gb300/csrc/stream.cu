@@ -75,7 +75,7 @@ constexpr int kNumCtr = 16;
 // call: [8] paths of the render (spp * npix), [9] sample offset (batches: the lane's
 // first path of the batch's sequence), [10] film address; [11] iterations run (batches)
 enum : int { kBigStarted = 0, kBigPaths, kBigClosest, kBigShadow, kBigVisit, kBigTotal = 8, kBigOffset, kBigFilm,
-             kBigRounds };
+             kBigIters };
 constexpr int kNumBig = 12;
 
 // a path's depth (bits 0..7), specular flag (bit 8) and, in batches, its render (bits
@@ -508,9 +508,9 @@ __global__ void k_sadvance(StreamArgs p) {
     const bool done = p.ctr[kCtrRays] == 0 && static_cast<long long>(p.big[kBigStarted]) >= totalPaths(p);
     p.ctr[kCtrDone] = done ? 1 : 0;
     if constexpr (BATCH) {
-        const long long rounds = static_cast<long long>(++p.big[kBigRounds]);
-        if (!done && rounds >= p.iterLimit) p.ctr[kCtrErr] |= 4;   // the pool did not drain in time
-        if (p.devLoop) cudaGraphSetConditional(p.cond, !done && rounds < p.iterLimit ? 1u : 0u);
+        const long long iters = static_cast<long long>(++p.big[kBigIters]);
+        if (!done && iters >= p.iterLimit) p.ctr[kCtrErr] |= 4;   // the pool did not drain in time
+        if (p.devLoop) cudaGraphSetConditional(p.cond, !done && iters < p.iterLimit ? 1u : 0u);
     }
 }
 
@@ -730,7 +730,6 @@ struct StreamBatch {
     std::vector<long long> hostStart;
     cudaGraphExec_t exec = nullptr;
     float4 *execFilm = nullptr;
-    long long rounds[Ctx::kPoolLanes] = {};
 };
 
 void freeStreamBatch(StreamBatch *SB) {
@@ -917,7 +916,7 @@ int streamBatchRun(Ctx &C, StreamBatch &SB, float4 *film, double *renderMs, unsi
         statsOut[0] += big[k][kBigPaths];
         statsOut[1] += big[k][kBigClosest];
         statsOut[2] += big[k][kBigShadow];
-        statsOut[3] += big[k][kBigRounds] * kSNumClasses + 1;
+        statsOut[3] += big[k][kBigIters] * kSNumClasses + 1;
         err |= ctr[k][kCtrErr];
         drained = drained && ctr[k][kCtrDone];
     }
